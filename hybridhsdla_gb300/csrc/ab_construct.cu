@@ -1,0 +1,285 @@
+// Kernel (a): FLAPW matching tensors A, B on the GPU in FP64.
+//
+// Restates construct_AB (flapw_opt/src/tensor_AB_match.cpp:63-129): for every
+// G vector, atom j, l, m
+//
+//   A = conj(Y_lm(R_j^T K^)) 4pi/sqrt(Omega) e^{i 2pi K.tau_j} / W_lj [udot_l |K| j_l'(|K|R) - udot'_l j_l(|K|R)]
+//   B = (same prefactor)                                              [-u_l |K| j_l'(|K|R) + u'_l j_l(|K|R)]
+//
+// with K = k + G, |K| = |bmat K| (types_helper.cpp:33) and j_l, j_l' from the
+// sphbes/dsphbs recurrences (external/compat/fleur/sphbes.f:19-76,
+// dsphbs.f:24-42), Y_lm from ylm4 (external/compat/fleur/ylm4.f:4-139).
+//
+// GB300 mapping: one CTA per G column (grid-strided).  Everything that does not
+// depend on the atom is hoisted out of the per-atom loop (Bessel values per
+// type, Y_lm per G when no atom carries its own rotation, the phase per atom),
+// then the whole 2*L*a column is written with consecutive threads on
+// consecutive 16-byte elements (coalesced, full 32-byte sectors).  Output
+// layout: rows ordered per atom as [A_a (L rows); B_a (L rows)], so that the
+// stacked contraction operand [A;B] is one column-major matrix.
+#include "common.cuh"
+
+namespace hsdla {
+namespace {
+
+// sphbes.f:19-76 (REAL = double).  fj[0..lmax].
+__device__ void sphbes_dev(int lmax, double x, double *fj) {
+    const double small = 1.0e-3;
+    const double xx = x * x;
+    if (x >= small) {
+        const double xinv = 1.0 / x;
+        double sn, cs;
+        sincos(x, &sn, &cs);
+        fj[0] = sn * xinv;
+        fj[1] = (fj[0] - cs) * xinv;
+        if ((double)lmax < x) {
+            for (int l = 2; l <= lmax; ++l) fj[l] = (2 * l - 1) * xinv * fj[l - 1] - fj[l - 2];
+        } else if (lmax >= 2) {
+            // Miller's downward recursion from n = int(lmax + 10 + x); only aux[0..lmax] is kept
+            const int n = (int)(lmax + 10 + x);
+            double aux[kMaxLmax + 1];
+            double a_next = 0.0;   // aux(i+1)
+            double a_cur = 1.0;    // aux(i), i = n-1
+            for (int i = n - 1; i >= 1; --i) {
+                const double a_prev = (2 * i + 1) * xinv * a_cur - a_next;
+                if (i - 1 <= lmax) aux[i - 1] = a_prev;
+                a_next = a_cur;
+                a_cur = a_prev;
+            }
+            const int mn = (fabs(fj[0]) < fabs(fj[1])) ? 1 : 0;
+            const double quot = fj[mn] / aux[mn];
+            for (int l = 2; l <= lmax; ++l) fj[l] = aux[l] * quot;
+        }
+    } else {
+        fj[0] = 1.0 - xx / 6.0 * (1.0 - xx / 20.0 * (1.0 - xx / 42.0));
+        fj[1] = (x / 3.0) * (1.0 - xx / 10.0 * (1.0 - xx / 28.0));
+        double fac = xx / 15.0;
+        for (int l = 2; l <= lmax; ++l) {
+            fj[l] = fac * (1.0 - xx / (4 * l + 6));
+            fac = x * fac / (2 * l + 3);
+        }
+    }
+}
+
+// dsphbs.f:24-42
+__device__ void dsphbs_dev(int lmax, double x, const double *fj, double *dfj) {
+    const double xlim = 1.0e-4;
+    dfj[0] = -fj[1];
+    if (x < xlim) {
+        const double x2 = 0.5 * x * x;
+        double fac = 1.0 / 3.0;
+        for (int l = 1; l <= lmax; ++l) {
+            dfj[l] = fac * (l - x2 * (l + 2) / (2 * l + 3));
+            fac = x * fac / (2 * l + 3);
+        }
+    } else {
+        for (int l = 1; l <= lmax; ++l) dfj[l] = fj[l - 1] - (l + 1) * fj[l] / x;
+    }
+}
+
+// ylm4.f:45-105 for one m (called by thread m = 0..lmax); writes ylm[l(l+1) +- m].
+__device__ void ylm_column_dev(int lmax, int m, const double *v, const double *ynorm, double2 *ylm) {
+    const double small = 1.0e-12;
+    const double x = v[0], y = v[1], z = v[2];
+    const double xy = x * x + y * y;
+    const double r = sqrt(xy + z * z);
+    const double rxy = sqrt(xy);
+    double cth, sth, cph, sph;
+    if (r > small) { cth = z / r; sth = rxy / r; } else { sth = 0.0; cth = 1.0; }
+    if (rxy > small) { cph = x / rxy; sph = y / rxy; } else { cph = 1.0; sph = 0.0; }
+    // the reference runs one sequential fac recursion over m; thread m replays its prefix
+    double fac = 1.0;
+    for (int mm = 0; mm < m; ++mm) {
+        fac = (double)(-(mm + mm - 1)) * fac;
+        fac = fac * sth;
+    }
+    double p[kMaxLmax + 1];   // p(l, m) for l = m..lmax
+    if (m < lmax) {
+        fac = (double)(-(m + m - 1)) * fac;
+        p[m] = fac;
+        p[m + 1] = (m + m + 1) * cth * fac;
+        for (int l = m + 2; l <= lmax; ++l)
+            p[l] = ((l + l - 1) * cth * p[l - 1] - (l + m - 1) * p[l - 2]) / (l - m);
+    } else {
+        p[m] = (double)(-(lmax + lmax - 1)) * fac;
+    }
+    // cos(m phi), sin(m phi) by the reference's recursion
+    double c0 = 1.0, s0 = 0.0, c1 = cph, s1 = sph;
+    double cm = (m == 0) ? c0 : c1, sm = (m == 0) ? s0 : s1;
+    const double cph2 = cph + cph;
+    for (int mm = 2; mm <= m; ++mm) {
+        const double s2 = cph2 * s1 - s0, c2 = cph2 * c1 - c0;
+        s0 = s1; c0 = c1; s1 = s2; c1 = c2;
+        sm = s2; cm = c2;
+    }
+    for (int l = m; l <= lmax; ++l) {
+        const int lm0 = l * (l + 1);
+        if (m == 0) {
+            ylm[lm0] = make_double2(ynorm[lm0] * p[l], 0.0);
+        } else {
+            const double yr = p[l] * cm, yi = p[l] * sm;
+            ylm[lm0 + m] = make_double2(ynorm[lm0 + m] * yr, ynorm[lm0 + m] * yi);
+            ylm[lm0 - m] = make_double2(yr * ynorm[lm0 - m], -yi * ynorm[lm0 - m]);
+        }
+    }
+}
+
+constexpr int kThreads = 256;
+constexpr int kRotChunk = 16;   // atoms whose Y_lm sets are staged together when atoms carry rotations
+
+__device__ __forceinline__ double2 cmul(double2 a, double2 b) {
+    return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+
+template <bool kRot>
+__global__ void __launch_bounds__(kThreads) construct_ab_kernel(DevSystem sys, DevKpoint kp, double2 *C,
+                                                                int64_t ldc) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int L = sys.L, nl = sys.max_lmax + 1, na = sys.num_atoms, nt = sys.num_types;
+    const int twoL = 2 * L;
+    double *au = reinterpret_cast<double *>(smem_raw);           // [nt*nl]
+    double *bu = au + nt * nl;                                     // [nt*nl]
+    double2 *vph = reinterpret_cast<double2 *>(bu + nt * nl);     // [na] vol_prefac * phase
+    double2 *ylm = vph + na;                                       // [L] or [kRotChunk*L]
+    unsigned char *l_of = reinterpret_cast<unsigned char *>(ylm + (kRot ? kRotChunk : 1) * L);  // [L]
+    __shared__ double kvec[3];
+    __shared__ double knorm;
+
+    for (int lm = threadIdx.x; lm < L; lm += blockDim.x) {
+        int l = (int)sqrt((double)lm);
+        while (l * l > lm) --l;
+        while ((l + 1) * (l + 1) <= lm) ++l;
+        l_of[lm] = (unsigned char)l;
+    }
+    for (int64_t gi = blockIdx.x; gi < kp.n_g; gi += gridDim.x) {
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            const int32_t *gv = kp.g + 3 * gi;
+            double K[3] = {kp.k[0] + gv[0], kp.k[1] + gv[1], kp.k[2] + gv[2]};
+            double s = 0.0;
+            for (int r = 0; r < 3; ++r) {
+                const double t = sys.bmat[3 * r] * K[0] + sys.bmat[3 * r + 1] * K[1] + sys.bmat[3 * r + 2] * K[2];
+                s += t * t;
+            }
+            kvec[0] = K[0]; kvec[1] = K[1]; kvec[2] = K[2];
+            knorm = sqrt(s);
+        }
+        __syncthreads();
+        const double K0 = kvec[0], K1 = kvec[1], K2 = kvec[2], kn = knorm;
+        // Bessel values per type (calc_bessel at R_t |K| for max_lmax, tensor_AB_match.cpp:104)
+        for (int t = threadIdx.x; t < nt; t += blockDim.x) {
+            double fj[kMaxLmax + 1], dfj[kMaxLmax + 1];
+            const double x = sys.type_rmt[t] * kn;
+            sphbes_dev(sys.max_lmax, x, fj);
+            dsphbs_dev(sys.max_lmax, x, fj, dfj);
+            for (int l = 0; l < nl; ++l) {
+                const int tl = t * nl + l;
+                au[tl] = sys.dE_u[tl] * kn * dfj[l] - sys.dE_u_dr[tl] * fj[l];
+                bu[tl] = -sys.u[tl] * kn * dfj[l] + sys.u_dr[tl] * fj[l];
+            }
+        }
+        // structure phase per atom, premultiplied by 4 pi / sqrt(Omega)
+        for (int j = threadIdx.x; j < na; j += blockDim.x) {
+            const double *p = sys.atom_pos + 3 * j;
+            const double arg = 2 * kPi * (K0 * p[0] + K1 * p[1] + K2 * p[2]);
+            double sn, cs;
+            sincos(arg, &sn, &cs);
+            vph[j] = make_double2(sys.vol_prefac * cs, sys.vol_prefac * sn);
+        }
+        if (!kRot) {
+            // K_base = normalise(bmat^T K): every atom shares R = bmat
+            if (threadIdx.x <= sys.max_lmax) {
+                double v[3];
+                for (int c = 0; c < 3; ++c)
+                    v[c] = sys.bmat[c] * K0 + sys.bmat[3 + c] * K1 + sys.bmat[6 + c] * K2;
+                const double nrm = sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+                if (nrm > 0.0) { v[0] /= nrm; v[1] /= nrm; v[2] /= nrm; }
+                ylm_column_dev(sys.max_lmax, threadIdx.x, v, sys.ynorm, ylm);
+            }
+            __syncthreads();
+            double2 *col = C + ldc * gi;
+            const int64_t nrow = (int64_t)twoL * na;
+            for (int64_t idx = threadIdx.x; idx < nrow; idx += blockDim.x) {
+                const int j = (int)(idx / twoL);
+                const int r = (int)(idx - (int64_t)j * twoL);
+                const bool isB = r >= L;
+                const int lm = isB ? r - L : r;
+                const int l = l_of[lm];
+                const int t = sys.atom_type[j];
+                double2 out = make_double2(0.0, 0.0);
+                if (l <= sys.type_lmax[t]) {
+                    const int tl = t * nl + l;
+                    const double2 common = make_double2(vph[j].x * sys.inv_w[tl], vph[j].y * sys.inv_w[tl]);
+                    const double2 y = ylm[lm];
+                    const double2 yc = make_double2(y.x, -y.y);
+                    const double2 ycc = cmul(yc, common);
+                    const double f = isB ? bu[tl] : au[tl];
+                    out = make_double2(ycc.x * f, ycc.y * f);
+                }
+                col[idx] = out;
+            }
+        } else {
+            for (int j0 = 0; j0 < na; j0 += kRotChunk) {
+                const int nj = min(kRotChunk, na - j0);
+                __syncthreads();
+                for (int w = threadIdx.x; w < nj * nl; w += blockDim.x) {
+                    const int jj = w / nl, m = w - jj * nl;
+                    const double *R = sys.atom_rotmat + 9 * (j0 + jj);
+                    double v[3];
+                    for (int c = 0; c < 3; ++c) v[c] = R[c] * K0 + R[3 + c] * K1 + R[6 + c] * K2;
+                    const double nrm = sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+                    if (nrm > 0.0) { v[0] /= nrm; v[1] /= nrm; v[2] /= nrm; }
+                    ylm_column_dev(sys.max_lmax, m, v, sys.ynorm, ylm + jj * L);
+                }
+                __syncthreads();
+                double2 *col = C + ldc * gi + (int64_t)twoL * j0;
+                const int nrow = twoL * nj;
+                for (int idx = threadIdx.x; idx < nrow; idx += blockDim.x) {
+                    const int jj = idx / twoL;
+                    const int r = idx - jj * twoL;
+                    const int j = j0 + jj;
+                    const bool isB = r >= L;
+                    const int lm = isB ? r - L : r;
+                    const int l = l_of[lm];
+                    const int t = sys.atom_type[j];
+                    double2 out = make_double2(0.0, 0.0);
+                    if (l <= sys.type_lmax[t]) {
+                        const int tl = t * nl + l;
+                        const double2 common = make_double2(vph[j].x * sys.inv_w[tl], vph[j].y * sys.inv_w[tl]);
+                        const double2 y = ylm[jj * L + lm];
+                        const double2 yc = make_double2(y.x, -y.y);
+                        const double2 ycc = cmul(yc, common);
+                        const double f = isB ? bu[tl] : au[tl];
+                        out = make_double2(ycc.x * f, ycc.y * f);
+                    }
+                    col[idx] = out;
+                }
+            }
+        }
+    }
+}
+
+}  // namespace
+
+cudaError_t launch_construct_ab(const DevSystem &sys, const DevKpoint &kp, double2 *C, int64_t ldc,
+                                cudaStream_t st) {
+    const bool rot = sys.atom_rotmat != nullptr;
+    const int nl = sys.max_lmax + 1;
+    size_t smem = sizeof(double) * 2 * sys.num_types * nl + sizeof(double2) * sys.num_atoms +
+                  sizeof(double2) * (rot ? kRotChunk : 1) * sys.L + sys.L + 16;
+    smem = (smem + 15) & ~size_t(15);
+    int dev = 0, nsm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    const int64_t grid = std::min<int64_t>(kp.n_g, (int64_t)nsm * 8);
+    if (rot) {
+        cudaFuncSetAttribute(construct_ab_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        construct_ab_kernel<true><<<(unsigned)grid, kThreads, smem, st>>>(sys, kp, C, ldc);
+    } else {
+        cudaFuncSetAttribute(construct_ab_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        construct_ab_kernel<false><<<(unsigned)grid, kThreads, smem, st>>>(sys, kp, C, ldc);
+    }
+    return cudaGetLastError();
+}
+
+}  // namespace hsdla

@@ -1,0 +1,66 @@
+// Shared definitions of the sm_103a H/S generation library.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/hsdla.h"
+
+namespace hsdla {
+
+constexpr int kMaxLmax = 14;                 // (14+1)^2 = 225 lm per atom
+constexpr int kMaxL = (kMaxLmax + 1) * (kMaxLmax + 1);
+constexpr int kMaxTypes = 64;
+constexpr double kPi = 3.14159265358979323846;
+
+// Device error word: kernels with bounded waits write a code here instead of trapping.
+enum DeviceError : int {
+    kDevOk = 0,
+    kDevTimeout = 1,
+    kDevBadInput = 2,
+};
+
+// ------------------------------------------------------------------ system
+// Device-resident per-run data (uploaded once per plan).
+struct DevSystem {
+    int num_atoms, num_types, max_lmax, L;
+    double vol_prefac;          // 4 pi / sqrt(Omega)
+    double bmat[9];             // row-major rows b_i
+    const int32_t *atom_type;   // [a]
+    const double *atom_pos;     // [a][3]
+    const double *atom_rotmat;  // [a][9] or nullptr
+    const double *type_rmt;     // [t]
+    const int32_t *type_lmax;   // [t]
+    // per (type, l), index t*(max_lmax+1)+l
+    const double *u, *u_dr, *dE_u, *dE_u_dr;
+    const double *inv_w;        // 1 / (udot u' - u udot')
+    const double *ynorm;        // [L] Y_lm normalisation (ylm4.f:111-137)
+};
+
+struct DevKpoint {
+    double k[3];
+    int64_t n_g;
+    const int32_t *g;           // [n_g][3]
+};
+
+// ----------------------------------------------------------- kernels (host)
+// (a) matching tensors of one k-point into C: (2 L a) x n_g column-major, per-atom [A_a; B_a]
+cudaError_t launch_construct_ab(const DevSystem &sys, const DevKpoint &kp, double2 *C, int64_t ldc,
+                                cudaStream_t st);
+
+// FP64 tiled contraction OUT = P^H diag(w) Q over a batch of jobs (kernels (b) and (c) in FP64).
+struct Fp64Job {
+    const double2 *P; int64_t ldp;   // k x m
+    const double2 *Q; int64_t ldq;   // k x n
+    const double *w;                 // k weights or nullptr
+    double2 *out; int64_t ldo;       // m x n
+    int64_t m, n, k;
+    int32_t lower;                   // 1: only elements with row >= col (m == n required)
+    int32_t tiles_n;                 // tile columns of this job
+    int64_t tile_begin;              // first global tile index of this job
+};
+constexpr int kFp64Tile = 64;
+int64_t fp64_job_tiles(const Fp64Job &j);
+cudaError_t launch_fp64_jobs(const Fp64Job *d_jobs, int num_jobs, int64_t total_tiles, cudaStream_t st);
+
+}  // namespace hsdla

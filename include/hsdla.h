@@ -1,0 +1,170 @@
+/*
+ * hsdla.h -- C ABI of the GB300 (sm_103a) FLAPW Hamiltonian/overlap generator.
+ *
+ * Drop-in boundary for the H/S generation step of HybridHSDLA.  The reference
+ * entry point is
+ *
+ *   double create_HS2(const arma::vec3& kpt, double kmax, const arma::mat33& bmat,
+ *                     const arma::imat& g_mesh, const AtomData& ad, GenMethod method,
+ *                     arma::cx_mat& H, arma::cx_mat& S)
+ *   (flapw_opt/src/h_and_s.cpp:591-893, STRIPPED build; called once per k-point
+ *    from generate_matrices, flapw_opt/src/h_and_s.cpp:919)
+ *
+ * which builds the matching tensors A, B (tensor_AB_match.cpp:63-129), applies
+ * the per-atom T matrices and forms the lower triangles of
+ *
+ *   S = sum_a A_a^H A_a + B_a^H U_a B_a
+ *   H = sum_a [A_a;B_a]^H [[T_AA, T_AB],[T_AB^H, T_BB]]_a [A_a;B_a]
+ *
+ * (h_and_s_stripped_v2.cpp:100-382).  Here the same quantities are passed as
+ * plain arrays; everything runs on one GPU; there is no CPU fallback.  All
+ * functions return HSDLA_OK (0) or a negative status; no function exits or
+ * aborts.  Complex numbers are (re, im) pairs of doubles, layout-compatible
+ * with std::complex<double> and Fortran double complex.
+ *
+ * Conventions (identical to the reference):
+ *   - bmat: 3x3 row-major, row i = reciprocal basis vector b_i (bohr^-1, incl. 2 pi);
+ *   - k-points and atom positions in fractional coordinates;
+ *   - r_K = |bmat (k+G)| (types_helper.cpp:33), direction R^T (k+G) with
+ *     R = mrot bmat per atom (tensor_AB_match.cpp:97, FleurData.cpp:453-455);
+ *   - lm index = l(l+1)+m, L = (max_lmax+1)^2;
+ *   - H, S: n_G x n_G column-major with leading dimension ld; only the lower
+ *     triangle (row >= column) is written, the upper triangle is left untouched.
+ */
+#ifndef HSDLA_H
+#define HSDLA_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct hsdla_cx { double re, im; } hsdla_cx;
+
+/* status codes */
+enum {
+    HSDLA_OK = 0,
+    HSDLA_ERR_ARG = -1,        /* invalid argument (null pointer, bad size, bad ld) */
+    HSDLA_ERR_CUDA = -2,       /* a CUDA runtime call failed */
+    HSDLA_ERR_NOMEM = -3,      /* device or pinned allocation failed or exceeds the cap */
+    HSDLA_ERR_INPUT = -4,      /* non-finite input, zero Wronskian, non-Hermitian T */
+    HSDLA_ERR_TIMEOUT = -5,    /* a bounded device-side wait expired (kernel error word) */
+    HSDLA_ERR_UNSUPPORTED = -6,/* size or option outside what this build supports */
+    HSDLA_ERR_DEVICE = -7      /* no usable sm_103a device */
+};
+
+/* precision of the H/S contractions */
+enum {
+    HSDLA_PREC_FP64 = 0,       /* plain FP64 (DMMA) */
+    HSDLA_PREC_OZAKI_FP8 = 1   /* Ozaki split: e4m3 integer digits on tcgen05, FP64 recombination */
+};
+
+/* One FLAPW cell: what the reference's AtomData holds (flapw_opt/src/include/AtomData.h:16-41),
+ * stored per type with an atom->type map instead of per-atom replication
+ * (FleurData.cpp:52-62 replicates per atom). */
+typedef struct hsdla_system {
+    int32_t num_atoms;
+    int32_t num_types;
+    int32_t max_lmax;            /* L = (max_lmax+1)^2 */
+    int32_t reserved0;
+    double vol_cell;             /* det(real basis), bohr^3 */
+    double bmat[9];              /* row-major, rows = reciprocal vectors */
+    const int32_t *atom_type;    /* [num_atoms], 0-based */
+    const double *atom_pos;      /* [num_atoms][3] fractional */
+    const double *atom_rotmat;   /* [num_atoms][9] row-major (mrot * bmat), or NULL: mrot = 1 */
+    const double *type_rmt;      /* [num_types] muffin-tin radius */
+    const int32_t *type_lmax;    /* [num_types] spherical cutoff, 1 <= lmax <= max_lmax */
+    const double *type_u;        /* [num_types][max_lmax+1] u_l(R)      */
+    const double *type_u_dr;     /* [num_types][max_lmax+1] u_l'(R)     */
+    const double *type_dE_u;     /* [num_types][max_lmax+1] udot_l(R)   */
+    const double *type_dE_u_dr;  /* [num_types][max_lmax+1] udot_l'(R)  */
+    const double *type_dE_u_norm;/* [num_types][max_lmax+1] ||udot_l||^2 */
+    const hsdla_cx *type_t_aa;   /* [num_types][L*L] augmented T_AA, column-major, Hermitian */
+    const hsdla_cx *type_t_ab;   /* [num_types][L*L] augmented T_AB, column-major (T_BA = T_AB^H) */
+    const hsdla_cx *type_t_bb;   /* [num_types][L*L] augmented T_BB, column-major, Hermitian */
+} hsdla_system;
+
+/* One k-point and its basis (the k_mesh of types.h:14-21; G list from the caller). */
+typedef struct hsdla_kpoint {
+    double k[3];                 /* fractional */
+    int64_t n_g;                 /* number of G vectors (>= 1) */
+    const int32_t *g;            /* [n_g][3] integer G vectors */
+} hsdla_kpoint;
+
+typedef struct hsdla_opts {
+    int32_t precision;           /* HSDLA_PREC_* */
+    int32_t num_slices;          /* Ozaki digit slices; 0 = autotune to the accuracy target */
+    double target_rel_err;       /* Ozaki accuracy target (default 1e-13 when 0) */
+    int32_t use_graph;           /* 1 = capture the whole multi-k-point pipeline in a CUDA graph */
+    int32_t reserved[7];
+} hsdla_opts;
+
+typedef struct hsdla_report {
+    double ms_total;             /* device time of the whole call (CUDA events) */
+    double ms_per_kpoint;
+    double flop;                 /* canonical 20 G^2 La + 24 L^2 a G, summed over k-points */
+    double eff_tflops;           /* flop / ms_total */
+    double ms_construct_ab;      /* stage times of the last un-graphed run (0 under a graph) */
+    double ms_tapply;
+    double ms_contract;
+    int32_t num_slices;          /* slices used (Ozaki) */
+    int32_t num_kpoints;
+    int32_t kernel_launches;     /* kernels launched per execution */
+    int32_t reserved[5];
+} hsdla_report;
+
+typedef struct hsdla_context hsdla_context;
+typedef struct hsdla_plan hsdla_plan;
+
+/* Library / device set-up (replaces dev_init/dev_finalize, flapw_opt/src/wrappers.cpp:111-148). */
+int hsdla_context_create(int device, hsdla_context **ctx);
+void hsdla_context_destroy(hsdla_context *ctx);
+const char *hsdla_last_error(const hsdla_context *ctx);
+/* Cap on device bytes the context may allocate (0 = no cap); exceeding it returns HSDLA_ERR_NOMEM. */
+int hsdla_set_mem_cap(hsdla_context *ctx, int64_t bytes);
+
+/* T-matrix preparation for one type: TMat::TMat + zero_nonsph + augment_tmats
+ * (flapw_opt/src/types_helper.cpp:41-90, flapw_opt/src/AtomData.cpp:95-145).
+ * taa, tbb, tab, tba: n x n column-major with n = (lmax+1)^2, only lower triangles
+ * read (Fleur's dump convention).  Outputs: n x n column-major augmented aa, ab, bb.
+ * Host-only, once per run. */
+int hsdla_prepare_tmat(int32_t lmax, int32_t lmax_nonsph, const hsdla_cx *taa, const hsdla_cx *tbb,
+                       const hsdla_cx *tab, const hsdla_cx *tba, const double *E_l,
+                       const double *dE_u_norm, hsdla_cx *aa, hsdla_cx *ab, hsdla_cx *bb);
+
+/* H and S for nk k-points, HOST buffers in and out (the create_HS2 drop-in; nk = 1 is
+ * exactly create_HS2's contract, h_and_s.cpp:591-893).  H[i], S[i]: n_g(i) x n_g(i)
+ * column-major host arrays with leading dimension ld[i] >= n_g(i). */
+int hsdla_create_hs(hsdla_context *ctx, const hsdla_system *sys, const hsdla_kpoint *kpts, int32_t nk,
+                    hsdla_cx *const *H, hsdla_cx *const *S, const int64_t *ld,
+                    const hsdla_opts *opts, hsdla_report *report);
+
+/* Device-resident execution: a plan uploads the system and the k-point lists once and owns
+ * the device workspace (A/B tensors, T blocks, digit slices). */
+int hsdla_plan_create(hsdla_context *ctx, const hsdla_system *sys, const hsdla_kpoint *kpts, int32_t nk,
+                      const hsdla_opts *opts, hsdla_plan **plan);
+/* dH[i], dS[i]: DEVICE pointers; stream: a cudaStream_t or NULL for the context stream. */
+int hsdla_plan_execute(hsdla_plan *plan, hsdla_cx *const *dH, hsdla_cx *const *dS, const int64_t *ld,
+                       void *stream, hsdla_report *report);
+int64_t hsdla_plan_workspace_bytes(const hsdla_plan *plan);
+void hsdla_plan_destroy(hsdla_plan *plan);
+
+/* ---- component entry points (parity tests; the fused pipeline does not call these) ---- */
+
+/* Kernel (a): matching tensors for k-point ik of a plan into a DEVICE buffer C of
+ * (2 L a) x n_g complex, column-major, rows ordered per atom as [A_a (L rows); B_a (L rows)]
+ * (the reference's A(lm, a, g) is C[2 L a + lm, g], B(lm, a, g) is C[2 L a + L + lm, g]). */
+int hsdla_plan_construct_ab(hsdla_plan *plan, int32_t ik, hsdla_cx *dC, void *stream);
+
+/* Kernel (c) standalone: lower triangle of OUT = P^H diag(w) Q for K x n column-major device
+ * matrices (the dev_zherk_/dev_zherkx_ plugin of flapw_opt/src/include/acc/wrappers.h:19-28
+ * with uplo 'L', trans 'C', alpha 1, beta 0).  w may be NULL (all ones).  Q == P gives zherk. */
+int hsdla_zherkx_lower(hsdla_context *ctx, int32_t precision, int32_t num_slices, int64_t n, int64_t k,
+                       const hsdla_cx *dP, int64_t ldp, const hsdla_cx *dQ, int64_t ldq,
+                       const double *dw, hsdla_cx *dOut, int64_t ldo, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* HSDLA_H */
