@@ -398,8 +398,6 @@ int hsdla_plan_create(hsdla_context *ctx, const hsdla_system *s, const hsdla_kpo
         build_tfull(s, t, L, tf);
         std::copy(tf.begin(), tf.end(), tf_all.begin() + (size_t)t * 4 * L * L);
     }
-    int64_t ng_total = 0;
-    for (int i = 0; i < nk; ++i) ng_total += kpts[i].n_g;
 
     // ---- one device block for all tables
     int64_t bytes = 0;
@@ -410,7 +408,7 @@ int hsdla_plan_create(hsdla_context *ctx, const hsdla_system *s, const hsdla_kpo
     add(sizeof(double) * L);
     add(sizeof(double2) * tf_all.size());
     add(sizeof(double) * pl->twoLa); add(sizeof(double) * pl->twoLa);
-    add(sizeof(int32_t) * 3 * std::max<int64_t>(ng_total, 1));
+    for (int i = 0; i < nk; ++i) add(sizeof(int32_t) * 3 * kpts[i].n_g);
     rc = ctx_malloc(ctx, &pl->tables, bytes);
     if (rc) { delete pl; return rc; }
     pl->tables_bytes = bytes;
@@ -471,7 +469,8 @@ int64_t hsdla_plan_workspace_bytes(const hsdla_plan *pl) {
     int64_t ngmax = 0;
     for (auto &k : pl->kps) ngmax = std::max(ngmax, k.n_g);
     int64_t b = 2 * (int64_t)sizeof(double2) * pl->twoLa * ngmax;   // C and X
-    if (pl->opts.precision == HSDLA_PREC_OZAKI_FP8) b += ozaki_workspace_bytes(pl->oz, pl->twoLa, ngmax);
+    if (pl->opts.precision == HSDLA_PREC_OZAKI_FP8)
+        b += ozaki_pipeline_workspace(pl->oz.num_slices, 2 * (int64_t)pl->L, pl->na, pl->nt, ngmax);
     return b;
 }
 
@@ -482,6 +481,7 @@ void hsdla_plan_destroy(hsdla_plan *pl) {
     cudaStreamSynchronize(ctx->stream);
     if (pl->d_jobs) ctx_free(ctx, pl->d_jobs, pl->jobs_cap * sizeof(Fp64Job));
     if (pl->tables) ctx_free(ctx, pl->tables, pl->tables_bytes);
+    ozaki_plan_release(pl->oz);
     delete pl;
 }
 
@@ -538,6 +538,7 @@ int hsdla_plan_execute(hsdla_plan *pl, hsdla_cx *const *dH, hsdla_cx *const *dS,
             jb.m = twoL; jb.n = G; jb.k = twoL; jb.lower = 0;
             pl->h_jobs.push_back(jb);
         }
+        if (pl->opts.precision != HSDLA_PREC_FP64) pl->h_jobs.clear();   // the Ozaki pipeline emulates (b) too
         const int64_t nt_b = assign_tiles(pl->h_jobs, 0);
         const size_t nb = pl->h_jobs.size();
         // (c) S and H lower triangles
@@ -552,18 +553,23 @@ int hsdla_plan_execute(hsdla_plan *pl, hsdla_cx *const *dH, hsdla_cx *const *dS,
             pl->h_jobs.push_back(jh);
         }
         const int64_t nt_c = assign_tiles(pl->h_jobs, nb);
-        rc = upload_jobs(pl, st);
-        if (rc) return rc;
-        CUDA_TRY(ctx, launch_fp64_jobs(pl->d_jobs, (int)nb, nt_b, st));
-        pl->launches++;
+        if (!pl->h_jobs.empty()) {
+            rc = upload_jobs(pl, st);
+            if (rc) return rc;
+            CUDA_TRY(ctx, launch_fp64_jobs(pl->d_jobs, (int)nb, nt_b, st));
+            pl->launches++;
+        }
         CUDA_TRY(ctx, cudaEventRecord(ctx->evs[2], st));
         if (pl->opts.precision == HSDLA_PREC_FP64) {
             CUDA_TRY(ctx, launch_fp64_jobs(pl->d_jobs + nb, (int)(pl->h_jobs.size() - nb), nt_c, st));
             pl->launches++;
         } else {
             int nl = 0;
-            rc = ozaki_contract(pl->oz, C, X, pl->wsqrt, twoLa, G, reinterpret_cast<double2 *>(dS[i]),
-                                reinterpret_cast<double2 *>(dH[i]), ld[i], oz_ws, st, &nl);
+            OzakiInputs in;
+            in.C = C; in.Tfull = pl->Tfull; in.w = pl->w; in.atom_type = pl->atom_type.data(); in.X = X;
+            in.twoL = twoL; in.na = pl->na; in.nt = pl->nt; in.G = G;
+            rc = ozaki_pipeline(pl->oz, in, reinterpret_cast<double2 *>(dS[i]), reinterpret_cast<double2 *>(dH[i]),
+                                ld[i], oz_ws, st, &nl);
             if (rc) return set_err(ctx, rc, "Ozaki contraction failed: %s", ozaki_last_error());
             pl->launches += nl;
         }
@@ -693,15 +699,16 @@ int hsdla_zherkx_lower(hsdla_context *ctx, int32_t precision, int32_t num_slices
         int rc = ozaki_plan_init(oz, num_slices, 1e-13);
         if (rc) return set_err(ctx, rc, "bad slice count");
         void *ws = nullptr;
-        rc = ctx_workspace(ctx, ozaki_workspace_bytes(oz, k, n), &ws);
+        rc = ctx_workspace(ctx, ozaki_herkx_workspace(oz.num_slices, k, n), &ws);
         if (rc) return rc;
         int nl = 0;
         rc = ozaki_herkx(oz, reinterpret_cast<const double2 *>(dP), ldp, reinterpret_cast<const double2 *>(dQ), ldq,
                          dw, k, n, reinterpret_cast<double2 *>(dOut), ldo, ws, st, &nl);
-        if (rc) return set_err(ctx, rc, "Ozaki zherkx failed: %s", ozaki_last_error());
+        if (rc) { ozaki_plan_release(oz); return set_err(ctx, rc, "Ozaki zherkx failed: %s", ozaki_last_error()); }
         cudaError_t e = cudaStreamSynchronize(st);
-        if (e != cudaSuccess) return set_err(ctx, HSDLA_ERR_CUDA, "zherkx ozaki: %s", cudaGetErrorString(e));
+        if (e != cudaSuccess) { ozaki_plan_release(oz); return set_err(ctx, HSDLA_ERR_CUDA, "zherkx ozaki: %s", cudaGetErrorString(e)); }
         rc = ozaki_check_device_error(oz);
+        ozaki_plan_release(oz);
         if (rc) return set_err(ctx, rc, "device-side error: %s", ozaki_last_error());
         return HSDLA_OK;
     }

@@ -1,27 +1,773 @@
-// Ozaki-split contraction: placeholder until the tcgen05 kernel lands.
+// Ozaki-split complex FP64 contractions on the FP8 tensor cores of sm_103a.
+//
+// Emulates the FP64 BLAS-3 work of create_HS2_stripped_v2
+// (flapw_opt/src/h_and_s_stripped_v2.cpp:155-368: zherk, zher2k, zherkx and the
+// per-atom zhemm/zgemm T application) with exact integer products on tcgen05:
+//
+//  * slicing (oz_slice_kernel): every column g of an operand Z (K x n) gets a
+//    power-of-two exponent e_g with max_k |Re,Im Z_kg| < 2^e_g, and the scaled
+//    column z = Z 2^-e_g is rounded to an integer X = rint(z 2^(5s-1)) that is
+//    split into s balanced base-32 digits
+//        z ~= sum_i d_i 2^(1-5i),  d_1 in [-16,16],  d_i in [-16,15]  (i >= 2).
+//    Every digit is an integer of magnitude <= 16, exactly representable in
+//    e4m3; one byte plane per (digit, re/im).  The digit extraction runs in
+//    64-bit integer arithmetic (one FP64 multiply and one conversion per value):
+//    GB300's FP64 pipe delivers ~1 TFLOP/s, its integer pipes far more.
+//  * products (oz_gemm_kernel): for the output tile (rows g, cols g') and each
+//    diagonal t = i + j of the digit-product triangle (t = 2..s+1), the FP32
+//    TMEM accumulator sums, over the contraction index and all pairs (i, t-i),
+//        Re += dr_i er_j + di_i ei_j,   Im += dr_i ei_j - di_i er_j
+//    as kind::f8f6f4 MMAs (e4m3 x e4m3 -> f32).  Products are integers <= 256,
+//    so a K chunk of at most 2^24 / (2 * 256 * pairs) complex terms keeps every
+//    partial sum an exactly representable integer; chunks are drained into the
+//    FP64 output tile with weight 2^(2-5t), and the last drain applies
+//    2^(e_g + e_g').
+//
+// GB300 mapping: persistent CTAs (one per SM, 512 TMEM columns = two 128x(128
+// re + 128 im) FP32 accumulators), warp-specialised: one TMA producer warp
+// (SW128 K-major 128x128-byte boxes, 64 KB per stage, 3 stages), one MMA warp
+// (single elected issuer, tcgen05.commit to release stages and publish
+// accumulators), four epilogue warps (tcgen05.ld 32x32b, FP64 recombination,
+// coalesced read-modify-write of the L2-resident output tile).  Every mbarrier
+// wait is bounded by a clock64 budget; on expiry the kernel records an error
+// word, stops issuing work, waits (bounded) for its in-flight copies and MMAs,
+// frees TMEM and returns.
+#include <cuda.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <vector>
+
 #include "ozaki.cuh"
 
 namespace hsdla {
 
 static const char *g_oz_err = "";
+const char *ozaki_last_error() { return g_oz_err; }
 
-int ozaki_plan_init(OzakiPlan &oz, int num_slices, double target) {
-    oz.num_slices = num_slices;
-    oz.target = target;
+namespace {
+
+// ------------------------------------------------------------------ constants
+constexpr int kTileM = 128;          // output rows per tile (TMEM lanes)
+constexpr int kTileN = 128;          // output complex columns per tile
+constexpr int kKBlock = 128;         // contraction bytes (e4m3 values) per stage
+constexpr int kStages = 3;
+constexpr int kStageBytes = 4 * kTileM * kKBlock;   // Ar, Ai, Br, Bi boxes
+constexpr int kThreads = 192;        // warp 0 TMA, warp 1 MMA, warps 2..5 epilogue
+constexpr long long kWaitCycles = 2000000000LL;    // ~1 s at 2 GHz
+constexpr int kExactTerms = 1 << 24;                // FP32 exact-integer bound
+
+struct OzJob {
+    int32_t lmap, rmap;        // tensor-map index (0..3) of the left / right digit operand
+    int32_t lower, pad0;       // 1: only tiles and elements with row >= col
+    int64_t lplane, rplane;    // rows per digit plane in each map
+    int64_t lrow0, rrow0;      // first operand row (output row / col 0) inside a plane
+    int64_t lk0, rk0;          // first contraction byte (multiple of 128)
+    int64_t nkb;               // contraction blocks of 128
+    int64_t m, n;              // valid output rows / cols
+    int64_t tiles_n;           // tile columns (full mode)
+    int64_t tile_begin;        // first global tile index
+    double2 *out;
+    int64_t ldo;
+    const int32_t *el;         // exponent of each output row (job-relative)
+    const int32_t *er;         // exponent of each output col (job-relative)
+};
+
+// ------------------------------------------------------------- PTX wrappers
+__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(smem_u32(bar)) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// Bounded wait.  Returns false (and raises the CTA abort flag) when the budget expires
+// or another role already aborted.
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, volatile int *abort_flag, int *err,
+                                          int where) {
+    if (mbar_try_wait(bar, parity)) return true;
+    const long long t0 = clock64();
+    while (!mbar_try_wait(bar, parity)) {
+        if (*abort_flag) return false;
+        if (clock64() - t0 > kWaitCycles) {
+            *abort_flag = 1;
+            atomicCAS(err, 0, kDevTimeout * 16 + where);
+            return false;
+        }
+    }
+    return true;
+}
+// Wait that ignores the abort flag (used only while draining in-flight work), still bounded.
+__device__ __forceinline__ void mbar_drain_wait(uint64_t *bar, uint32_t parity) {
+    const long long t0 = clock64();
+    while (!mbar_try_wait(bar, parity))
+        if (clock64() - t0 > kWaitCycles) return;
+}
+
+__device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, uint64_t *bar, int x, int y) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4}], [%2];\n" ::"r"(
+            smem_u32(dst)),
+        "l"((uint64_t)map), "r"(smem_u32(bar)), "r"(x), "r"(y)
+        : "memory");
+}
+
+__device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr) {
+    uint64_t d = 0;
+    d |= (uint64_t)((saddr & 0x3FFFF) >> 4);          // start address
+    d |= (uint64_t)1 << 16;                          // leading byte offset (unused for SW128 K-major)
+    d |= (uint64_t)(1024 >> 4) << 32;                // stride byte offset: 8 rows x 128 B
+    d |= (uint64_t)1 << 46;                          // descriptor version (sm_100 family)
+    d |= (uint64_t)2 << 61;                          // SWIZZLE_128B
+    return d;
+}
+
+// kind::f8f6f4, A = B = e4m3, D = f32, both K-major, M = 128, N = 128
+__host__ __device__ constexpr uint32_t idesc_f8(bool negA) {
+    return (1u << 4) | (0u << 7) | (0u << 10) | ((negA ? 1u : 0u) << 13) | (0u << 14) | (0u << 15) | (0u << 16) |
+           ((uint32_t)(kTileN >> 3) << 17) | ((uint32_t)(kTileM >> 4) << 24);
+}
+
+__device__ __forceinline__ void mma_f8(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                       uint32_t accumulate) {
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::f8f6f4 [%0], %1, %2, %3, p;\n}\n" ::"r"(
+            d_tmem),
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+        : "memory");
+}
+__device__ __forceinline__ void mma_commit(uint64_t *bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(smem_u32(bar))
+                 : "memory");
+}
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory"); }
+
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,%18,%19,"
+        "%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];\n"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+          "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]),
+          "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
+          "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+        : "r"(taddr));
+}
+__device__ __forceinline__ void tmem_ld_wait() { asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory"); }
+
+// ------------------------------------------------------- work decomposition
+__device__ __forceinline__ int job_of(const OzJob *jobs, int num_jobs, int64_t tile) {
+    int lo = 0, hi = num_jobs - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (jobs[mid].tile_begin <= tile) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+__device__ __forceinline__ void tile_coords(const OzJob &j, int64_t x, int64_t &tm, int64_t &tn) {
+    if (j.lower) {
+        int64_t r = (int64_t)((sqrt(8.0 * (double)x + 1.0) - 1.0) * 0.5);
+        while (r * (r + 1) / 2 > x) --r;
+        while ((r + 1) * (r + 2) / 2 <= x) ++r;
+        tm = r;
+        tn = x - r * (r + 1) / 2;
+    } else {
+        tm = x / j.tiles_n;
+        tn = x - tm * j.tiles_n;
+    }
+}
+// k-blocks per exact accumulation chunk on diagonal t (pairs = t - 1 for t <= s + 1)
+__host__ __device__ __forceinline__ int64_t chunk_kblocks(int pairs) {
+    const int64_t terms_per_kb = (int64_t)2 * kKBlock * pairs * 256;   // re/im products x max |product|
+    int64_t c = kExactTerms / terms_per_kb;
+    return c < 1 ? 1 : c;
+}
+
+struct __align__(8) Barriers {
+    uint64_t full[kStages];
+    uint64_t empty[kStages];
+    uint64_t tfull[2];
+    uint64_t tempty[2];
+};
+
+__global__ void __launch_bounds__(kThreads, 1)
+    oz_gemm_kernel(const __grid_constant__ CUtensorMap map0, const __grid_constant__ CUtensorMap map1,
+                   const __grid_constant__ CUtensorMap map2, const __grid_constant__ CUtensorMap map3,
+                   const OzJob *__restrict__ jobs, int num_jobs, int64_t total_tiles, int s, int *err) {
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    // 1024-byte alignment of the stage buffers (SW128 atoms)
+    unsigned char *smem = reinterpret_cast<unsigned char *>(
+        (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    __shared__ Barriers bars;
+    __shared__ uint32_t tmem_base_sh;
+    __shared__ volatile int abort_flag;
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    auto map_of = [&](int i) -> const CUtensorMap * {
+        return i == 0 ? &map0 : i == 1 ? &map1 : i == 2 ? &map2 : &map3;
+    };
+
+    if (threadIdx.x == 0) {
+        for (int i = 0; i < kStages; ++i) { mbar_init(&bars.full[i], 1); mbar_init(&bars.empty[i], 1); }
+        for (int i = 0; i < 2; ++i) { mbar_init(&bars.tfull[i], 1); mbar_init(&bars.tempty[i], 128); }
+        abort_flag = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+        for (int i = 0; i < 4; ++i) asm volatile("prefetch.tensormap [%0];\n" ::"l"((uint64_t)map_of(i)) : "memory");
+    }
+    if (warp == 1) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 512;\n" ::"r"(smem_u32(&tmem_base_sh))
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem_base = tmem_base_sh;
+
+    if (warp == 0) {
+        // ------------------------------------------------------------ TMA producer
+        if (lane == 0) {
+            int stage = 0;
+            uint32_t phase = 0;
+            int64_t issued = 0;
+            bool ok = true;
+            for (int64_t tile = blockIdx.x; ok && tile < total_tiles; tile += gridDim.x) {
+                const OzJob &j = jobs[job_of(jobs, num_jobs, tile)];
+                int64_t tm, tn;
+                tile_coords(j, tile - j.tile_begin, tm, tn);
+                const CUtensorMap *lm = map_of(j.lmap), *rm = map_of(j.rmap);
+                for (int t = 2; ok && t <= s + 1; ++t) {
+                    const int ilo = max(1, t - s), ihi = min(s, t - 1);
+                    const int64_t ck = chunk_kblocks(ihi - ilo + 1);
+                    for (int64_t cb = 0; ok && cb < j.nkb; cb += ck) {
+                        const int64_t ce = min(j.nkb, cb + ck);
+                        for (int64_t kb = cb; ok && kb < ce; ++kb) {
+                            for (int i = ilo; i <= ihi; ++i) {
+                                const int jj = t - i;
+                                if (!mbar_wait(&bars.empty[stage], phase ^ 1, &abort_flag, err, 1)) { ok = false; break; }
+                                unsigned char *st = smem + stage * kStageBytes;
+                                mbar_expect_tx(&bars.full[stage], kStageBytes);
+                                const int xl = (int)(j.lk0 + kb * kKBlock), xr = (int)(j.rk0 + kb * kKBlock);
+                                const int64_t yl = j.lrow0 + tm * kTileM, yr = j.rrow0 + tn * kTileN;
+                                tma_load_2d(st, lm, &bars.full[stage], xl, (int)((2 * (i - 1)) * j.lplane + yl));
+                                tma_load_2d(st + 16384, lm, &bars.full[stage], xl, (int)((2 * (i - 1) + 1) * j.lplane + yl));
+                                tma_load_2d(st + 32768, rm, &bars.full[stage], xr, (int)((2 * (jj - 1)) * j.rplane + yr));
+                                tma_load_2d(st + 49152, rm, &bars.full[stage], xr, (int)((2 * (jj - 1) + 1) * j.rplane + yr));
+                                ++issued;
+                                if (++stage == kStages) { stage = 0; phase ^= 1; }
+                            }
+                        }
+                    }
+                }
+            }
+            // drain: every issued stage must have landed before the CTA may exit
+            if (!ok) {
+                for (int q = 0; q < kStages; ++q) {
+                    // the last kStages issued stages are the only ones possibly in flight
+                    if (issued == 0) break;
+                    if (--stage < 0) { stage = kStages - 1; phase ^= 1; }
+                    mbar_drain_wait(&bars.full[stage], phase);
+                    --issued;
+                }
+            }
+        }
+    } else if (warp == 1) {
+        // ------------------------------------------------------------ MMA issuer
+        if (lane == 0) {
+            int stage = 0;
+            uint32_t phase = 0;
+            int64_t unit = 0;
+            bool ok = true;
+            const uint32_t id_pos = idesc_f8(false), id_neg = idesc_f8(true);
+            const uint32_t sbase = smem_u32(smem);
+            for (int64_t tile = blockIdx.x; ok && tile < total_tiles; tile += gridDim.x) {
+                const OzJob &j = jobs[job_of(jobs, num_jobs, tile)];
+                for (int t = 2; ok && t <= s + 1; ++t) {
+                    const int ilo = max(1, t - s), ihi = min(s, t - 1);
+                    const int64_t ck = chunk_kblocks(ihi - ilo + 1);
+                    for (int64_t cb = 0; ok && cb < j.nkb; cb += ck) {
+                        const int64_t ce = min(j.nkb, cb + ck);
+                        const int buf = (int)(unit & 1);
+                        const uint32_t uphase = (uint32_t)((unit >> 1) & 1);
+                        if (!mbar_wait(&bars.tempty[buf], uphase ^ 1, &abort_flag, err, 2)) { ok = false; break; }
+                        tc_fence_after();
+                        const uint32_t d_re = tmem_base + buf * 256, d_im = d_re + 128;
+                        bool first = true;
+                        for (int64_t kb = cb; ok && kb < ce; ++kb) {
+                            for (int i = ilo; i <= ihi; ++i) {
+                                if (!mbar_wait(&bars.full[stage], phase, &abort_flag, err, 3)) { ok = false; break; }
+                                tc_fence_after();
+                                const uint32_t a_re = sbase + stage * kStageBytes, a_im = a_re + 16384;
+                                const uint32_t b_re = a_re + 32768, b_im = a_re + 49152;
+#pragma unroll
+                                for (int kk = 0; kk < kKBlock / 32; ++kk) {
+                                    const uint32_t off = kk * 32;
+                                    const uint32_t acc = first ? 0u : 1u;
+                                    mma_f8(d_re, sw128_desc(a_re + off), sw128_desc(b_re + off), id_pos, acc);
+                                    mma_f8(d_re, sw128_desc(a_im + off), sw128_desc(b_im + off), id_pos, 1u);
+                                    mma_f8(d_im, sw128_desc(a_re + off), sw128_desc(b_im + off), id_pos, acc);
+                                    mma_f8(d_im, sw128_desc(a_im + off), sw128_desc(b_re + off), id_neg, 1u);
+                                    first = false;
+                                }
+                                mma_commit(&bars.empty[stage]);
+                                if (++stage == kStages) { stage = 0; phase ^= 1; }
+                            }
+                        }
+                        if (!ok) break;
+                        mma_commit(&bars.tfull[buf]);
+                        ++unit;
+                    }
+                }
+            }
+            // wait for the MMAs still in flight before TMEM is freed
+            if (unit > 0) {
+                const int64_t u = unit - 1;
+                mbar_drain_wait(&bars.tfull[u & 1], (uint32_t)((u >> 1) & 1));
+            }
+            if (!ok) {
+                // a partially issued unit may still be running: commit and wait for it too
+                mma_commit(&bars.tfull[unit & 1]);
+                mbar_drain_wait(&bars.tfull[unit & 1], (uint32_t)((unit >> 1) & 1));
+            }
+        }
+    } else {
+        // ------------------------------------------------------------ epilogue (warps 2..5)
+        const int q = warp & 3;                      // TMEM lane quadrant of this warp
+        const int r_in_tile = q * 32 + lane;
+        int64_t unit = 0;
+        bool ok = true;
+        for (int64_t tile = blockIdx.x; ok && tile < total_tiles; tile += gridDim.x) {
+            const OzJob &j = jobs[job_of(jobs, num_jobs, tile)];
+            int64_t tm, tn;
+            tile_coords(j, tile - j.tile_begin, tm, tn);
+            const int64_t row = tm * kTileM + r_in_tile;
+            const bool row_ok = row < j.m;
+            const int erow = row_ok ? j.el[row] : 0;
+            for (int t = 2; ok && t <= s + 1; ++t) {
+                const int ilo = max(1, t - s), ihi = min(s, t - 1);
+                const int64_t ck = chunk_kblocks(ihi - ilo + 1);
+                const double wt = ldexp(1.0, 2 - 5 * t);
+                for (int64_t cb = 0; ok && cb < j.nkb; cb += ck) {
+                    const bool first = (t == 2 && cb == 0);
+                    const bool last = (t == s + 1 && cb + ck >= j.nkb);
+                    const int buf = (int)(unit & 1);
+                    const uint32_t uphase = (uint32_t)((unit >> 1) & 1);
+                    if (!mbar_wait(&bars.tfull[buf], uphase, &abort_flag, err, 4)) { ok = false; break; }
+                    tc_fence_after();
+                    const uint32_t tbase = tmem_base + ((uint32_t)(q * 32) << 16) + buf * 256;
+#pragma unroll 1
+                    for (int c0 = 0; c0 < kTileN; c0 += 32) {
+                        uint32_t vre[32], vim[32];
+                        tmem_ld32(tbase + c0, vre);
+                        tmem_ld32(tbase + 128 + c0, vim);
+                        tmem_ld_wait();
+                        if (c0 + 32 >= kTileN) {
+                            tc_fence_before();
+                            mbar_arrive(&bars.tempty[buf]);
+                        }
+                        if (!row_ok) continue;
+#pragma unroll
+                        for (int cc = 0; cc < 32; ++cc) {
+                            const int64_t col = tn * kTileN + c0 + cc;
+                            if (col >= j.n || (j.lower && row < col)) continue;
+                            double2 *p = j.out + row + j.ldo * col;
+                            double re = (double)__uint_as_float(vre[cc]) * wt;
+                            double im = (double)__uint_as_float(vim[cc]) * wt;
+                            if (!first) {
+                                const double2 o = *p;
+                                re += o.x;
+                                im += o.y;
+                            }
+                            if (last) {
+                                const double sc = ldexp(1.0, erow + j.er[col]);
+                                re *= sc;
+                                im *= sc;
+                            }
+                            *p = make_double2(re, im);
+                        }
+                    }
+                    ++unit;
+                }
+            }
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 1) {
+        tc_fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;\n" ::"r"(tmem_base) : "memory");
+    }
+}
+
+// --------------------------------------------------------------- slicing
+// Digit planes of Z (Kin x ncols, column-major, ld ldz) with optional row weights v:
+// padded contraction layout: source rows [b*rpb, (b+1)*rpb) land at [b*bpad, b*bpad + rpb).
+constexpr int kSliceThreads = 256;
+constexpr int kSliceVec = 8;       // consecutive contraction bytes per thread and plane
+
+__device__ __forceinline__ uint32_t e4m3_of_digit(int d) {
+    const uint32_t sgn = d < 0 ? 0x80u : 0u;
+    const uint32_t a = (uint32_t)(d < 0 ? -d : d);
+    if (a == 0) return 0u;
+    const uint32_t e = 31u - __clz(a);             // 0..4
+    const uint32_t man = ((a << 3) >> e) & 7u;
+    return sgn | ((e + 7u) << 3) | man;
+}
+
+__global__ void __launch_bounds__(kSliceThreads) oz_slice_kernel(const double2 *__restrict__ Z, int64_t ldz,
+                                                                 const double *__restrict__ v, int64_t Kin,
+                                                                 int64_t ncols, int64_t rpb, int64_t bpad, int s,
+                                                                 uint8_t *__restrict__ digits, int64_t Kpad,
+                                                                 int64_t plane_rows, int32_t *__restrict__ expo) {
+    const int64_t g = blockIdx.x;
+    __shared__ double red[kSliceThreads / 32];
+    __shared__ int e_sh;
+    const bool live = g < ncols;
+    // pass 1: column max of max(|re|, |im|) * v
+    double mx = 0.0;
+    if (live) {
+        const double2 *col = Z + ldz * g;
+        for (int64_t k = threadIdx.x; k < Kin; k += blockDim.x) {
+            const double2 z = col[k];
+            double a = fmax(fabs(z.x), fabs(z.y));
+            if (v) a *= v[k];
+            mx = fmax(mx, a);
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = mx;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double m = 0.0;
+        for (int i = 0; i < kSliceThreads / 32; ++i) m = fmax(m, red[i]);
+        int e = 0;
+        if (m > 0.0) frexp(m, &e);                 // m < 2^e
+        e_sh = e;
+        if (g < plane_rows) expo[g] = e;
+    }
+    __syncthreads();
+    const int e = e_sh;
+    const int top = 5 * s - 1;                     // X = rint(z 2^(5s-1)), |z| < 1
+    const double base_scale = ldexp(1.0, top - e);
+    const int64_t nb = Kpad / bpad;
+    for (int64_t kp0 = (int64_t)threadIdx.x * kSliceVec; kp0 < Kpad; kp0 += (int64_t)blockDim.x * kSliceVec) {
+        long long xr[kSliceVec], xi[kSliceVec];
+#pragma unroll
+        for (int u = 0; u < kSliceVec; ++u) {
+            const int64_t kp = kp0 + u;
+            const int64_t b = kp / bpad, r = kp - b * bpad;
+            const int64_t k = b * rpb + r;
+            xr[u] = 0; xi[u] = 0;
+            if (live && b < nb && r < rpb && k < Kin) {
+                const double2 z = Z[ldz * g + k];
+                const double sc = v ? base_scale * v[k] : base_scale;
+                xr[u] = __double2ll_rn(z.x * sc);
+                xi[u] = __double2ll_rn(z.y * sc);
+            }
+        }
+        // digits from the least significant: d_i = ((X + 16) mod 32) - 16, X = (X - d_i) / 32
+        uint32_t lo_r[kOzMaxSlices], hi_r[kOzMaxSlices], lo_i[kOzMaxSlices], hi_i[kOzMaxSlices];
+#pragma unroll
+        for (int i = 0; i < kOzMaxSlices; ++i) { lo_r[i] = hi_r[i] = lo_i[i] = hi_i[i] = 0u; }
+#pragma unroll
+        for (int u = 0; u < kSliceVec; ++u) {
+            long long a = xr[u], b = xi[u];
+#pragma unroll
+            for (int i = kOzMaxSlices - 1; i >= 0; --i) {
+                if (i >= s) continue;
+                int da, db;
+                if (i == 0) {
+                    da = (int)a; db = (int)b;
+                } else {
+                    da = (int)(((a + 16) & 31) - 16);
+                    db = (int)(((b + 16) & 31) - 16);
+                    a = (a - da) >> 5;
+                    b = (b - db) >> 5;
+                }
+                const uint32_t ea = e4m3_of_digit(da) << (8 * (u & 3));
+                const uint32_t eb = e4m3_of_digit(db) << (8 * (u & 3));
+                if (u < 4) { lo_r[i] |= ea; lo_i[i] |= eb; } else { hi_r[i] |= ea; hi_i[i] |= eb; }
+            }
+        }
+#pragma unroll
+        for (int i = 0; i < kOzMaxSlices; ++i) {
+            if (i >= s) continue;
+            uint8_t *pr = digits + ((int64_t)(2 * i) * plane_rows + g) * Kpad + kp0;
+            uint8_t *pi = digits + ((int64_t)(2 * i + 1) * plane_rows + g) * Kpad + kp0;
+            *reinterpret_cast<uint2 *>(pr) = make_uint2(lo_r[i], hi_r[i]);
+            *reinterpret_cast<uint2 *>(pi) = make_uint2(lo_i[i], hi_i[i]);
+        }
+    }
+}
+
+// ------------------------------------------------------------ host helpers
+typedef CUresult (*PFN_encodeTiled)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                    const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                    CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+PFN_encodeTiled get_encode() {
+    static PFN_encodeTiled fn = nullptr;
+    if (!fn) {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<PFN_encodeTiled>(p);
+    }
+    return fn;
+}
+
+// digit operand: 2s planes of plane_rows x Kpad bytes
+struct DigitOperand {
+    uint8_t *digits = nullptr;
+    int32_t *expo = nullptr;
+    int64_t plane_rows = 0, Kpad = 0;
+    CUtensorMap map;
+};
+
+int make_map(DigitOperand &d, int s) {
+    PFN_encodeTiled enc = get_encode();
+    if (!enc) { g_oz_err = "cuTensorMapEncodeTiled unavailable"; return HSDLA_ERR_CUDA; }
+    if (d.Kpad % 128 != 0 || (reinterpret_cast<uintptr_t>(d.digits) & 255) != 0) {
+        g_oz_err = "digit operand misaligned";
+        return HSDLA_ERR_ARG;
+    }
+    const int64_t rows = d.plane_rows * 2 * s;
+    if (rows > INT32_MAX || d.Kpad > INT32_MAX) { g_oz_err = "digit operand too large for TMA"; return HSDLA_ERR_UNSUPPORTED; }
+    cuuint64_t dims[2] = {(cuuint64_t)d.Kpad, (cuuint64_t)rows};
+    cuuint64_t strides[1] = {(cuuint64_t)d.Kpad};
+    cuuint32_t box[2] = {(cuuint32_t)kKBlock, (cuuint32_t)kTileM};
+    cuuint32_t es[2] = {1, 1};
+    CUresult r = enc(&d.map, CU_TENSOR_MAP_DATA_TYPE_UINT8, 2, d.digits, dims, strides, box, es,
+                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                     CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) { g_oz_err = "cuTensorMapEncodeTiled failed"; return HSDLA_ERR_CUDA; }
     return HSDLA_OK;
 }
-int64_t ozaki_workspace_bytes(const OzakiPlan &, int64_t, int64_t) { return 0; }
-int ozaki_contract(OzakiPlan &, const double2 *, const double2 *, const double *, int64_t, int64_t, double2 *,
-                   double2 *, int64_t, void *, cudaStream_t, int *) {
-    g_oz_err = "Ozaki path not built";
-    return HSDLA_ERR_UNSUPPORTED;
+
+int64_t round_up(int64_t x, int64_t m) { return (x + m - 1) / m * m; }
+
+// Bump allocator over the caller's workspace.
+struct Arena {
+    char *p;
+    int64_t used = 0;
+    template <typename T>
+    T *take(int64_t count) {
+        T *r = reinterpret_cast<T *>(p + used);
+        used += round_up((int64_t)sizeof(T) * count, 1024);
+        return r;
+    }
+};
+
+int64_t operand_bytes(int s, int64_t rows, int64_t Kpad) {
+    const int64_t pr = round_up(rows, kTileM) + kTileM;
+    return round_up(2 * s * pr * Kpad, 1024) + round_up(4 * pr, 1024);
 }
-int ozaki_herkx(OzakiPlan &, const double2 *, int64_t, const double2 *, int64_t, const double *, int64_t, int64_t,
-                double2 *, int64_t, void *, cudaStream_t, int *) {
-    g_oz_err = "Ozaki path not built";
-    return HSDLA_ERR_UNSUPPORTED;
+
+void carve_operand(Arena &a, DigitOperand &d, int s, int64_t rows, int64_t Kpad) {
+    d.plane_rows = round_up(rows, kTileM) + kTileM;
+    d.Kpad = Kpad;
+    d.digits = a.take<uint8_t>(2 * s * d.plane_rows * Kpad);
+    d.expo = a.take<int32_t>(d.plane_rows);
 }
-int ozaki_check_device_error(OzakiPlan &) { return HSDLA_OK; }
-const char *ozaki_last_error() { return g_oz_err; }
+
+cudaError_t slice(const double2 *Z, int64_t ldz, const double *v, int64_t Kin, int64_t ncols, int64_t rpb,
+                  int64_t bpad, int s, DigitOperand &d, cudaStream_t st) {
+    oz_slice_kernel<<<(unsigned)d.plane_rows, kSliceThreads, 0, st>>>(Z, ldz, v, Kin, ncols, rpb, bpad, s, d.digits,
+                                                                       d.Kpad, d.plane_rows, d.expo);
+    return cudaGetLastError();
+}
+
+int64_t job_tiles(const OzJob &j) {
+    const int64_t tm = (j.m + kTileM - 1) / kTileM, tn = (j.n + kTileN - 1) / kTileN;
+    return j.lower ? tm * (tm + 1) / 2 : tm * tn;
+}
+
+int launch_gemm(std::vector<OzJob> &jobs, const CUtensorMap *maps, int s, int *d_err, OzJob *d_jobs,
+                cudaStream_t st) {
+    int64_t total = 0;
+    for (auto &j : jobs) {
+        j.tiles_n = (j.n + kTileN - 1) / kTileN;
+        j.tile_begin = total;
+        total += job_tiles(j);
+    }
+    if (total == 0) return HSDLA_OK;
+    cudaError_t e = cudaMemcpyAsync(d_jobs, jobs.data(), sizeof(OzJob) * jobs.size(), cudaMemcpyHostToDevice, st);
+    if (e != cudaSuccess) { g_oz_err = cudaGetErrorString(e); return HSDLA_ERR_CUDA; }
+    const size_t smem = (size_t)kStages * kStageBytes + 1024;
+    e = cudaFuncSetAttribute(oz_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) { g_oz_err = cudaGetErrorString(e); return HSDLA_ERR_CUDA; }
+    int dev = 0, nsm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    const int64_t grid = std::min<int64_t>(total, nsm);
+    oz_gemm_kernel<<<(unsigned)grid, kThreads, smem, st>>>(maps[0], maps[1], maps[2], maps[3], d_jobs,
+                                                            (int)jobs.size(), total, s, d_err);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) { g_oz_err = cudaGetErrorString(e); return HSDLA_ERR_CUDA; }
+    // the job table is read by the kernel: keep the host copy alive until it is consumed
+    e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) { g_oz_err = cudaGetErrorString(e); return HSDLA_ERR_CUDA; }
+    return HSDLA_OK;
+}
+
+}  // namespace
+
+// ==================================================================== API
+int ozaki_plan_init(OzakiPlan &oz, int num_slices, double target) {
+    if (num_slices == 0) num_slices = 10;
+    if (num_slices < 2 || num_slices > kOzMaxSlices) { g_oz_err = "num_slices outside [2, 12]"; return HSDLA_ERR_ARG; }
+    oz.num_slices = num_slices;
+    oz.target = target;
+    if (!oz.d_error) {
+        if (cudaMalloc(&oz.d_error, sizeof(int)) != cudaSuccess) { g_oz_err = "cudaMalloc"; return HSDLA_ERR_NOMEM; }
+        cudaMemset(oz.d_error, 0, sizeof(int));
+    }
+    return HSDLA_OK;
+}
+
+void ozaki_plan_release(OzakiPlan &oz) {
+    if (oz.d_error) cudaFree(oz.d_error);
+    oz.d_error = nullptr;
+}
+
+int ozaki_check_device_error(OzakiPlan &oz) {
+    if (!oz.d_error) return HSDLA_OK;
+    int h = 0;
+    if (cudaMemcpy(&h, oz.d_error, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess) return HSDLA_ERR_CUDA;
+    if (h != 0) {
+        static char buf[96];
+        snprintf(buf, sizeof(buf), "device wait expired (code %d, role %d)", h / 16, h % 16);
+        g_oz_err = buf;
+        cudaMemset(oz.d_error, 0, sizeof(int));
+        return HSDLA_ERR_TIMEOUT;
+    }
+    return HSDLA_OK;
+}
+
+int64_t ozaki_herkx_workspace(int s, int64_t K, int64_t n) {
+    const int64_t Kpad = round_up(std::max<int64_t>(K, 1), kKBlock);
+    return 2 * operand_bytes(s, n, Kpad) + 4096 + 4096;
+}
+
+int ozaki_herkx(OzakiPlan &oz, const double2 *P, int64_t ldp, const double2 *Q, int64_t ldq, const double *w,
+                int64_t K, int64_t n, double2 *out, int64_t ldo, void *ws, cudaStream_t st, int *launches) {
+    const int s = oz.num_slices;
+    const int64_t Kpad = round_up(std::max<int64_t>(K, 1), kKBlock);
+    Arena ar{reinterpret_cast<char *>(ws)};
+    DigitOperand dp, dq;
+    carve_operand(ar, dp, s, n, Kpad);
+    carve_operand(ar, dq, s, n, Kpad);
+    OzJob *d_jobs = ar.take<OzJob>(4);
+    cudaError_t e = slice(P, ldp, nullptr, K, n, Kpad, Kpad, s, dp, st);
+    if (e == cudaSuccess) e = slice(Q, ldq, w, K, n, Kpad, Kpad, s, dq, st);
+    if (e != cudaSuccess) { g_oz_err = cudaGetErrorString(e); return HSDLA_ERR_CUDA; }
+    int rc = make_map(dp, s);
+    if (!rc) rc = make_map(dq, s);
+    if (rc) return rc;
+    CUtensorMap maps[4] = {dp.map, dq.map, dp.map, dp.map};
+    std::vector<OzJob> jobs(1);
+    OzJob &j = jobs[0];
+    memset(&j, 0, sizeof(j));
+    j.lmap = 0; j.rmap = 1; j.lower = 1;
+    j.lplane = dp.plane_rows; j.rplane = dq.plane_rows;
+    j.nkb = Kpad / kKBlock; j.m = n; j.n = n;
+    j.out = out; j.ldo = ldo; j.el = dp.expo; j.er = dq.expo;
+    rc = launch_gemm(jobs, maps, s, oz.d_error, d_jobs, st);
+    if (launches) *launches = 3;
+    return rc;
+}
+
+// Full pipeline for one k-point: slices of C, wC, T, the Ozaki T application
+// X = T C (FP64 out), slices of X, then the S and H lower-triangle tiles in one launch.
+int64_t ozaki_pipeline_workspace(int s, int64_t twoL, int64_t na, int64_t nt, int64_t G) {
+    const int64_t bpad = round_up(twoL, kKBlock);
+    const int64_t Kpad = bpad * na;
+    return 3 * operand_bytes(s, G, Kpad) + operand_bytes(s, nt * twoL, bpad) +
+           round_up(sizeof(OzJob) * (na + 4), 1024) + 4096;
+}
+
+int ozaki_pipeline(OzakiPlan &oz, const OzakiInputs &in, double2 *S, double2 *H, int64_t ldo, void *ws,
+                   cudaStream_t st, int *launches) {
+    const int s = oz.num_slices;
+    const int64_t twoL = in.twoL, na = in.na, nt = in.nt, G = in.G;
+    const int64_t K = twoL * na;
+    const int64_t bpad = round_up(twoL, kKBlock);
+    const int64_t Kpad = bpad * na;
+    Arena ar{reinterpret_cast<char *>(ws)};
+    DigitOperand dC, dW, dX, dT;
+    carve_operand(ar, dC, s, G, Kpad);
+    carve_operand(ar, dW, s, G, Kpad);
+    carve_operand(ar, dX, s, G, Kpad);
+    carve_operand(ar, dT, s, nt * twoL, bpad);
+    OzJob *d_jobs = ar.take<OzJob>(na + 4);
+    int nl = 0;
+    cudaError_t e = slice(in.C, K, nullptr, K, G, twoL, bpad, s, dC, st);
+    if (e == cudaSuccess) e = slice(in.C, K, in.w, K, G, twoL, bpad, s, dW, st);
+    if (e == cudaSuccess) e = slice(in.Tfull, twoL, nullptr, twoL, nt * twoL, twoL, bpad, s, dT, st);
+    if (e != cudaSuccess) { g_oz_err = cudaGetErrorString(e); return HSDLA_ERR_CUDA; }
+    nl += 3;
+    int rc = make_map(dC, s);
+    if (!rc) rc = make_map(dW, s);
+    if (!rc) rc = make_map(dX, s);
+    if (!rc) rc = make_map(dT, s);
+    if (rc) return rc;
+    CUtensorMap maps[4] = {dC.map, dW.map, dX.map, dT.map};
+    // (b) X_a = T_t C_a for every atom: left = T digits (rows = T columns of type t), right = C digits
+    std::vector<OzJob> jobs;
+    for (int64_t a = 0; a < na; ++a) {
+        OzJob j;
+        memset(&j, 0, sizeof(j));
+        const int64_t t = in.atom_type[a];
+        j.lmap = 3; j.rmap = 0; j.lower = 0;
+        j.lplane = dT.plane_rows; j.rplane = dC.plane_rows;
+        j.lrow0 = t * twoL; j.rrow0 = 0;
+        j.lk0 = 0; j.rk0 = a * bpad;
+        j.nkb = bpad / kKBlock;
+        j.m = twoL; j.n = G;
+        j.out = in.X + twoL * a; j.ldo = K;
+        j.el = dT.expo + t * twoL; j.er = dC.expo;
+        jobs.push_back(j);
+    }
+    rc = launch_gemm(jobs, maps, s, oz.d_error, d_jobs, st);
+    if (rc) return rc;
+    nl += 1;
+    e = slice(in.X, K, nullptr, K, G, twoL, bpad, s, dX, st);
+    if (e != cudaSuccess) { g_oz_err = cudaGetErrorString(e); return HSDLA_ERR_CUDA; }
+    nl += 1;
+    // (c) S = C^H (w C), H = C^H X: lower-triangle tiles of both in one launch
+    jobs.clear();
+    for (int which = 0; which < 2; ++which) {
+        OzJob j;
+        memset(&j, 0, sizeof(j));
+        j.lmap = 0; j.rmap = which == 0 ? 1 : 2; j.lower = 1;
+        j.lplane = dC.plane_rows; j.rplane = which == 0 ? dW.plane_rows : dX.plane_rows;
+        j.nkb = Kpad / kKBlock;
+        j.m = G; j.n = G;
+        j.out = which == 0 ? S : H; j.ldo = ldo;
+        j.el = dC.expo; j.er = which == 0 ? dW.expo : dX.expo;
+        jobs.push_back(j);
+    }
+    rc = launch_gemm(jobs, maps, s, oz.d_error, d_jobs, st);
+    nl += 1;
+    if (launches) *launches = nl;
+    return rc;
+}
 
 }  // namespace hsdla

@@ -13,11 +13,25 @@ struct OzakiPlan {
     int *d_error = nullptr;      // device error word (bounded waits)
 };
 
+// Inputs of one k-point: C = [A_a; B_a] (K = 2 L a rows, G columns, ld K),
+// per-type Hermitian T blocks (2L x 2L each, column-major, concatenated),
+// S row weights w (K), FP64 workspace X (K x G, ld K).
+struct OzakiInputs {
+    const double2 *C;
+    const double2 *Tfull;
+    const double *w;
+    const int32_t *atom_type;    // host array [na]
+    double2 *X;
+    int64_t twoL, na, nt, G;
+};
+
 int ozaki_plan_init(OzakiPlan &oz, int num_slices, double target);
-int64_t ozaki_workspace_bytes(const OzakiPlan &oz, int64_t K, int64_t n);
-// S = (diag(wsqrt) C)^H (diag(wsqrt) C), H = C^H X; lower triangles; C, X: K x G, ld K.
-int ozaki_contract(OzakiPlan &oz, const double2 *C, const double2 *X, const double *wsqrt, int64_t K, int64_t G,
-                   double2 *S, double2 *H, int64_t ldo, void *ws, cudaStream_t st, int *launches);
+void ozaki_plan_release(OzakiPlan &oz);
+int64_t ozaki_pipeline_workspace(int s, int64_t twoL, int64_t na, int64_t nt, int64_t G);
+int64_t ozaki_herkx_workspace(int s, int64_t K, int64_t n);
+// S = C^H diag(w) C and H = C^H (T C) (lower triangles) with the T application emulated too.
+int ozaki_pipeline(OzakiPlan &oz, const OzakiInputs &in, double2 *S, double2 *H, int64_t ldo, void *ws,
+                   cudaStream_t st, int *launches);
 // OUT = P^H diag(w) Q, lower triangle (standalone component).
 int ozaki_herkx(OzakiPlan &oz, const double2 *P, int64_t ldp, const double2 *Q, int64_t ldq, const double *w,
                 int64_t K, int64_t n, double2 *out, int64_t ldo, void *ws, cudaStream_t st, int *launches);
