@@ -1,0 +1,320 @@
+"""Benchmark of the H/S generation path on GB300.
+
+One step = H and S (lower triangles, complex128) of one k-point of the
+precision-form workload: cubic cell a = 24 bohr, 128 atoms of 8 types,
+R_MT = 2.0, lmax = 10 (L = 121, K = 2 L a = 30976 stacked rows), n_G = 8000,
+seeded synthetic inputs (see hybridhsdla_gb300/synth.py, config "c2").
+
+Reported:
+  value        effective FP64-equivalent TFLOP/s of the Ozaki-FP8 path with the
+               inputs resident in HBM (canonical work 20 G^2 La + 24 L^2 a G per
+               k-point, the reference's own flop formulas);
+  e2e          the same metric through the C ABI entry point hsdla_create_hs with
+               pinned HOST buffers: input upload and the H/S download are inside
+               the timed region;
+  fp64         the plain FP64 (DMMA) path on the same k-point, and the Ozaki
+               path's relative errors against it;
+  roofline     the dominant launch (the S/H digit-product contraction) against the
+               FP8 tensor peak;
+  cpu_baseline the oracle port of the reference CPU path (construct_AB + the
+               create_HS2_stripped_v2 BLAS sequence on OpenBLAS), bounded sample.
+
+``--impl reference`` times the reference CPU path (the oracle port: the
+reference itself does not build on this image) on a bounded sample of the same
+workload, in the same unit.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "H+S gen ms/k-point & eff. TFLOP/s: emulated vs native FP64 at ≤1e-13 rel err"
+UNIT = "TFLOP/s (FP64-equivalent, 20*G^2*La + 24*L^2*a*G per k-point)"
+WORKLOAD = "c2"
+PROFILE_SUMMARY = os.path.join(ROOT, "profiles", "oz_gemm_c2.md")
+
+
+def _peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f), "measured"
+    except Exception:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}, "fallback"
+
+
+def _traffic_from_profile():
+    """dram bytes per launch of the dominant kernel from the committed ncu summary."""
+    try:
+        for line in open(PROFILE_SUMMARY):
+            if line.strip().startswith("traffic_bytes_per_launch_c2:"):
+                return float(line.split(":", 1)[1].split()[0])
+    except OSError:
+        pass
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    def __init__(self, index: int = 0):
+        self.samples = []
+        self.proc = None
+        self.index = index
+
+    def __enter__(self):
+        q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) == 7:
+                self.samples.append(parts)
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = sorted(float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit())
+        mx = max(float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit())
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for s in self.samples for i in range(4) if s[3 + i].lower().startswith("active")})
+        return {"sm_mhz": sm[len(sm) // 2] if sm else None, "sm_max_mhz": mx, "reasons": reasons,
+                "samples": len(self.samples)}
+
+
+def _dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def _barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def _max_over_ranks(ws, x: float) -> float:
+    if ws == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def cpu_reference_step(sys_, n_g_sample: int, threads: int):
+    """One bounded sample of the reference CPU path: the c2 system with the basis
+    truncated to its first n_g_sample G-vectors.  Returns (seconds, flop)."""
+    import oracle
+    from hybridhsdla_gb300 import synth
+    kp = sys_.kpoints[0]
+    sub = synth.KPoint(k=kp.k, g=kp.g[:n_g_sample])
+    t0 = time.perf_counter()
+    oracle.reference_hs(sys_, sub, nthreads=threads)
+    return time.perf_counter() - t0, sys_.flop_per_kpoint(n_g_sample)
+
+
+def run_reference(args):
+    ws, rank, _ = _dist()
+    if rank != 0:
+        return
+    os.environ.setdefault("OPENBLAS_NUM_THREADS", str(os.cpu_count() or 1))
+    import oracle
+    from hybridhsdla_gb300 import synth
+    threads = oracle.nthreads_default()
+    sys_ = synth.make_system(WORKLOAD)
+    ng = args.ref_sample_ng
+    for _ in range(args.warmup):
+        cpu_reference_step(sys_, ng, threads)
+    tot_s, tot_f = 0.0, 0.0
+    for _ in range(args.steps):
+        s, f = cpu_reference_step(sys_, ng, threads)
+        tot_s += s
+        tot_f += f
+    v = tot_f / tot_s / 1e12
+    sample = f"c2 system (128 atoms, lmax 10) with the basis truncated to its first {ng} of 8000 G-vectors"
+    line = {"metric": METRIC, "value": v, "unit": UNIT, "impl": "reference", "n_gpus": ws,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tot_s / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded)", "config": {"workload": "c2 sample", "n_g_sample": ng,
+                                                      "atoms": 128, "lmax": 10},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    import numpy as np
+    import torch
+
+    from hybridhsdla_gb300 import api, synth
+
+    ws, rank, local = _dist()
+    if ws > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("gloo")
+    dev = local if ws > 1 else 0
+    torch.cuda.set_device(dev)
+    ctx = api.Context(dev)
+    sys_ = synth.make_system(WORKLOAD)
+    kp = sys_.kpoints[0]
+    G = kp.n_g
+    flop = sys_.flop_per_kpoint(G)
+
+    plan = ctx.plan(sys_, precision="ozaki", num_slices=args.slices)
+    outs = plan.alloc_outputs()
+    stream = torch.cuda.current_stream()
+    for _ in range(args.warmup):
+        rep = plan.execute(outs)
+    torch.cuda.synchronize()
+    _barrier(ws)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    dom_ms, launches = [], 0
+    with ClockSampler(dev) as clk:
+        torch.cuda.synchronize()
+        ev0.record(stream)
+        for _ in range(args.steps):
+            rep = plan.execute(outs)
+            dom_ms.append(rep["ms_dominant"])
+            launches += rep["kernel_launches"]
+        ev1.record(stream)
+        torch.cuda.synchronize()
+    _barrier(ws)
+    ms = ev0.elapsed_time(ev1) / args.steps
+    ms = _max_over_ranks(ws, ms)
+    value = ws * flop / (ms * 1e-3) / 1e12
+    dominant_flop = rep["dominant_flop"]
+    S_oz = outs[0][1].clone()
+    H_oz = outs[0][0].clone()
+    plan.close()
+
+    # ---- end to end through the C ABI with pinned host buffers
+    Hh = torch.empty((G, G), dtype=torch.complex128).pin_memory()
+    Sh = torch.empty((G, G), dtype=torch.complex128).pin_memory()
+    outs_h = [(Hh.numpy().T, Sh.numpy().T)]          # column-major views of the pinned buffers
+    tmats = api.prepare_tmats(sys_)
+    ctx.create_hs(sys_, precision="ozaki", num_slices=args.slices, tmats=tmats, out=outs_h)  # warm
+    torch.cuda.synchronize()
+    e2e_steps = max(1, min(args.steps, 5))
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        _, rep_e = ctx.create_hs(sys_, precision="ozaki", num_slices=args.slices, tmats=tmats, out=outs_h)
+    e2e_s = (time.perf_counter() - t0) / e2e_steps
+    e2e_s = _max_over_ranks(ws, e2e_s)
+    h2d = sum(a.nbytes for a in (kp.g, tmats[0], tmats[1], tmats[2], sys_.u, sys_.u_dr, sys_.dE_u,
+                                  sys_.dE_u_dr, sys_.dE_u_norm, sys_.atom_pos, sys_.atom_type, sys_.type_rmt))
+    d2h = 2 * G * G * 16
+
+    # ---- plain FP64 path on the same k-point, and the Ozaki error against it
+    fp64 = None
+    if not args.skip_fp64 and rank == 0:
+        pl64 = ctx.plan(sys_, precision="fp64")
+        o64 = pl64.alloc_outputs()
+        r64 = pl64.execute(o64)
+        torch.cuda.synchronize()
+
+        def errs(X, R):
+            Xl = torch.tril(X.transpose(0, 1))
+            Rl = torch.tril(R.transpose(0, 1))
+            d = Xl - Rl
+            return (float(torch.linalg.norm(d) / torch.linalg.norm(Rl)),
+                    float(d.abs().max() / Rl.abs().max()))
+        eS, eH = errs(S_oz, o64[0][1]), errs(H_oz, o64[0][0])
+        fp64 = {"ms_per_kpoint": r64["ms_total"], "tflops": r64["eff_tflops"],
+                "dominant_ms": r64["ms_dominant"],
+                "ozaki_speedup": r64["ms_total"] / ms,
+                "ozaki_rel_err_vs_fp64": {"S_fro": eS[0], "S_max": eS[1], "H_fro": eH[0], "H_max": eH[1]}}
+        pl64.close()
+        del o64
+
+    peaks, src = _peaks()
+    fp8_peak = 2.0 * peaks["bf16_tflops"]
+    dom = float(np.median(dom_ms))
+    achieved = dominant_flop / (dom * 1e-3) / 1e12
+    traffic = _traffic_from_profile()
+    roof = {"bound": "tensor", "achieved": achieved, "peak": fp8_peak, "unit": "TFLOP/s",
+            "frac": achieved / fp8_peak, "traffic": traffic,
+            "kernel": "oz_gemm_kernel (S and H lower-triangle digit products)",
+            "peak_source": f"2 x {src} bf16 burst (FP8 e4m3 dense rate = 2x bf16 on tcgen05)"}
+
+    cpu = None
+    if not args.skip_cpu and rank == 0:
+        import oracle
+        os.environ.setdefault("OPENBLAS_NUM_THREADS", str(os.cpu_count() or 1))
+        threads = oracle.nthreads_default()
+        cpu_reference_step(sys_, args.ref_sample_ng, threads)       # warm
+        s_, f_ = cpu_reference_step(sys_, args.ref_sample_ng, threads)
+        cpu = {"value": f_ / s_ / 1e12, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": f"c2 system with the basis truncated to its first {args.ref_sample_ng} G-vectors, "
+                         f"{s_:.1f} s"}
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded generators, no dataset)",
+                "config": {"workload": "c2: cubic a=24 bohr, 128 atoms / 8 types, lmax 10, n_G 8000, 1 k-point",
+                           "precision": f"ozaki-fp8 e4m3, {rep['num_slices']} digit slices",
+                           "ms_per_kpoint": ms, "l2": "inputs larger than L2 (digit operands ~16 GB)",
+                           "parallelism": f"replicas{ws}"},
+                "e2e": {"value": ws * flop / e2e_s / 1e12, "unit": UNIT, "ms_per_kpoint": e2e_s * 1e3,
+                        "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
+                "gpu_launches": launches,
+                "stage_ms": {"construct_ab": rep["ms_construct_ab"], "tapply": rep["ms_tapply"],
+                             "contract": rep["ms_contract"], "dominant": dom},
+                "fp64": fp64, "roofline": roof, "cpu_baseline": cpu, "clocks": clk.summary()}
+        print(json.dumps(line), flush=True)
+    ctx.close()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--slices", type=int, default=0, help="Ozaki digit slices (0 = default)")
+    ap.add_argument("--ref-sample-ng", type=int, default=1500)
+    ap.add_argument("--skip-fp64", action="store_true")
+    ap.add_argument("--skip-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -67,6 +67,8 @@ class ReportStruct(ctypes.Structure):
     _fields_ = [("ms_total", ctypes.c_double), ("ms_per_kpoint", ctypes.c_double), ("flop", ctypes.c_double),
                 ("eff_tflops", ctypes.c_double), ("ms_construct_ab", ctypes.c_double),
                 ("ms_tapply", ctypes.c_double), ("ms_contract", ctypes.c_double),
+                ("ms_dominant", ctypes.c_double), ("dominant_flop", ctypes.c_double),
+                ("est_rel_err", ctypes.c_double),
                 ("num_slices", ctypes.c_int32), ("num_kpoints", ctypes.c_int32),
                 ("kernel_launches", ctypes.c_int32), ("reserved", ctypes.c_int32 * 5)]
 

@@ -35,7 +35,7 @@ struct hsdla_context {
     // persistent workspace reused across calls (grows on demand)
     void *ws = nullptr;
     int64_t ws_bytes = 0;
-    cudaEvent_t ev0 = nullptr, ev1 = nullptr, evs[4] = {nullptr, nullptr, nullptr, nullptr};
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr, evs[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
 };
 
 struct PlanKpoint {
@@ -62,6 +62,8 @@ struct hsdla_plan {
     int64_t jobs_cap = 0;
     std::vector<Fp64Job> h_jobs;
     OzakiPlan oz{};
+    bool autotune = false;           // Ozaki slice count still to be chosen from the data
+    double est_err = 0.0;            // autotuner's predicted relative error
     int launches = 0;
 };
 
@@ -265,6 +267,115 @@ int64_t assign_tiles(std::vector<Fp64Job> &jobs, size_t first) {
     return t;
 }
 
+// Lower-triangle relative errors (Frobenius, max) of X against R, both n x n column-major.
+void lower_errors(const std::vector<std::complex<double>> &X, const std::vector<std::complex<double>> &R, int64_t n,
+                  double &fro, double &mx) {
+    double d2 = 0, r2 = 0, dm = 0, rm = 0;
+    for (int64_t c = 0; c < n; ++c)
+        for (int64_t r = c; r < n; ++r) {
+            const auto d = X[r + n * c] - R[r + n * c];
+            d2 += std::norm(d); r2 += std::norm(R[r + n * c]);
+            dm = std::max(dm, std::abs(d)); rm = std::max(rm, std::abs(R[r + n * c]));
+        }
+    fro = r2 > 0 ? std::sqrt(d2 / r2) : 0.0;
+    mx = rm > 0 ? dm / rm : 0.0;
+}
+
+// Slice autotuner: an a-posteriori check of the Ozaki contraction on a column sample
+// re-done in FP64.  The error of the S and H sample tiles at a probe slice count is
+// extrapolated by 2^-5 per extra digit (each digit carries 5 bits) and, for the
+// Frobenius ratio, by sqrt(n_G / n_sample) (digit errors are uniform over the matrix
+// while its norm is carried by the diagonal); the smallest slice count whose
+// prediction stays below a quarter of the target is kept for the plan.
+int autotune_slices(hsdla_plan *pl, double2 *C, cudaStream_t st) {
+    hsdla_context *ctx = pl->ctx;
+    constexpr int kProbe = 8;
+    int ik = 0;
+    for (int i = 0; i < (int)pl->kps.size(); ++i)
+        if (pl->kps[i].n_g > pl->kps[ik].n_g) ik = i;
+    const int64_t G = pl->kps[ik].n_g;
+    if (G == 0) { pl->autotune = false; return HSDLA_OK; }
+    const int64_t ns = std::min<int64_t>(G, 384), step = G / ns;
+    const int64_t K = pl->twoLa, twoL = 2 * (int64_t)pl->L;
+    OzakiPlan probe{};
+    int rc = ozaki_plan_init(probe, kProbe, pl->opts.target_rel_err);
+    if (rc) return set_err(ctx, rc, "autotune: %s", ozaki_last_error());
+    const int64_t bytes_sample = 2 * K * ns * (int64_t)sizeof(double2) + 4 * ns * ns * (int64_t)sizeof(double2);
+    const int64_t bytes_oz = ozaki_pipeline_workspace(kProbe, twoL, pl->na, pl->nt, ns) + 1024;
+    void *buf = nullptr;
+    rc = ctx_malloc(ctx, &buf, bytes_sample + bytes_oz);
+    if (rc) { ozaki_plan_release(probe); return rc; }
+    double2 *Cs = reinterpret_cast<double2 *>(buf), *Xs = Cs + K * ns;
+    double2 *Sr = Xs + K * ns, *Hr = Sr + ns * ns, *So = Hr + ns * ns, *Ho = So + ns * ns;
+    char *wz = reinterpret_cast<char *>((reinterpret_cast<uintptr_t>(Ho + ns * ns) + 1023) & ~uintptr_t(1023));
+    auto fail = [&](int code, const char *what) {
+        cudaStreamSynchronize(st);
+        ctx_free(ctx, buf, bytes_sample + bytes_oz);
+        ozaki_plan_release(probe);
+        return set_err(ctx, code, "autotune: %s", what);
+    };
+    if (launch_construct_ab(pl->dsys, pl->kps[ik].dk, C, K, st) != cudaSuccess) return fail(HSDLA_ERR_CUDA, "construct_ab");
+    if (cudaMemcpy2DAsync(Cs, K * sizeof(double2), C, step * K * sizeof(double2), K * sizeof(double2), ns,
+                          cudaMemcpyDeviceToDevice, st) != cudaSuccess)
+        return fail(HSDLA_ERR_CUDA, "sample gather");
+    // FP64 reference on the sample
+    pl->h_jobs.clear();
+    for (int j = 0; j < pl->na; ++j) {
+        Fp64Job jb{};
+        jb.P = pl->Tfull + (int64_t)pl->atom_type[j] * twoL * twoL; jb.ldp = twoL;
+        jb.Q = Cs + twoL * j; jb.ldq = K; jb.out = Xs + twoL * j; jb.ldo = K;
+        jb.m = twoL; jb.n = ns; jb.k = twoL;
+        pl->h_jobs.push_back(jb);
+    }
+    const int64_t t1 = assign_tiles(pl->h_jobs, 0);
+    const size_t nb = pl->h_jobs.size();
+    Fp64Job js{};
+    js.P = Cs; js.ldp = K; js.Q = Cs; js.ldq = K; js.w = pl->w; js.out = Sr; js.ldo = ns;
+    js.m = ns; js.n = ns; js.k = K; js.lower = 1;
+    Fp64Job jh = js;
+    jh.Q = Xs; jh.w = nullptr; jh.out = Hr;
+    pl->h_jobs.push_back(js);
+    pl->h_jobs.push_back(jh);
+    const int64_t t2 = assign_tiles(pl->h_jobs, nb);
+    if (upload_jobs(pl, st)) return fail(HSDLA_ERR_CUDA, "job upload");
+    if (launch_fp64_jobs(pl->d_jobs, (int)nb, t1, st) != cudaSuccess ||
+        launch_fp64_jobs(pl->d_jobs + nb, 2, t2, st) != cudaSuccess)
+        return fail(HSDLA_ERR_CUDA, "fp64 sample");
+    // Ozaki at the probe slice count (overwrites Xs after the FP64 H job, in stream order)
+    OzakiInputs in;
+    in.C = Cs; in.Tfull = pl->Tfull; in.w = pl->w; in.atom_type = pl->atom_type.data(); in.X = Xs;
+    in.twoL = twoL; in.na = pl->na; in.nt = pl->nt; in.G = ns;
+    int nl = 0;
+    rc = ozaki_pipeline(probe, in, So, Ho, ns, wz, st, &nl);
+    if (rc) return fail(rc, ozaki_last_error());
+    std::vector<std::complex<double>> h[4];
+    double2 *src[4] = {Sr, Hr, So, Ho};
+    for (int q = 0; q < 4; ++q) {
+        h[q].resize(ns * ns);
+        if (cudaMemcpyAsync(h[q].data(), src[q], ns * ns * sizeof(double2), cudaMemcpyDeviceToHost, st) != cudaSuccess)
+            return fail(HSDLA_ERR_CUDA, "sample download");
+    }
+    if (cudaStreamSynchronize(st) != cudaSuccess) return fail(HSDLA_ERR_CUDA, "sync");
+    if (ozaki_check_device_error(probe)) return fail(HSDLA_ERR_TIMEOUT, ozaki_last_error());
+    double fS, mS, fH, mH;
+    lower_errors(h[2], h[0], ns, fS, mS);
+    lower_errors(h[3], h[1], ns, fH, mH);
+    const double grow = std::sqrt((double)G / (double)ns);
+    const double e = std::max(std::max(fS, fH) * grow, std::max(mS, mH));
+    int s = kProbe;
+    double pred = e;
+    while (s < kOzMaxSlices && pred > 0.25 * pl->opts.target_rel_err) {
+        ++s;
+        pred *= 1.0 / 32.0;
+    }
+    pl->oz.num_slices = s;
+    pl->est_err = pred;
+    pl->autotune = false;
+    ctx_free(ctx, buf, bytes_sample + bytes_oz);
+    ozaki_plan_release(probe);
+    return HSDLA_OK;
+}
+
 }  // namespace
 
 // =====================================================================================
@@ -457,6 +568,7 @@ int hsdla_plan_create(hsdla_context *ctx, const hsdla_system *s, const hsdla_kpo
         return set_err(ctx, HSDLA_ERR_CUDA, "table upload failed: %s", cudaGetErrorString(e));
     }
     if (pl->opts.precision == HSDLA_PREC_OZAKI_FP8) {
+        pl->autotune = pl->opts.num_slices == 0;
         rc = ozaki_plan_init(pl->oz, pl->opts.num_slices, pl->opts.target_rel_err);
         if (rc) { hsdla_plan_destroy(pl); return set_err(ctx, rc, "Ozaki plan set-up failed"); }
     }
@@ -470,7 +582,7 @@ int64_t hsdla_plan_workspace_bytes(const hsdla_plan *pl) {
     for (auto &k : pl->kps) ngmax = std::max(ngmax, k.n_g);
     int64_t b = 2 * (int64_t)sizeof(double2) * pl->twoLa * ngmax;   // C and X
     if (pl->opts.precision == HSDLA_PREC_OZAKI_FP8)
-        b += ozaki_pipeline_workspace(pl->oz.num_slices, 2 * (int64_t)pl->L, pl->na, pl->nt, ngmax);
+        b += 1024 + ozaki_pipeline_workspace(pl->oz.num_slices, 2 * (int64_t)pl->L, pl->na, pl->nt, ngmax);
     return b;
 }
 
@@ -514,11 +626,21 @@ int hsdla_plan_execute(hsdla_plan *pl, hsdla_cx *const *dH, hsdla_cx *const *dS,
     int rc = ctx_workspace(ctx, hsdla_plan_workspace_bytes(pl), &ws);
     if (rc) return rc;
     double2 *C = reinterpret_cast<double2 *>(ws);
+    if (pl->autotune) {
+        rc = autotune_slices(pl, C, st);
+        if (rc) return rc;
+        rc = ctx_workspace(ctx, hsdla_plan_workspace_bytes(pl), &ws);
+        if (rc) return rc;
+        C = reinterpret_cast<double2 *>(ws);
+    }
     double2 *X = C + pl->twoLa * ngmax;
-    char *oz_ws = reinterpret_cast<char *>(X + pl->twoLa * ngmax);
+    // the digit workspace needs 1024-byte alignment (TMA boxes, SW128 atoms)
+    char *oz_ws = reinterpret_cast<char *>((reinterpret_cast<uintptr_t>(X + pl->twoLa * ngmax) + 1023) &
+                                           ~uintptr_t(1023));
     const int64_t L = pl->L, twoL = 2 * L, twoLa = pl->twoLa;
     pl->launches = 0;
-    float ms_ab = 0.f, ms_t = 0.f, ms_c = 0.f;
+    float ms_ab = 0.f, ms_t = 0.f, ms_c = 0.f, ms_dom = 0.f;
+    double dom_flop = 0.0;
     CUDA_TRY(ctx, cudaEventRecord(ctx->ev0, st));
     for (int i = 0; i < nk; ++i) {
         const int64_t G = pl->kps[i].n_g;
@@ -560,14 +682,21 @@ int hsdla_plan_execute(hsdla_plan *pl, hsdla_cx *const *dH, hsdla_cx *const *dS,
             pl->launches++;
         }
         CUDA_TRY(ctx, cudaEventRecord(ctx->evs[2], st));
+        const double lower_cflop = 4.0 * (double)G * (double)(G + 1) * (double)twoLa;   // one lower triangle
         if (pl->opts.precision == HSDLA_PREC_FP64) {
+            CUDA_TRY(ctx, cudaEventRecord(ctx->evs[4], st));
             CUDA_TRY(ctx, launch_fp64_jobs(pl->d_jobs + nb, (int)(pl->h_jobs.size() - nb), nt_c, st));
+            CUDA_TRY(ctx, cudaEventRecord(ctx->evs[5], st));
             pl->launches++;
+            dom_flop = 2.0 * lower_cflop;
         } else {
+            const double s_ = pl->oz.num_slices;
+            dom_flop = 2.0 * lower_cflop * s_ * (s_ + 1) / 2;
             int nl = 0;
             OzakiInputs in;
             in.C = C; in.Tfull = pl->Tfull; in.w = pl->w; in.atom_type = pl->atom_type.data(); in.X = X;
             in.twoL = twoL; in.na = pl->na; in.nt = pl->nt; in.G = G;
+            in.ev_dom0 = ctx->evs[4]; in.ev_dom1 = ctx->evs[5];
             rc = ozaki_pipeline(pl->oz, in, reinterpret_cast<double2 *>(dS[i]), reinterpret_cast<double2 *>(dH[i]),
                                 ld[i], oz_ws, st, &nl);
             if (rc) return set_err(ctx, rc, "Ozaki contraction failed: %s", ozaki_last_error());
@@ -575,11 +704,12 @@ int hsdla_plan_execute(hsdla_plan *pl, hsdla_cx *const *dH, hsdla_cx *const *dS,
         }
         CUDA_TRY(ctx, cudaEventRecord(ctx->evs[3], st));
         CUDA_TRY(ctx, cudaEventSynchronize(ctx->evs[3]));
-        float a = 0, b = 0, c = 0;
+        float a = 0, b = 0, c = 0, d = 0;
         cudaEventElapsedTime(&a, ctx->evs[0], ctx->evs[1]);
         cudaEventElapsedTime(&b, ctx->evs[1], ctx->evs[2]);
         cudaEventElapsedTime(&c, ctx->evs[2], ctx->evs[3]);
-        ms_ab += a; ms_t += b; ms_c += c;
+        cudaEventElapsedTime(&d, ctx->evs[4], ctx->evs[5]);
+        ms_ab += a; ms_t += b; ms_c += c; ms_dom = d;
     }
     CUDA_TRY(ctx, cudaEventRecord(ctx->ev1, st));
     CUDA_TRY(ctx, cudaEventSynchronize(ctx->ev1));
@@ -597,7 +727,10 @@ int hsdla_plan_execute(hsdla_plan *pl, hsdla_cx *const *dH, hsdla_cx *const *dS,
         rep->ms_construct_ab = ms_ab;
         rep->ms_tapply = ms_t;
         rep->ms_contract = ms_c;
+        rep->ms_dominant = ms_dom;
+        rep->dominant_flop = dom_flop;
         rep->num_slices = pl->opts.precision == HSDLA_PREC_OZAKI_FP8 ? pl->oz.num_slices : 0;
+        rep->est_rel_err = pl->est_err;
         rep->kernel_launches = pl->launches;
     }
     return HSDLA_OK;

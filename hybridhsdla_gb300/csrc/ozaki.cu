@@ -600,7 +600,7 @@ int64_t job_tiles(const OzJob &j) {
 }
 
 int launch_gemm(std::vector<OzJob> &jobs, const CUtensorMap *maps, int s, int *d_err, OzJob *d_jobs,
-                cudaStream_t st) {
+                cudaStream_t st, cudaEvent_t ev0 = nullptr, cudaEvent_t ev1 = nullptr) {
     int64_t total = 0;
     for (auto &j : jobs) {
         j.tiles_n = (j.n + kTileN - 1) / kTileN;
@@ -617,9 +617,11 @@ int launch_gemm(std::vector<OzJob> &jobs, const CUtensorMap *maps, int s, int *d
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
     const int64_t grid = std::min<int64_t>(total, nsm);
+    if (ev0) cudaEventRecord(ev0, st);
     oz_gemm_kernel<<<(unsigned)grid, kThreads, smem, st>>>(maps[0], maps[1], maps[2], maps[3], d_jobs,
                                                             (int)jobs.size(), total, s, d_err);
     e = cudaGetLastError();
+    if (ev1) cudaEventRecord(ev1, st);
     if (e != cudaSuccess) { g_oz_err = cudaGetErrorString(e); return HSDLA_ERR_CUDA; }
     // the job table is read by the kernel: keep the host copy alive until it is consumed
     e = cudaStreamSynchronize(st);
@@ -631,7 +633,7 @@ int launch_gemm(std::vector<OzJob> &jobs, const CUtensorMap *maps, int s, int *d
 
 // ==================================================================== API
 int ozaki_plan_init(OzakiPlan &oz, int num_slices, double target) {
-    if (num_slices == 0) num_slices = 10;
+    if (num_slices == 0) num_slices = kOzDefaultSlices;
     if (num_slices < 2 || num_slices > kOzMaxSlices) { g_oz_err = "num_slices outside [2, 12]"; return HSDLA_ERR_ARG; }
     oz.num_slices = num_slices;
     oz.target = target;
@@ -764,7 +766,7 @@ int ozaki_pipeline(OzakiPlan &oz, const OzakiInputs &in, double2 *S, double2 *H,
         j.el = dC.expo; j.er = which == 0 ? dW.expo : dX.expo;
         jobs.push_back(j);
     }
-    rc = launch_gemm(jobs, maps, s, oz.d_error, d_jobs, st);
+    rc = launch_gemm(jobs, maps, s, oz.d_error, d_jobs, st, in.ev_dom0, in.ev_dom1);
     nl += 1;
     if (launches) *launches = nl;
     return rc;

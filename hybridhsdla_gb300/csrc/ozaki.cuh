@@ -6,6 +6,9 @@
 namespace hsdla {
 
 constexpr int kOzMaxSlices = 12;
+// 11 digits (4 + 5*10 = 54 bits per value, 66 digit products) keep the relative error
+// of H and S near 1e-15 on the FLAPW workloads; 10 digits land at ~1e-13.
+constexpr int kOzDefaultSlices = 11;
 
 struct OzakiPlan {
     int num_slices = 0;          // digit slices per operand
@@ -23,6 +26,7 @@ struct OzakiInputs {
     const int32_t *atom_type;    // host array [na]
     double2 *X;
     int64_t twoL, na, nt, G;
+    cudaEvent_t ev_dom0 = nullptr, ev_dom1 = nullptr;   // recorded around the S/H launch when set
 };
 
 int ozaki_plan_init(OzakiPlan &oz, int num_slices, double target);

@@ -108,6 +108,9 @@ typedef struct hsdla_report {
     double ms_construct_ab;      /* stage times of the last un-graphed run (0 under a graph) */
     double ms_tapply;
     double ms_contract;
+    double ms_dominant;          /* device time of the dominant launch: the S/H contraction of the last k-point */
+    double dominant_flop;        /* algorithmic flops of that launch (FP8 digit products for Ozaki, FP64 for plain) */
+    double est_rel_err;          /* Ozaki: relative error predicted by the slice autotuner (0 if not tuned) */
     int32_t num_slices;          /* slices used (Ozaki) */
     int32_t num_kpoints;
     int32_t kernel_launches;     /* kernels launched per execution */

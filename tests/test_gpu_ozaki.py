@@ -105,3 +105,25 @@ def test_create_hs_ozaki_c1(ctx):
     s = synth.make_system("c1")
     res, rep = ctx.create_hs(s, precision="ozaki")
     _hs_parity(res, s)
+
+
+def test_autotuned_slices_meet_target_c1(ctx):
+    """num_slices = 0: the plan samples columns, checks them against FP64 and picks s."""
+    import torch
+    s = synth.make_system("c1")
+    pl = ctx.plan(s, precision="ozaki", num_slices=0)
+    outs = pl.alloc_outputs()
+    rep = pl.execute(outs)
+    torch.cuda.synchronize()
+    assert 9 <= rep["num_slices"] <= 12
+    assert 0 < rep["est_rel_err"] <= 0.25e-13
+    H = np.tril(outs[0][0].cpu().numpy().T)
+    S = np.tril(outs[0][1].cpu().numpy().T)
+    _hs_parity([(H, S)], s)
+    pl.close()
+
+
+def test_create_hs_ozaki_rotations(ctx):
+    s = synth.with_rotations(synth.make_system("t1"))
+    res, _ = ctx.create_hs(s, precision="ozaki")
+    _hs_parity(res, s)
