@@ -225,6 +225,8 @@ class Context:
         if rc != 0:
             raise HsdlaError(rc, "hsdla_context_create failed (no sm_100+ GPU?)")
         self.h = h
+        import weakref
+        self._plans = weakref.WeakSet()
 
     def check(self, rc: int):
         if rc != 0:
@@ -235,6 +237,9 @@ class Context:
 
     def close(self):
         if self.h:
+            # plans hold device memory of this context: destroy them first
+            for p in list(self._plans):
+                p.close()
             self.lib.hsdla_context_destroy(self.h)
             self.h = None
 
@@ -299,6 +304,7 @@ class Plan:
         ctx.check(ctx.lib.hsdla_plan_create(ctx.h, ctypes.byref(self._sh.struct), self._kh.arr, len(self.kpoints),
                                             ctypes.byref(o), ctypes.byref(h)))
         self.h = h
+        ctx._plans.add(self)
 
     def workspace_bytes(self) -> int:
         return int(self.ctx.lib.hsdla_plan_workspace_bytes(self.h))
@@ -333,9 +339,9 @@ class Plan:
         return C
 
     def close(self):
-        if getattr(self, "h", None):
+        if getattr(self, "h", None) and self.ctx.h:
             self.ctx.lib.hsdla_plan_destroy(self.h)
-            self.h = None
+        self.h = None
 
     def __del__(self):
         try:

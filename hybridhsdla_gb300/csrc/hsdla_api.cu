@@ -17,6 +17,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <set>
 #include <string>
 #include <vector>
 
@@ -36,6 +37,7 @@ struct hsdla_context {
     void *ws = nullptr;
     int64_t ws_bytes = 0;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr, evs[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+    std::set<hsdla_plan *> plans;   // live plans, destroyed with the context
 };
 
 struct PlanKpoint {
@@ -408,6 +410,7 @@ void hsdla_context_destroy(hsdla_context *ctx) {
     if (!ctx) return;
     cudaSetDevice(ctx->device);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    while (!ctx->plans.empty()) hsdla_plan_destroy(*ctx->plans.begin());
     if (ctx->ws) ctx_free(ctx, ctx->ws, ctx->ws_bytes);
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
     if (ctx->ev1) cudaEventDestroy(ctx->ev1);
@@ -572,6 +575,7 @@ int hsdla_plan_create(hsdla_context *ctx, const hsdla_system *s, const hsdla_kpo
         rc = ozaki_plan_init(pl->oz, pl->opts.num_slices, pl->opts.target_rel_err);
         if (rc) { hsdla_plan_destroy(pl); return set_err(ctx, rc, "Ozaki plan set-up failed"); }
     }
+    ctx->plans.insert(pl);
     *out = pl;
     return HSDLA_OK;
 }
@@ -594,6 +598,7 @@ void hsdla_plan_destroy(hsdla_plan *pl) {
     if (pl->d_jobs) ctx_free(ctx, pl->d_jobs, pl->jobs_cap * sizeof(Fp64Job));
     if (pl->tables) ctx_free(ctx, pl->tables, pl->tables_bytes);
     ozaki_plan_release(pl->oz);
+    ctx->plans.erase(pl);
     delete pl;
 }
 

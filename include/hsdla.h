@@ -122,6 +122,7 @@ typedef struct hsdla_plan hsdla_plan;
 
 /* Library / device set-up (replaces dev_init/dev_finalize, flapw_opt/src/wrappers.cpp:111-148). */
 int hsdla_context_create(int device, hsdla_context **ctx);
+/* Destroys the context and every plan still alive in it (plan handles become invalid). */
 void hsdla_context_destroy(hsdla_context *ctx);
 const char *hsdla_last_error(const hsdla_context *ctx);
 /* Cap on device bytes the context may allocate (0 = no cap); exceeding it returns HSDLA_ERR_NOMEM. */
