@@ -606,7 +606,7 @@ int hsdla_plan_construct_ab(hsdla_plan *pl, int32_t ik, hsdla_cx *dC, void *stre
     if (!pl || !dC || ik < 0 || ik >= (int)pl->kps.size()) return HSDLA_ERR_ARG;
     hsdla_context *ctx = pl->ctx;
     CUDA_TRY(ctx, cudaSetDevice(ctx->device));
-    cudaStream_t st = stream ? (cudaStream_t)stream : ctx->stream;
+    cudaStream_t st = (cudaStream_t)stream;   // NULL = the default (legacy) stream, as in CUDA
     if (pl->kps[ik].n_g == 0) return HSDLA_OK;
     CUDA_TRY(ctx, launch_construct_ab(pl->dsys, pl->kps[ik].dk, reinterpret_cast<double2 *>(dC), pl->twoLa, st));
     return HSDLA_OK;
@@ -617,7 +617,7 @@ int hsdla_plan_execute(hsdla_plan *pl, hsdla_cx *const *dH, hsdla_cx *const *dS,
     if (!pl || (!pl->kps.empty() && (!dH || !dS || !ld))) return HSDLA_ERR_ARG;
     hsdla_context *ctx = pl->ctx;
     CUDA_TRY(ctx, cudaSetDevice(ctx->device));
-    cudaStream_t st = stream ? (cudaStream_t)stream : ctx->stream;
+    cudaStream_t st = (cudaStream_t)stream;   // NULL = the default (legacy) stream, as in CUDA
     const int nk = (int)pl->kps.size();
     for (int i = 0; i < nk; ++i) {
         if (pl->kps[i].n_g == 0) continue;
@@ -812,7 +812,7 @@ int hsdla_zherkx_lower(hsdla_context *ctx, int32_t precision, int32_t num_slices
     if (n < 0 || k < 0 || !dP || !dQ || !dOut || ldp < k || ldq < k || ldo < n)
         return set_err(ctx, HSDLA_ERR_ARG, "bad zherkx arguments");
     CUDA_TRY(ctx, cudaSetDevice(ctx->device));
-    cudaStream_t st = stream ? (cudaStream_t)stream : ctx->stream;
+    cudaStream_t st = (cudaStream_t)stream;   // NULL = the default (legacy) stream, as in CUDA
     if (n == 0) return HSDLA_OK;
     if (precision == HSDLA_PREC_FP64) {
         std::vector<Fp64Job> jobs(1);

@@ -148,7 +148,8 @@ int hsdla_create_hs(hsdla_context *ctx, const hsdla_system *sys, const hsdla_kpo
  * the device workspace (A/B tensors, T blocks, digit slices). */
 int hsdla_plan_create(hsdla_context *ctx, const hsdla_system *sys, const hsdla_kpoint *kpts, int32_t nk,
                       const hsdla_opts *opts, hsdla_plan **plan);
-/* dH[i], dS[i]: DEVICE pointers; stream: a cudaStream_t or NULL for the context stream. */
+/* dH[i], dS[i]: DEVICE pointers; stream: a cudaStream_t (NULL = the default stream, as in CUDA).
+ * The call returns after the work on that stream has completed. */
 int hsdla_plan_execute(hsdla_plan *plan, hsdla_cx *const *dH, hsdla_cx *const *dS, const int64_t *ld,
                        void *stream, hsdla_report *report);
 int64_t hsdla_plan_workspace_bytes(const hsdla_plan *plan);
