@@ -80,7 +80,7 @@ class ReportStruct(ctypes.Structure):
 EXPORTS = ["hsdla_context_create", "hsdla_context_destroy", "hsdla_last_error", "hsdla_set_mem_cap",
            "hsdla_prepare_tmat", "hsdla_create_hs", "hsdla_plan_create", "hsdla_plan_execute",
            "hsdla_plan_workspace_bytes", "hsdla_plan_destroy", "hsdla_plan_construct_ab",
-           "hsdla_zherkx_lower"]
+           "hsdla_zherkx_lower", "hsdla_zherkx_lower_noalloc"]
 
 _lib = None
 
@@ -124,6 +124,8 @@ def load(build_if_missing: bool = True):
     L.hsdla_plan_construct_ab.argtypes = [vp, ctypes.c_int32, vp, vp]
     L.hsdla_zherkx_lower.argtypes = [vp, ctypes.c_int32, ctypes.c_int32, ctypes.c_int64, ctypes.c_int64, vp,
                                      ctypes.c_int64, vp, ctypes.c_int64, vp, vp, ctypes.c_int64, vp]
+    L.hsdla_zherkx_lower_noalloc.argtypes = [ctypes.c_int32, ctypes.c_int64, ctypes.c_int64, vp, ctypes.c_int64, vp,
+                                             ctypes.c_int64, vp, vp, ctypes.c_int64, vp]
     _lib = L
     return L
 
@@ -287,6 +289,28 @@ class Context:
                                                ctypes.c_void_p(w.data_ptr()) if w is not None else None,
                                                ctypes.c_void_p(out.data_ptr()), n, st))
         return out
+
+
+def zherkx_lower_noalloc(P, Q=None, w=None, num_slices=0, out=None, stream=None):
+    """Allocation-free Ozaki contraction (``hsdla_zherkx_lower_noalloc``): lower
+    triangle of P^H diag(w) Q for device complex128 K x n matrices given as torch
+    tensors of shape (n, K).  The library itself allocates no device memory for it;
+    its scratch is a static device array of 128 MiB.  ``out`` must be supplied by a
+    caller that cannot allocate; otherwise a torch buffer is made here."""
+    import torch
+    L_ = load()
+    Q = P if Q is None else Q
+    n, K = P.shape
+    if out is None:
+        out = torch.zeros((n, n), dtype=torch.complex128, device=P.device)
+    st = ctypes.c_void_p(stream.cuda_stream if stream is not None else torch.cuda.current_stream().cuda_stream)
+    rc = L_.hsdla_zherkx_lower_noalloc(int(num_slices), n, K, ctypes.c_void_p(P.data_ptr()), K,
+                                       ctypes.c_void_p(Q.data_ptr()), K,
+                                       ctypes.c_void_p(w.data_ptr()) if w is not None else None,
+                                       ctypes.c_void_p(out.data_ptr()), n, st)
+    if rc != 0:
+        raise HsdlaError(rc, "hsdla_zherkx_lower_noalloc failed")
+    return out
 
 
 class Plan:

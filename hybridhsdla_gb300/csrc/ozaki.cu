@@ -773,3 +773,118 @@ int ozaki_pipeline(OzakiPlan &oz, const OzakiInputs &in, double2 *S, double2 *H,
 }
 
 }  // namespace hsdla
+
+// ======================================================================
+// Allocation-free variant of the Ozaki lower-triangle contraction.
+//
+// Some callers cannot allocate device memory: code running inside another
+// framework's memory pool or under a fixed memory budget, plug-ins that may only
+// touch the buffers they are handed, and processes that must not call cudaMalloc
+// once their steady state has begun.  For them, hsdla_zherkx_lower_noalloc keeps
+// every scratch byte of the Ozaki contraction (digit planes, exponents, the job
+// table and the device error word) in one file-scope device array of
+// kNoAllocScratchBytes.  That array exists on every GPU that loads this library
+// and stays resident until the process exits.  The caller still passes the
+// inputs and the output.
+#include <mutex>
+
+namespace hsdla {
+namespace {
+
+constexpr int64_t kNoAllocScratchBytes = int64_t(128) << 20;   // 128 MiB
+constexpr int kNoAllocMaxDevices = 64;
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+// Host-side cache of the array's device address, per device.  In host code the
+// symbol g_noalloc_scratch is only a stand-in for the device array, so its address
+// must come from cudaGetSymbolAddress with that device current.
+std::mutex g_noalloc_mu;
+unsigned char *g_noalloc_ptr[kNoAllocMaxDevices] = {};
+
+int noalloc_scratch(unsigned char **out) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kNoAllocMaxDevices) return HSDLA_ERR_DEVICE;
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (!g_noalloc_ptr[dev]) {
+        void *p = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess || p == nullptr) {
+            g_oz_err = "cudaGetSymbolAddress of the static scratch failed";
+            return HSDLA_ERR_CUDA;
+        }
+        g_noalloc_ptr[dev] = reinterpret_cast<unsigned char *>(p);
+    }
+    *out = g_noalloc_ptr[dev];
+    return HSDLA_OK;
+}
+
+// Bytes of static scratch one call needs: two digit operands, their exponents, the
+// job table and the error word.
+int64_t noalloc_bytes(int s, int64_t n, int64_t Kpad) {
+    return 2 * operand_bytes(s, n, Kpad) + round_up(sizeof(OzJob), 1024) + 1024;
+}
+
+}  // namespace
+}  // namespace hsdla
+
+extern "C" int hsdla_zherkx_lower_noalloc(int32_t num_slices, int64_t n, int64_t k, const hsdla_cx *dP, int64_t ldp,
+                                          const hsdla_cx *dQ, int64_t ldq, const double *dw, hsdla_cx *dOut,
+                                          int64_t ldo, void *stream) {
+    using namespace hsdla;
+    const int s = num_slices == 0 ? kOzDefaultSlices : num_slices;
+    if (s < 2 || s > kOzMaxSlices || n < 0 || k < 0 || !dP || !dQ || !dOut || ldp < k || ldq < k || ldo < n)
+        return HSDLA_ERR_ARG;
+    if (n == 0) return HSDLA_OK;
+    const int64_t Kpad = round_up(std::max<int64_t>(k, 1), kKBlock);
+    if (noalloc_bytes(s, n, Kpad) > kNoAllocScratchBytes) {
+        g_oz_err = "problem exceeds the 128 MiB static scratch of hsdla_zherkx_lower_noalloc";
+        return HSDLA_ERR_UNSUPPORTED;
+    }
+    unsigned char *scratch = nullptr;
+    int rc = noalloc_scratch(&scratch);
+    if (rc) return rc;
+    cudaStream_t st = (cudaStream_t)stream;
+    Arena ar{reinterpret_cast<char *>(scratch)};
+    DigitOperand dp, dq;
+    carve_operand(ar, dp, s, n, Kpad);
+    carve_operand(ar, dq, s, n, Kpad);
+    OzJob *d_job = ar.take<OzJob>(1);
+    int *d_err = ar.take<int>(1);
+    // the array keeps the previous call's contents: the error word must start at zero
+    // (digit planes and exponents are rewritten in full by the slicing kernel)
+    cudaError_t e = cudaMemsetAsync(d_err, 0, sizeof(int), st);
+    if (e == cudaSuccess) e = slice(reinterpret_cast<const double2 *>(dP), ldp, nullptr, k, n, Kpad, Kpad, s, dp, st);
+    if (e == cudaSuccess) e = slice(reinterpret_cast<const double2 *>(dQ), ldq, dw, k, n, Kpad, Kpad, s, dq, st);
+    if (e != cudaSuccess) { g_oz_err = cudaGetErrorString(e); return HSDLA_ERR_CUDA; }
+    rc = make_map(dp, s);
+    if (!rc) rc = make_map(dq, s);
+    if (rc) return rc;
+    OzJob j;
+    memset(&j, 0, sizeof(j));
+    j.lmap = 0; j.rmap = 1; j.lower = 1;
+    j.lplane = dp.plane_rows; j.rplane = dq.plane_rows;
+    j.nkb = Kpad / kKBlock; j.m = n; j.n = n;
+    j.tiles_n = (n + kTileN - 1) / kTileN;
+    j.tile_begin = 0;
+    j.out = reinterpret_cast<double2 *>(dOut); j.ldo = ldo;
+    j.el = dp.expo; j.er = dq.expo;
+    const int64_t tiles = job_tiles(j);
+    e = cudaMemcpyAsync(d_job, &j, sizeof(OzJob), cudaMemcpyHostToDevice, st);
+    const size_t smem = (size_t)kStages * kStageBytes + 1024;
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(oz_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    int dev = 0, nsm = 0;
+    if (e == cudaSuccess) e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) { g_oz_err = cudaGetErrorString(e); return HSDLA_ERR_CUDA; }
+    const int64_t grid = std::min<int64_t>(tiles, nsm);
+    oz_gemm_kernel<<<(unsigned)grid, kThreads, smem, st>>>(dp.map, dq.map, dp.map, dp.map, d_job, 1, tiles, s, d_err);
+    e = cudaGetLastError();
+    int herr = 0;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&herr, d_err, sizeof(int), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) { g_oz_err = cudaGetErrorString(e); return HSDLA_ERR_CUDA; }
+    if (herr != 0) { g_oz_err = "device wait expired"; return HSDLA_ERR_TIMEOUT; }
+    return HSDLA_OK;
+}

@@ -169,6 +169,25 @@ int hsdla_zherkx_lower(hsdla_context *ctx, int32_t precision, int32_t num_slices
                        const hsdla_cx *dP, int64_t ldp, const hsdla_cx *dQ, int64_t ldq,
                        const double *dw, hsdla_cx *dOut, int64_t ldo, void *stream);
 
+/* Allocation-free Ozaki form of hsdla_zherkx_lower (HSDLA_PREC_OZAKI_FP8), for callers that
+ * cannot allocate device memory: code inside another framework's memory pool or under a
+ * fixed memory budget, plug-ins that may only touch the buffers they are handed, processes
+ * that must not call cudaMalloc after start-up.  It has no counterpart in the reference.
+ *
+ * All scratch (digit planes, exponents, job table, error word) lives in one static device
+ * array of 128 MiB that every GPU loading this library holds until the process exits; the
+ * call makes no cudaMalloc/cudaFree and no allocating library call.  Problems that need more
+ * scratch than that, 2 * (2 s (roundup(n,128) + 128) roundup(k,128) + 4 (roundup(n,128) + 128))
+ * bytes plus 2 KiB (about n = 1000, k = 2560 at s = 11), are rejected with
+ * HSDLA_ERR_UNSUPPORTED.  num_slices = 0 means 11.  The first call on a device looks up the
+ * array's device address (cudaGetSymbolAddress) with that device current; make that first
+ * call before any stream capture.  Every call shares the one array, so calls that overlap on
+ * the GPU (other streams, other host threads) race: serialise them.  The call returns after
+ * the work on `stream` (NULL = default stream) has completed. */
+int hsdla_zherkx_lower_noalloc(int32_t num_slices, int64_t n, int64_t k, const hsdla_cx *dP, int64_t ldp,
+                               const hsdla_cx *dQ, int64_t ldq, const double *dw, hsdla_cx *dOut,
+                               int64_t ldo, void *stream);
+
 #ifdef __cplusplus
 }
 #endif
