@@ -17,6 +17,8 @@
 // consecutive 16-byte elements (coalesced, full 32-byte sectors).  Output
 // layout: rows ordered per atom as [A_a (L rows); B_a (L rows)], so that the
 // stacked contraction operand [A;B] is one column-major matrix.
+#include <algorithm>
+
 #include "common.cuh"
 
 namespace hsdla {
@@ -133,7 +135,7 @@ __device__ __forceinline__ double2 cmul(double2 a, double2 b) {
 
 template <bool kRot>
 __global__ void __launch_bounds__(kThreads) construct_ab_kernel(DevSystem sys, DevKpoint kp, double2 *C,
-                                                                int64_t ldc) {
+                                                                int64_t ldc, double2 *M, int64_t ldm) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int L = sys.L, nl = sys.max_lmax + 1, na = sys.num_atoms, nt = sys.num_types;
     const int twoL = 2 * L;
@@ -218,6 +220,28 @@ __global__ void __launch_bounds__(kThreads) construct_ab_kernel(DevSystem sys, D
                 }
                 col[idx] = out;
             }
+            // phase-free per-type rows M_t = [A_t; B_t] / e^{i 2pi K.tau} (shared by every atom of type t)
+            if (M) {
+                double2 *mcol = M + ldm * gi;
+                const int nrm = twoL * nt;
+                for (int idx = threadIdx.x; idx < nrm; idx += blockDim.x) {
+                    const int t = idx / twoL;
+                    const int r = idx - t * twoL;
+                    const bool isB = r >= L;
+                    const int lm = isB ? r - L : r;
+                    const int l = l_of[lm];
+                    double2 out = make_double2(0.0, 0.0);
+                    if (l <= sys.type_lmax[t]) {
+                        const int tl = t * nl + l;
+                        const double2 common = make_double2(sys.vol_prefac * sys.inv_w[tl], 0.0);
+                        const double2 y = ylm[lm];
+                        const double2 ycc = cmul(make_double2(y.x, -y.y), common);
+                        const double f = isB ? bu[tl] : au[tl];
+                        out = make_double2(ycc.x * f, ycc.y * f);
+                    }
+                    mcol[idx] = out;
+                }
+            }
         } else {
             for (int j0 = 0; j0 < na; j0 += kRotChunk) {
                 const int nj = min(kRotChunk, na - j0);
@@ -261,8 +285,48 @@ __global__ void __launch_bounds__(kThreads) construct_ab_kernel(DevSystem sys, D
 
 }  // namespace
 
+// X[2L a + r, g] = e^{i 2pi (k+g).tau_a} Z[2L t(a) + r, g]: the per-atom T application rebuilt
+// from the per-type product Z_t = T_t M_t.
+__global__ void __launch_bounds__(kThreads) apply_phase_kernel(DevSystem sys, DevKpoint kp, const double2 *Z,
+                                                               int64_t ldz, double2 *X, int64_t ldx) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    double2 *ph = reinterpret_cast<double2 *>(smem_raw);       // [na]
+    const int twoL = 2 * sys.L, na = sys.num_atoms;
+    for (int64_t gi = blockIdx.x; gi < kp.n_g; gi += gridDim.x) {
+        __syncthreads();
+        const int32_t *gv = kp.g + 3 * gi;
+        const double K0 = kp.k[0] + gv[0], K1 = kp.k[1] + gv[1], K2 = kp.k[2] + gv[2];
+        for (int j = threadIdx.x; j < na; j += blockDim.x) {
+            const double *p = sys.atom_pos + 3 * j;
+            double sn, cs;
+            sincos(2 * kPi * (K0 * p[0] + K1 * p[1] + K2 * p[2]), &sn, &cs);
+            ph[j] = make_double2(cs, sn);
+        }
+        __syncthreads();
+        const double2 *zc = Z + ldz * gi;
+        double2 *xc = X + ldx * gi;
+        const int64_t nrow = (int64_t)twoL * na;
+        for (int64_t idx = threadIdx.x; idx < nrow; idx += blockDim.x) {
+            const int j = (int)(idx / twoL);
+            const int r = (int)(idx - (int64_t)j * twoL);
+            xc[idx] = cmul(ph[j], zc[(int64_t)twoL * sys.atom_type[j] + r]);
+        }
+    }
+}
+
+cudaError_t launch_apply_phase(const DevSystem &sys, const DevKpoint &kp, const double2 *Z, int64_t ldz,
+                               double2 *X, int64_t ldx, cudaStream_t st) {
+    int dev = 0, nsm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    const int64_t grid = std::min<int64_t>(kp.n_g, (int64_t)nsm * 8);
+    const size_t smem = sizeof(double2) * sys.num_atoms;
+    apply_phase_kernel<<<(unsigned)grid, kThreads, smem, st>>>(sys, kp, Z, ldz, X, ldx);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_construct_ab(const DevSystem &sys, const DevKpoint &kp, double2 *C, int64_t ldc,
-                                cudaStream_t st) {
+                                cudaStream_t st, double2 *M, int64_t ldm) {
     const bool rot = sys.atom_rotmat != nullptr;
     const int nl = sys.max_lmax + 1;
     size_t smem = sizeof(double) * 2 * sys.num_types * nl + sizeof(double2) * sys.num_atoms +
@@ -274,10 +338,11 @@ cudaError_t launch_construct_ab(const DevSystem &sys, const DevKpoint &kp, doubl
     const int64_t grid = std::min<int64_t>(kp.n_g, (int64_t)nsm * 8);
     if (rot) {
         cudaFuncSetAttribute(construct_ab_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        construct_ab_kernel<true><<<(unsigned)grid, kThreads, smem, st>>>(sys, kp, C, ldc);
+        if (M) return cudaErrorInvalidValue;     // per-type rows exist only when atoms share the rotation
+        construct_ab_kernel<true><<<(unsigned)grid, kThreads, smem, st>>>(sys, kp, C, ldc, nullptr, 0);
     } else {
         cudaFuncSetAttribute(construct_ab_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        construct_ab_kernel<false><<<(unsigned)grid, kThreads, smem, st>>>(sys, kp, C, ldc);
+        construct_ab_kernel<false><<<(unsigned)grid, kThreads, smem, st>>>(sys, kp, C, ldc, M, ldm);
     }
     return cudaGetLastError();
 }

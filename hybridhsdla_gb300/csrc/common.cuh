@@ -45,8 +45,13 @@ struct DevKpoint {
 
 // ----------------------------------------------------------- kernels (host)
 // (a) matching tensors of one k-point into C: (2 L a) x n_g column-major, per-atom [A_a; B_a]
+// Optionally also the phase-free per-type rows M ((2 L nt) x n_g, ld ldm) when no atom carries
+// its own rotation (M_t = C_a e^{-i 2pi K.tau_a} for every atom a of type t).
 cudaError_t launch_construct_ab(const DevSystem &sys, const DevKpoint &kp, double2 *C, int64_t ldc,
-                                cudaStream_t st);
+                                cudaStream_t st, double2 *M = nullptr, int64_t ldm = 0);
+// X[2L a + r, g] = e^{i 2pi (k+g).tau_a} Z[2L t(a) + r, g]
+cudaError_t launch_apply_phase(const DevSystem &sys, const DevKpoint &kp, const double2 *Z, int64_t ldz,
+                               double2 *X, int64_t ldx, cudaStream_t st);
 
 // FP64 tiled contraction OUT = P^H diag(w) Q over a batch of jobs (kernels (b) and (c) in FP64).
 struct Fp64Job {

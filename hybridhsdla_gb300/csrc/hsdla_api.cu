@@ -65,6 +65,7 @@ struct hsdla_plan {
     std::vector<Fp64Job> h_jobs;
     OzakiPlan oz{};
     bool autotune = false;           // Ozaki slice count still to be chosen from the data
+    bool hoist = false;              // T application per type (no atom carries its own rotation)
     double est_err = 0.0;            // autotuner's predicted relative error
     int launches = 0;
 };
@@ -485,6 +486,7 @@ int hsdla_plan_create(hsdla_context *ctx, const hsdla_system *s, const hsdla_kpo
     if (pl->opts.target_rel_err <= 0.0) pl->opts.target_rel_err = 1e-13;
     const int na = s->num_atoms, nt = s->num_types, nl = s->max_lmax + 1, L = nl * nl;
     pl->L = L; pl->na = na; pl->nt = nt; pl->max_lmax = s->max_lmax;
+    pl->hoist = s->atom_rotmat == nullptr;
     pl->twoLa = 2 * (int64_t)L * na;
     pl->atom_type.assign(s->atom_type, s->atom_type + na);
 
@@ -585,6 +587,7 @@ int64_t hsdla_plan_workspace_bytes(const hsdla_plan *pl) {
     int64_t ngmax = 0;
     for (auto &k : pl->kps) ngmax = std::max(ngmax, k.n_g);
     int64_t b = 2 * (int64_t)sizeof(double2) * pl->twoLa * ngmax;   // C and X
+    if (pl->hoist) b += 2 * (int64_t)sizeof(double2) * 2 * pl->L * pl->nt * ngmax + 1024;   // M and Z
     if (pl->opts.precision == HSDLA_PREC_OZAKI_FP8)
         b += 1024 + ozaki_pipeline_workspace(pl->oz.num_slices, 2 * (int64_t)pl->L, pl->na, pl->nt, ngmax);
     return b;
@@ -639,9 +642,12 @@ int hsdla_plan_execute(hsdla_plan *pl, hsdla_cx *const *dH, hsdla_cx *const *dS,
         C = reinterpret_cast<double2 *>(ws);
     }
     double2 *X = C + pl->twoLa * ngmax;
+    const int64_t ldm = 2 * (int64_t)pl->L * pl->nt;
+    double2 *Mt = pl->hoist ? X + pl->twoLa * ngmax : nullptr;
+    double2 *Zt = pl->hoist ? Mt + ldm * ngmax : nullptr;
+    char *tail = reinterpret_cast<char *>(pl->hoist ? Zt + ldm * ngmax : X + pl->twoLa * ngmax);
     // the digit workspace needs 1024-byte alignment (TMA boxes, SW128 atoms)
-    char *oz_ws = reinterpret_cast<char *>((reinterpret_cast<uintptr_t>(X + pl->twoLa * ngmax) + 1023) &
-                                           ~uintptr_t(1023));
+    char *oz_ws = reinterpret_cast<char *>((reinterpret_cast<uintptr_t>(tail) + 1023) & ~uintptr_t(1023));
     const int64_t L = pl->L, twoL = 2 * L, twoLa = pl->twoLa;
     pl->launches = 0;
     float ms_ab = 0.f, ms_t = 0.f, ms_c = 0.f, ms_dom = 0.f;
@@ -651,19 +657,30 @@ int hsdla_plan_execute(hsdla_plan *pl, hsdla_cx *const *dH, hsdla_cx *const *dS,
         const int64_t G = pl->kps[i].n_g;
         if (G == 0) continue;
         CUDA_TRY(ctx, cudaEventRecord(ctx->evs[0], st));
-        CUDA_TRY(ctx, launch_construct_ab(pl->dsys, pl->kps[i].dk, C, twoLa, st));
+        CUDA_TRY(ctx, launch_construct_ab(pl->dsys, pl->kps[i].dk, C, twoLa, st, Mt, ldm));
         pl->launches++;
         CUDA_TRY(ctx, cudaEventRecord(ctx->evs[1], st));
-        // (b) X_a = T_a C_a for every atom, one launch
+        // (b) X_a = T_a C_a: per type (Z_t = T_t M_t, expanded by the phases) or per atom, one launch
         pl->h_jobs.clear();
-        for (int j = 0; j < pl->na; ++j) {
-            Fp64Job jb{};
-            jb.P = pl->Tfull + (int64_t)pl->atom_type[j] * twoL * twoL; jb.ldp = twoL;
-            jb.Q = C + twoL * j; jb.ldq = twoLa;
-            jb.w = nullptr;
-            jb.out = X + twoL * j; jb.ldo = twoLa;
-            jb.m = twoL; jb.n = G; jb.k = twoL; jb.lower = 0;
-            pl->h_jobs.push_back(jb);
+        if (pl->hoist) {
+            for (int t = 0; t < pl->nt; ++t) {
+                Fp64Job jb{};
+                jb.P = pl->Tfull + (int64_t)t * twoL * twoL; jb.ldp = twoL;
+                jb.Q = Mt + twoL * t; jb.ldq = ldm;
+                jb.out = Zt + twoL * t; jb.ldo = ldm;
+                jb.m = twoL; jb.n = G; jb.k = twoL; jb.lower = 0;
+                pl->h_jobs.push_back(jb);
+            }
+        } else {
+            for (int j = 0; j < pl->na; ++j) {
+                Fp64Job jb{};
+                jb.P = pl->Tfull + (int64_t)pl->atom_type[j] * twoL * twoL; jb.ldp = twoL;
+                jb.Q = C + twoL * j; jb.ldq = twoLa;
+                jb.w = nullptr;
+                jb.out = X + twoL * j; jb.ldo = twoLa;
+                jb.m = twoL; jb.n = G; jb.k = twoL; jb.lower = 0;
+                pl->h_jobs.push_back(jb);
+            }
         }
         if (pl->opts.precision != HSDLA_PREC_FP64) pl->h_jobs.clear();   // the Ozaki pipeline emulates (b) too
         const int64_t nt_b = assign_tiles(pl->h_jobs, 0);
@@ -683,8 +700,14 @@ int hsdla_plan_execute(hsdla_plan *pl, hsdla_cx *const *dH, hsdla_cx *const *dS,
         if (!pl->h_jobs.empty()) {
             rc = upload_jobs(pl, st);
             if (rc) return rc;
+        }
+        if (nb > 0) {
             CUDA_TRY(ctx, launch_fp64_jobs(pl->d_jobs, (int)nb, nt_b, st));
             pl->launches++;
+            if (pl->hoist) {
+                CUDA_TRY(ctx, launch_apply_phase(pl->dsys, pl->kps[i].dk, Zt, ldm, X, twoLa, st));
+                pl->launches++;
+            }
         }
         CUDA_TRY(ctx, cudaEventRecord(ctx->evs[2], st));
         const double lower_cflop = 4.0 * (double)G * (double)(G + 1) * (double)twoLa;   // one lower triangle
@@ -702,6 +725,7 @@ int hsdla_plan_execute(hsdla_plan *pl, hsdla_cx *const *dH, hsdla_cx *const *dS,
             in.C = C; in.Tfull = pl->Tfull; in.w = pl->w; in.atom_type = pl->atom_type.data(); in.X = X;
             in.twoL = twoL; in.na = pl->na; in.nt = pl->nt; in.G = G;
             in.ev_dom0 = ctx->evs[4]; in.ev_dom1 = ctx->evs[5];
+            if (pl->hoist) { in.M = Mt; in.Z = Zt; in.sys = &pl->dsys; in.kp = &pl->kps[i].dk; }
             rc = ozaki_pipeline(pl->oz, in, reinterpret_cast<double2 *>(dS[i]), reinterpret_cast<double2 *>(dH[i]),
                                 ld[i], oz_ws, st, &nl);
             if (rc) return set_err(ctx, rc, "Ozaki contraction failed: %s", ozaki_last_error());

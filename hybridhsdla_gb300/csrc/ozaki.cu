@@ -191,6 +191,21 @@ __device__ __forceinline__ void tile_coords(const OzJob &j, int64_t x, int64_t &
         tn = x - tm * j.tiles_n;
     }
 }
+// Tile g of the launch: from the host-built schedule (job, tm, tn) when given, else the
+// jobs' own row-major order.
+__device__ __forceinline__ const OzJob &resolve_tile(const OzJob *jobs, int num_jobs, const int4 *tile_list,
+                                                     int64_t tile, int64_t &tm, int64_t &tn) {
+    if (tile_list) {
+        const int4 e = tile_list[tile];
+        tm = e.y;
+        tn = e.z;
+        return jobs[e.x];
+    }
+    const OzJob &j = jobs[job_of(jobs, num_jobs, tile)];
+    tile_coords(j, tile - j.tile_begin, tm, tn);
+    return j;
+}
+
 // k-blocks per exact accumulation chunk on diagonal t (pairs = t - 1 for t <= s + 1)
 __host__ __device__ __forceinline__ int64_t chunk_kblocks(int pairs) {
     const int64_t terms_per_kb = (int64_t)2 * kKBlock * pairs * 256;   // re/im products x max |product|
@@ -208,7 +223,8 @@ struct __align__(8) Barriers {
 __global__ void __launch_bounds__(kThreads, 1)
     oz_gemm_kernel(const __grid_constant__ CUtensorMap map0, const __grid_constant__ CUtensorMap map1,
                    const __grid_constant__ CUtensorMap map2, const __grid_constant__ CUtensorMap map3,
-                   const OzJob *__restrict__ jobs, int num_jobs, int64_t total_tiles, int s, int *err) {
+                   const OzJob *__restrict__ jobs, int num_jobs, int64_t total_tiles, int s, int *err,
+                   const int4 *__restrict__ tile_list) {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     // 1024-byte alignment of the stage buffers (SW128 atoms)
     unsigned char *smem = reinterpret_cast<unsigned char *>(
@@ -247,9 +263,8 @@ __global__ void __launch_bounds__(kThreads, 1)
             int64_t issued = 0;
             bool ok = true;
             for (int64_t tile = blockIdx.x; ok && tile < total_tiles; tile += gridDim.x) {
-                const OzJob &j = jobs[job_of(jobs, num_jobs, tile)];
                 int64_t tm, tn;
-                tile_coords(j, tile - j.tile_begin, tm, tn);
+                const OzJob &j = resolve_tile(jobs, num_jobs, tile_list, tile, tm, tn);
                 const CUtensorMap *lm = map_of(j.lmap), *rm = map_of(j.rmap);
                 for (int t = 2; ok && t <= s + 1; ++t) {
                     const int ilo = max(1, t - s), ihi = min(s, t - 1);
@@ -296,7 +311,8 @@ __global__ void __launch_bounds__(kThreads, 1)
             const uint32_t id_pos = idesc_f8(false), id_neg = idesc_f8(true);
             const uint32_t sbase = smem_u32(smem);
             for (int64_t tile = blockIdx.x; ok && tile < total_tiles; tile += gridDim.x) {
-                const OzJob &j = jobs[job_of(jobs, num_jobs, tile)];
+                int64_t tm_, tn_;
+                const OzJob &j = resolve_tile(jobs, num_jobs, tile_list, tile, tm_, tn_);
                 for (int t = 2; ok && t <= s + 1; ++t) {
                     const int ilo = max(1, t - s), ihi = min(s, t - 1);
                     const int64_t ck = chunk_kblocks(ihi - ilo + 1);
@@ -352,9 +368,8 @@ __global__ void __launch_bounds__(kThreads, 1)
         int64_t unit = 0;
         bool ok = true;
         for (int64_t tile = blockIdx.x; ok && tile < total_tiles; tile += gridDim.x) {
-            const OzJob &j = jobs[job_of(jobs, num_jobs, tile)];
             int64_t tm, tn;
-            tile_coords(j, tile - j.tile_begin, tm, tn);
+            const OzJob &j = resolve_tile(jobs, num_jobs, tile_list, tile, tm, tn);
             const int64_t row = tm * kTileM + r_in_tile;
             const bool row_ok = row < j.m;
             const int erow = row_ok ? j.el[row] : 0;
@@ -599,8 +614,40 @@ int64_t job_tiles(const OzJob &j) {
     return j.lower ? tm * (tm + 1) / 2 : tm * tn;
 }
 
+// Host-built tile schedule.  Persistent CTAs take tiles g, g + grid, ... so tiles that are
+// close in the list run at the same time and share their operand panels in L2.  Lower-
+// triangle jobs of equal size (S and H of one k-point) are walked together in square super-
+// blocks of kSuperBlock x kSuperBlock tiles, the jobs' tiles of one (tm, tn) adjacent (they
+// share the left operand); full jobs (T application) go job by job, tile columns outermost.
+constexpr int kSuperBlock = 8;
+
+void build_schedule(const std::vector<OzJob> &jobs, std::vector<int4> &list) {
+    list.clear();
+    std::vector<char> done(jobs.size(), 0);
+    for (size_t a = 0; a < jobs.size(); ++a) {
+        if (done[a]) continue;
+        const OzJob &ja = jobs[a];
+        if (ja.lower) {
+            std::vector<int> group;
+            for (size_t b = a; b < jobs.size(); ++b)
+                if (!done[b] && jobs[b].lower && jobs[b].n == ja.n) { group.push_back((int)b); done[b] = 1; }
+            const int64_t T = (ja.n + kTileN - 1) / kTileN;
+            for (int64_t I = 0; I < T; I += kSuperBlock)
+                for (int64_t J = 0; J <= I; J += kSuperBlock)
+                    for (int64_t tm = I; tm < std::min(T, I + kSuperBlock); ++tm)
+                        for (int64_t tn = J; tn < std::min(tm + 1, J + kSuperBlock); ++tn)
+                            for (int g : group) list.push_back(make_int4(g, (int)tm, (int)tn, 0));
+        } else {
+            done[a] = 1;
+            const int64_t tmn = (ja.m + kTileM - 1) / kTileM, tnn = (ja.n + kTileN - 1) / kTileN;
+            for (int64_t tn = 0; tn < tnn; ++tn)
+                for (int64_t tm = 0; tm < tmn; ++tm) list.push_back(make_int4((int)a, (int)tm, (int)tn, 0));
+        }
+    }
+}
+
 int launch_gemm(std::vector<OzJob> &jobs, const CUtensorMap *maps, int s, int *d_err, OzJob *d_jobs,
-                cudaStream_t st, cudaEvent_t ev0 = nullptr, cudaEvent_t ev1 = nullptr) {
+                cudaStream_t st, cudaEvent_t ev0 = nullptr, cudaEvent_t ev1 = nullptr, int4 *d_list = nullptr) {
     int64_t total = 0;
     for (auto &j : jobs) {
         j.tiles_n = (j.n + kTileN - 1) / kTileN;
@@ -610,6 +657,13 @@ int launch_gemm(std::vector<OzJob> &jobs, const CUtensorMap *maps, int s, int *d
     if (total == 0) return HSDLA_OK;
     cudaError_t e = cudaMemcpyAsync(d_jobs, jobs.data(), sizeof(OzJob) * jobs.size(), cudaMemcpyHostToDevice, st);
     if (e != cudaSuccess) { g_oz_err = cudaGetErrorString(e); return HSDLA_ERR_CUDA; }
+    std::vector<int4> list;
+    if (d_list) {
+        build_schedule(jobs, list);
+        if ((int64_t)list.size() != total) { g_oz_err = "tile schedule size mismatch"; return HSDLA_ERR_ARG; }
+        e = cudaMemcpyAsync(d_list, list.data(), sizeof(int4) * list.size(), cudaMemcpyHostToDevice, st);
+        if (e != cudaSuccess) { g_oz_err = cudaGetErrorString(e); return HSDLA_ERR_CUDA; }
+    }
     const size_t smem = (size_t)kStages * kStageBytes + 1024;
     e = cudaFuncSetAttribute(oz_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) { g_oz_err = cudaGetErrorString(e); return HSDLA_ERR_CUDA; }
@@ -619,7 +673,7 @@ int launch_gemm(std::vector<OzJob> &jobs, const CUtensorMap *maps, int s, int *d
     const int64_t grid = std::min<int64_t>(total, nsm);
     if (ev0) cudaEventRecord(ev0, st);
     oz_gemm_kernel<<<(unsigned)grid, kThreads, smem, st>>>(maps[0], maps[1], maps[2], maps[3], d_jobs,
-                                                            (int)jobs.size(), total, s, d_err);
+                                                            (int)jobs.size(), total, s, d_err, d_list);
     e = cudaGetLastError();
     if (ev1) cudaEventRecord(ev1, st);
     if (e != cudaSuccess) { g_oz_err = cudaGetErrorString(e); return HSDLA_ERR_CUDA; }
@@ -663,9 +717,14 @@ int ozaki_check_device_error(OzakiPlan &oz) {
     return HSDLA_OK;
 }
 
+int64_t schedule_capacity_lower(int64_t n) {
+    const int64_t T = (n + kTileN - 1) / kTileN;
+    return T * (T + 1);                                     // two lower-triangle jobs
+}
+
 int64_t ozaki_herkx_workspace(int s, int64_t K, int64_t n) {
     const int64_t Kpad = round_up(std::max<int64_t>(K, 1), kKBlock);
-    return 2 * operand_bytes(s, n, Kpad) + 4096 + 4096;
+    return 2 * operand_bytes(s, n, Kpad) + 4096 + 4096 + round_up(sizeof(int4) * schedule_capacity_lower(n), 1024);
 }
 
 int ozaki_herkx(OzakiPlan &oz, const double2 *P, int64_t ldp, const double2 *Q, int64_t ldq, const double *w,
@@ -677,6 +736,7 @@ int ozaki_herkx(OzakiPlan &oz, const double2 *P, int64_t ldp, const double2 *Q, 
     carve_operand(ar, dp, s, n, Kpad);
     carve_operand(ar, dq, s, n, Kpad);
     OzJob *d_jobs = ar.take<OzJob>(4);
+    int4 *d_list = ar.take<int4>(schedule_capacity_lower(n));
     cudaError_t e = slice(P, ldp, nullptr, K, n, Kpad, Kpad, s, dp, st);
     if (e == cudaSuccess) e = slice(Q, ldq, w, K, n, Kpad, Kpad, s, dq, st);
     if (e != cudaSuccess) { g_oz_err = cudaGetErrorString(e); return HSDLA_ERR_CUDA; }
@@ -691,7 +751,7 @@ int ozaki_herkx(OzakiPlan &oz, const double2 *P, int64_t ldp, const double2 *Q, 
     j.lplane = dp.plane_rows; j.rplane = dq.plane_rows;
     j.nkb = Kpad / kKBlock; j.m = n; j.n = n;
     j.out = out; j.ldo = ldo; j.el = dp.expo; j.er = dq.expo;
-    rc = launch_gemm(jobs, maps, s, oz.d_error, d_jobs, st);
+    rc = launch_gemm(jobs, maps, s, oz.d_error, d_jobs, st, nullptr, nullptr, d_list);
     if (launches) *launches = 3;
     return rc;
 }
@@ -701,8 +761,10 @@ int ozaki_herkx(OzakiPlan &oz, const double2 *P, int64_t ldp, const double2 *Q, 
 int64_t ozaki_pipeline_workspace(int s, int64_t twoL, int64_t na, int64_t nt, int64_t G) {
     const int64_t bpad = round_up(twoL, kKBlock);
     const int64_t Kpad = bpad * na;
+    const int64_t tiles_t = na * ((twoL + kTileM - 1) / kTileM) * ((G + kTileN - 1) / kTileN);
+    const int64_t cap = std::max(tiles_t, schedule_capacity_lower(G));
     return 3 * operand_bytes(s, G, Kpad) + operand_bytes(s, nt * twoL, bpad) +
-           round_up(sizeof(OzJob) * (na + 4), 1024) + 4096;
+           round_up(sizeof(OzJob) * (na + 4), 1024) + 4096 + round_up(sizeof(int4) * cap, 1024);
 }
 
 int ozaki_pipeline(OzakiPlan &oz, const OzakiInputs &in, double2 *S, double2 *H, int64_t ldo, void *ws,
@@ -719,6 +781,8 @@ int ozaki_pipeline(OzakiPlan &oz, const OzakiInputs &in, double2 *S, double2 *H,
     carve_operand(ar, dX, s, G, Kpad);
     carve_operand(ar, dT, s, nt * twoL, bpad);
     OzJob *d_jobs = ar.take<OzJob>(na + 4);
+    const int64_t tiles_t = na * ((twoL + kTileM - 1) / kTileM) * ((G + kTileN - 1) / kTileN);
+    int4 *d_list = ar.take<int4>(std::max(tiles_t, schedule_capacity_lower(G)));
     int nl = 0;
     cudaError_t e = slice(in.C, K, nullptr, K, G, twoL, bpad, s, dC, st);
     if (e == cudaSuccess) e = slice(in.C, K, in.w, K, G, twoL, bpad, s, dW, st);
@@ -731,8 +795,41 @@ int ozaki_pipeline(OzakiPlan &oz, const OzakiInputs &in, double2 *S, double2 *H,
     if (!rc) rc = make_map(dT, s);
     if (rc) return rc;
     CUtensorMap maps[4] = {dC.map, dW.map, dX.map, dT.map};
-    // (b) X_a = T_t C_a for every atom: left = T digits (rows = T columns of type t), right = C digits
     std::vector<OzJob> jobs;
+    if (in.M) {
+        // (b) per type: Z_t = T_t M_t, then X_a = phase_a Z_t.  The M digits borrow the X digit
+        // region, which is free until X is sliced.
+        DigitOperand dM;
+        dM.plane_rows = dX.plane_rows;
+        dM.Kpad = bpad * nt;
+        dM.digits = dX.digits;
+        dM.expo = dX.expo;
+        e = slice(in.M, twoL * nt, nullptr, twoL * nt, G, twoL, bpad, s, dM, st);
+        if (e != cudaSuccess) { g_oz_err = cudaGetErrorString(e); return HSDLA_ERR_CUDA; }
+        nl += 1;
+        rc = make_map(dM, s);
+        if (rc) return rc;
+        CUtensorMap tmaps[4] = {dM.map, dM.map, dM.map, dT.map};
+        for (int64_t t = 0; t < nt; ++t) {
+            OzJob j;
+            memset(&j, 0, sizeof(j));
+            j.lmap = 3; j.rmap = 0; j.lower = 0;
+            j.lplane = dT.plane_rows; j.rplane = dM.plane_rows;
+            j.lrow0 = t * twoL; j.rrow0 = 0;
+            j.lk0 = 0; j.rk0 = t * bpad;
+            j.nkb = bpad / kKBlock;
+            j.m = twoL; j.n = G;
+            j.out = in.Z + twoL * t; j.ldo = twoL * nt;
+            j.el = dT.expo + t * twoL; j.er = dM.expo;
+            jobs.push_back(j);
+        }
+        rc = launch_gemm(jobs, tmaps, s, oz.d_error, d_jobs, st, nullptr, nullptr, d_list);
+        if (rc) return rc;
+        e = launch_apply_phase(*in.sys, *in.kp, in.Z, twoL * nt, in.X, K, st);
+        if (e != cudaSuccess) { g_oz_err = cudaGetErrorString(e); return HSDLA_ERR_CUDA; }
+        nl += 2;
+    } else {
+    // (b) X_a = T_t C_a for every atom: left = T digits (rows = T columns of type t), right = C digits
     for (int64_t a = 0; a < na; ++a) {
         OzJob j;
         memset(&j, 0, sizeof(j));
@@ -747,9 +844,10 @@ int ozaki_pipeline(OzakiPlan &oz, const OzakiInputs &in, double2 *S, double2 *H,
         j.el = dT.expo + t * twoL; j.er = dC.expo;
         jobs.push_back(j);
     }
-    rc = launch_gemm(jobs, maps, s, oz.d_error, d_jobs, st);
+    rc = launch_gemm(jobs, maps, s, oz.d_error, d_jobs, st, nullptr, nullptr, d_list);
     if (rc) return rc;
     nl += 1;
+    }
     e = slice(in.X, K, nullptr, K, G, twoL, bpad, s, dX, st);
     if (e != cudaSuccess) { g_oz_err = cudaGetErrorString(e); return HSDLA_ERR_CUDA; }
     nl += 1;
@@ -766,7 +864,7 @@ int ozaki_pipeline(OzakiPlan &oz, const OzakiInputs &in, double2 *S, double2 *H,
         j.el = dC.expo; j.er = which == 0 ? dW.expo : dX.expo;
         jobs.push_back(j);
     }
-    rc = launch_gemm(jobs, maps, s, oz.d_error, d_jobs, st, in.ev_dom0, in.ev_dom1);
+    rc = launch_gemm(jobs, maps, s, oz.d_error, d_jobs, st, in.ev_dom0, in.ev_dom1, d_list);
     nl += 1;
     if (launches) *launches = nl;
     return rc;
@@ -879,7 +977,8 @@ extern "C" int hsdla_zherkx_lower_noalloc(int32_t num_slices, int64_t n, int64_t
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
     if (e != cudaSuccess) { g_oz_err = cudaGetErrorString(e); return HSDLA_ERR_CUDA; }
     const int64_t grid = std::min<int64_t>(tiles, nsm);
-    oz_gemm_kernel<<<(unsigned)grid, kThreads, smem, st>>>(dp.map, dq.map, dp.map, dp.map, d_job, 1, tiles, s, d_err);
+    oz_gemm_kernel<<<(unsigned)grid, kThreads, smem, st>>>(dp.map, dq.map, dp.map, dp.map, d_job, 1, tiles, s, d_err,
+                                                            nullptr);
     e = cudaGetLastError();
     int herr = 0;
     if (e == cudaSuccess) e = cudaMemcpyAsync(&herr, d_err, sizeof(int), cudaMemcpyDeviceToHost, st);

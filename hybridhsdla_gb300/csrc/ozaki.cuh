@@ -27,6 +27,12 @@ struct OzakiInputs {
     double2 *X;
     int64_t twoL, na, nt, G;
     cudaEvent_t ev_dom0 = nullptr, ev_dom1 = nullptr;   // recorded around the S/H launch when set
+    // Per-type T application (atoms share their rotation): phase-free rows M ((2L nt) x G, ld 2L nt),
+    // FP64 workspace Z of the same shape, and the data the phase expansion X_a = phase_a Z_t needs.
+    const double2 *M = nullptr;
+    double2 *Z = nullptr;
+    const DevSystem *sys = nullptr;
+    const DevKpoint *kp = nullptr;
 };
 
 int ozaki_plan_init(OzakiPlan &oz, int num_slices, double target);
