@@ -39,6 +39,11 @@ sys.path.insert(0, ROOT)
 METRIC = "H+S gen ms/k-point & eff. TFLOP/s: emulated vs native FP64 at ≤1e-13 rel err"
 UNIT = "TFLOP/s (FP64-equivalent, 20*G^2*La + 24*L^2*a*G per k-point)"
 WORKLOAD = "c2"
+WORKLOAD_TEXT = {
+    "c0": "c0: cubic a=10 bohr, 4 atoms / 2 types, lmax 6, n_G 500, 1 k-point",
+    "c1": "c1: 14x14x20 bohr, 32 atoms / 4 types, lmax 8, n_G 3000, 1 k-point",
+    "c2": "c2: cubic a=24 bohr, 128 atoms / 8 types, lmax 10, n_G 8000, 1 k-point",
+}
 PROFILE_SUMMARY = os.path.join(ROOT, "profiles", "oz_gemm_c2.md")
 
 
@@ -186,7 +191,7 @@ def run_ours(args):
     dev = local if ws > 1 else 0
     torch.cuda.set_device(dev)
     ctx = api.Context(dev)
-    sys_ = synth.make_system(WORKLOAD)
+    sys_ = synth.make_system(args.workload)
     kp = sys_.kpoints[0]
     G = kp.n_g
     flop = sys_.flop_per_kpoint(G)
@@ -282,7 +287,7 @@ def run_ours(args):
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded generators, no dataset)",
-                "config": {"workload": "c2: cubic a=24 bohr, 128 atoms / 8 types, lmax 10, n_G 8000, 1 k-point",
+                "config": {"workload": WORKLOAD_TEXT.get(args.workload, args.workload),
                            "precision": f"ozaki-fp8 e4m3, {rep['num_slices']} digit slices",
                            "ms_per_kpoint": ms, "l2": "inputs larger than L2 (digit operands ~16 GB)",
                            "parallelism": f"replicas{ws}"},
@@ -309,6 +314,8 @@ def main():
     ap.add_argument("--ref-sample-ng", type=int, default=1500)
     ap.add_argument("--skip-fp64", action="store_true")
     ap.add_argument("--skip-cpu", action="store_true")
+    ap.add_argument("--workload", default=WORKLOAD, choices=sorted(WORKLOAD_TEXT),
+                    help="workload (default: the c2 precision-form case the metric is quoted on)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

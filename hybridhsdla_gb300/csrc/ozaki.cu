@@ -448,7 +448,8 @@ __global__ void __launch_bounds__(kSliceThreads) oz_slice_kernel(const double2 *
                                                                  const double *__restrict__ v, int64_t Kin,
                                                                  int64_t ncols, int64_t rpb, int64_t bpad, int s,
                                                                  uint8_t *__restrict__ digits, int64_t Kpad,
-                                                                 int64_t plane_rows, int32_t *__restrict__ expo) {
+                                                                 int64_t plane_rows, int32_t *__restrict__ expo,
+                                                                 int64_t pitch) {
     const int64_t g = blockIdx.x;
     __shared__ double red[kSliceThreads / 32];
     __shared__ int e_sh;
@@ -522,8 +523,8 @@ __global__ void __launch_bounds__(kSliceThreads) oz_slice_kernel(const double2 *
 #pragma unroll
         for (int i = 0; i < kOzMaxSlices; ++i) {
             if (i >= s) continue;
-            uint8_t *pr = digits + ((int64_t)(2 * i) * plane_rows + g) * Kpad + kp0;
-            uint8_t *pi = digits + ((int64_t)(2 * i + 1) * plane_rows + g) * Kpad + kp0;
+            uint8_t *pr = digits + ((int64_t)(2 * i) * plane_rows + g) * pitch + kp0;
+            uint8_t *pi = digits + ((int64_t)(2 * i + 1) * plane_rows + g) * pitch + kp0;
             *reinterpret_cast<uint2 *>(pr) = make_uint2(lo_r[i], hi_r[i]);
             *reinterpret_cast<uint2 *>(pi) = make_uint2(lo_i[i], hi_i[i]);
         }
@@ -548,25 +549,46 @@ PFN_encodeTiled get_encode() {
     return fn;
 }
 
-// digit operand: 2s planes of plane_rows x Kpad bytes
+// digit operand: 2s planes of plane_rows rows; a row holds Kpad digit bytes at a row pitch of
+// Kpad + pad bytes.  The pad keeps the pitch off a power of two: with a power-of-two pitch the
+// 128 rows of one TMA box fall on the same L2 sets and memory channels.
 struct DigitOperand {
     uint8_t *digits = nullptr;
     int32_t *expo = nullptr;
-    int64_t plane_rows = 0, Kpad = 0;
+    int64_t plane_rows = 0, Kpad = 0, pitch = 0;
     CUtensorMap map;
 };
+
+int64_t env_int(const char *name, int64_t dflt) {
+    const char *v = getenv(name);
+    if (!v || !*v) return dflt;
+    char *end = nullptr;
+    const long long x = strtoll(v, &end, 10);
+    return (end && *end == 0) ? (int64_t)x : dflt;
+}
+
+// Row pitch pad of the digit planes (bytes, multiple of 16); HSDLA_DIGIT_PITCH_PAD overrides.
+int64_t pitch_pad() {
+    static const int64_t p = [] {
+        int64_t x = env_int("HSDLA_DIGIT_PITCH_PAD", 128);
+        if (x < 0 || x > 4096) x = 128;
+        return (x + 15) / 16 * 16;
+    }();
+    return p;
+}
 
 int make_map(DigitOperand &d, int s) {
     PFN_encodeTiled enc = get_encode();
     if (!enc) { g_oz_err = "cuTensorMapEncodeTiled unavailable"; return HSDLA_ERR_CUDA; }
-    if (d.Kpad % 128 != 0 || (reinterpret_cast<uintptr_t>(d.digits) & 255) != 0) {
+    if (d.Kpad % 128 != 0 || d.pitch % 16 != 0 || d.pitch < d.Kpad ||
+        (reinterpret_cast<uintptr_t>(d.digits) & 255) != 0) {
         g_oz_err = "digit operand misaligned";
         return HSDLA_ERR_ARG;
     }
     const int64_t rows = d.plane_rows * 2 * s;
     if (rows > INT32_MAX || d.Kpad > INT32_MAX) { g_oz_err = "digit operand too large for TMA"; return HSDLA_ERR_UNSUPPORTED; }
     cuuint64_t dims[2] = {(cuuint64_t)d.Kpad, (cuuint64_t)rows};
-    cuuint64_t strides[1] = {(cuuint64_t)d.Kpad};
+    cuuint64_t strides[1] = {(cuuint64_t)d.pitch};
     cuuint32_t box[2] = {(cuuint32_t)kKBlock, (cuuint32_t)kTileM};
     cuuint32_t es[2] = {1, 1};
     CUresult r = enc(&d.map, CU_TENSOR_MAP_DATA_TYPE_UINT8, 2, d.digits, dims, strides, box, es,
@@ -592,20 +614,21 @@ struct Arena {
 
 int64_t operand_bytes(int s, int64_t rows, int64_t Kpad) {
     const int64_t pr = round_up(rows, kTileM) + kTileM;
-    return round_up(2 * s * pr * Kpad, 1024) + round_up(4 * pr, 1024);
+    return round_up(2 * s * pr * (Kpad + pitch_pad()), 1024) + round_up(4 * pr, 1024);
 }
 
 void carve_operand(Arena &a, DigitOperand &d, int s, int64_t rows, int64_t Kpad) {
     d.plane_rows = round_up(rows, kTileM) + kTileM;
     d.Kpad = Kpad;
-    d.digits = a.take<uint8_t>(2 * s * d.plane_rows * Kpad);
+    d.pitch = Kpad + pitch_pad();
+    d.digits = a.take<uint8_t>(2 * s * d.plane_rows * d.pitch);
     d.expo = a.take<int32_t>(d.plane_rows);
 }
 
 cudaError_t slice(const double2 *Z, int64_t ldz, const double *v, int64_t Kin, int64_t ncols, int64_t rpb,
                   int64_t bpad, int s, DigitOperand &d, cudaStream_t st) {
     oz_slice_kernel<<<(unsigned)d.plane_rows, kSliceThreads, 0, st>>>(Z, ldz, v, Kin, ncols, rpb, bpad, s, d.digits,
-                                                                       d.Kpad, d.plane_rows, d.expo);
+                                                                       d.Kpad, d.plane_rows, d.expo, d.pitch);
     return cudaGetLastError();
 }
 
@@ -617,11 +640,22 @@ int64_t job_tiles(const OzJob &j) {
 // Host-built tile schedule.  Persistent CTAs take tiles g, g + grid, ... so tiles that are
 // close in the list run at the same time and share their operand panels in L2.  Lower-
 // triangle jobs of equal size (S and H of one k-point) are walked together in square super-
-// blocks of kSuperBlock x kSuperBlock tiles, the jobs' tiles of one (tm, tn) adjacent (they
-// share the left operand); full jobs (T application) go job by job, tile columns outermost.
-constexpr int kSuperBlock = 8;
+// blocks of super_block() tiles, the jobs' tiles of one (tm, tn) adjacent (they share the
+// left operand); full jobs (T application) go job by job, tile columns outermost.
+// Super-block edge in tiles; HSDLA_SCHED_SUPERBLOCK overrides.  The default 0 means one block
+// spanning the whole triangle, i.e. row-major order with the jobs' tiles of one (tm, tn)
+// adjacent: on the 8000-column FLAPW workload it beat 4-, 8- and 16-tile super-blocks by
+// 7-10% (a row of tiles then shares one left panel across ~60 concurrent CTAs).
+int64_t super_block() {
+    static const int64_t b = [] {
+        const int64_t x = env_int("HSDLA_SCHED_SUPERBLOCK", 0);
+        return x <= 0 ? (int64_t)1 << 30 : x;
+    }();
+    return b;
+}
 
 void build_schedule(const std::vector<OzJob> &jobs, std::vector<int4> &list) {
+    const int64_t kSuperBlock = super_block();
     list.clear();
     std::vector<char> done(jobs.size(), 0);
     for (size_t a = 0; a < jobs.size(); ++a) {
@@ -802,6 +836,7 @@ int ozaki_pipeline(OzakiPlan &oz, const OzakiInputs &in, double2 *S, double2 *H,
         DigitOperand dM;
         dM.plane_rows = dX.plane_rows;
         dM.Kpad = bpad * nt;
+        dM.pitch = dM.Kpad + pitch_pad();
         dM.digits = dX.digits;
         dM.expo = dX.expo;
         e = slice(in.M, twoL * nt, nullptr, twoL * nt, G, twoL, bpad, s, dM, st);

@@ -177,8 +177,8 @@ int hsdla_zherkx_lower(hsdla_context *ctx, int32_t precision, int32_t num_slices
  * All scratch (digit planes, exponents, job table, error word) lives in one static device
  * array of 128 MiB that every GPU loading this library holds until the process exits; the
  * call makes no cudaMalloc/cudaFree and no allocating library call.  Problems that need more
- * scratch than that, 2 * (2 s (roundup(n,128) + 128) roundup(k,128) + 4 (roundup(n,128) + 128))
- * bytes plus 2 KiB (about n = 1000, k = 2560 at s = 11), are rejected with
+ * scratch than that, 2 * (2 s (roundup(n,128) + 128) (roundup(k,128) + 128) + 4 (roundup(n,128) + 128))
+ * bytes plus 2 KiB (about n = 1000, k = 2432 at s = 11), are rejected with
  * HSDLA_ERR_UNSUPPORTED.  num_slices = 0 means 11.  The first call on a device looks up the
  * array's device address (cudaGetSymbolAddress) with that device current; make that first
  * call before any stream capture.  Every call shares the one array, so calls that overlap on
