@@ -57,6 +57,8 @@ constexpr int kStageBytes = 4 * kTileM * kKBlock;   // Ar, Ai, Br, Bi boxes
 constexpr int kThreads = 192;        // warp 0 TMA, warp 1 MMA, warps 2..5 epilogue
 constexpr long long kWaitCycles = 2000000000LL;    // ~1 s at 2 GHz
 constexpr int kExactTerms = 1 << 24;                // FP32 exact-integer bound
+constexpr int kSyncEvery = 64;                      // stages per lockstep epoch (cooperative launches)
+constexpr int kRetired = 0x7F7F7F7F;                // progress value of a CTA that has no work left
 
 struct OzJob {
     int32_t lmap, rmap;        // tensor-map index (0..3) of the left / right digit operand
@@ -213,6 +215,30 @@ __host__ __device__ __forceinline__ int64_t chunk_kblocks(int pairs) {
     return c < 1 ? 1 : c;
 }
 
+// Loose grid-wide lockstep for cooperative launches: every CTA publishes its stage epoch, and a
+// producer may run at most one epoch ahead of the slowest CTA.  All persistent CTAs walk
+// identical stage sequences, so staying within an epoch keeps the operand panels they share
+// resident in L2 (left to themselves, CTAs drift apart by far more than L2 can hold).
+// Bounded: on expiry the CTA raises the abort flag and records the error word.
+__device__ bool grid_lockstep(int *progress, int n, int epoch, volatile int *abort_flag, int *err) {
+    atomicExch(progress + blockIdx.x, epoch);
+    const long long t0 = clock64();
+    while (true) {
+        int mn = kRetired;
+        for (int i = 0; i < n; i += 4) {
+            const int4 v = __ldcg(reinterpret_cast<const int4 *>(progress + i));
+            mn = min(mn, min(min(v.x, v.y), min(v.z, v.w)));
+        }
+        if (mn >= epoch - 1) return true;
+        if (*abort_flag) return false;
+        if (clock64() - t0 > kWaitCycles) {
+            *abort_flag = 1;
+            atomicCAS(err, 0, kDevTimeout * 16 + 5);
+            return false;
+        }
+    }
+}
+
 struct __align__(8) Barriers {
     uint64_t full[kStages];
     uint64_t empty[kStages];
@@ -224,7 +250,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     oz_gemm_kernel(const __grid_constant__ CUtensorMap map0, const __grid_constant__ CUtensorMap map1,
                    const __grid_constant__ CUtensorMap map2, const __grid_constant__ CUtensorMap map3,
                    const OzJob *__restrict__ jobs, int num_jobs, int64_t total_tiles, int s, int *err,
-                   const int4 *__restrict__ tile_list) {
+                   const int4 *__restrict__ tile_list, int *progress) {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     // 1024-byte alignment of the stage buffers (SW128 atoms)
     unsigned char *smem = reinterpret_cast<unsigned char *>(
@@ -274,6 +300,9 @@ __global__ void __launch_bounds__(kThreads, 1)
                         for (int64_t kb = cb; ok && kb < ce; ++kb) {
                             for (int i = ilo; i <= ihi; ++i) {
                                 const int jj = t - i;
+                                if (progress && issued > 0 && issued % kSyncEvery == 0 &&
+                                    !grid_lockstep(progress, (int)gridDim.x, (int)(issued / kSyncEvery), &abort_flag,
+                                                   err)) { ok = false; break; }
                                 if (!mbar_wait(&bars.empty[stage], phase ^ 1, &abort_flag, err, 1)) { ok = false; break; }
                                 unsigned char *st = smem + stage * kStageBytes;
                                 mbar_expect_tx(&bars.full[stage], kStageBytes);
@@ -290,6 +319,7 @@ __global__ void __launch_bounds__(kThreads, 1)
                     }
                 }
             }
+            if (progress) atomicExch(progress + blockIdx.x, kRetired);
             // drain: every issued stage must have landed before the CTA may exit
             if (!ok) {
                 for (int q = 0; q < kStages; ++q) {
@@ -680,8 +710,11 @@ void build_schedule(const std::vector<OzJob> &jobs, std::vector<int4> &list) {
     }
 }
 
+constexpr int kProgressCap = 1024;   // progress slots (>= SM count, multiple of 4)
+
 int launch_gemm(std::vector<OzJob> &jobs, const CUtensorMap *maps, int s, int *d_err, OzJob *d_jobs,
-                cudaStream_t st, cudaEvent_t ev0 = nullptr, cudaEvent_t ev1 = nullptr, int4 *d_list = nullptr) {
+                cudaStream_t st, cudaEvent_t ev0 = nullptr, cudaEvent_t ev1 = nullptr, int4 *d_list = nullptr,
+                int *d_progress = nullptr) {
     int64_t total = 0;
     for (auto &j : jobs) {
         j.tiles_n = (j.n + kTileN - 1) / kTileN;
@@ -705,10 +738,31 @@ int launch_gemm(std::vector<OzJob> &jobs, const CUtensorMap *maps, int s, int *d
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
     const int64_t grid = std::min<int64_t>(total, nsm);
+    // lockstep needs every CTA resident at once: cooperative launch, one CTA per SM
+    const bool lockstep = d_progress != nullptr && grid > 1 && grid <= kProgressCap && env_int("HSDLA_LOCKSTEP", 1) != 0;
+    if (lockstep) {
+        const int64_t g4 = (grid + 3) / 4 * 4;
+        e = cudaMemsetAsync(d_progress, 0, sizeof(int) * grid, st);
+        if (e == cudaSuccess && g4 > grid) e = cudaMemsetAsync(d_progress + grid, 0x7F, sizeof(int) * (g4 - grid), st);
+        if (e != cudaSuccess) { g_oz_err = cudaGetErrorString(e); return HSDLA_ERR_CUDA; }
+    }
     if (ev0) cudaEventRecord(ev0, st);
-    oz_gemm_kernel<<<(unsigned)grid, kThreads, smem, st>>>(maps[0], maps[1], maps[2], maps[3], d_jobs,
-                                                            (int)jobs.size(), total, s, d_err, d_list);
-    e = cudaGetLastError();
+    if (lockstep) {
+        CUtensorMap m0 = maps[0], m1 = maps[1], m2 = maps[2], m3 = maps[3];
+        const OzJob *pj = d_jobs;
+        int nj = (int)jobs.size();
+        int64_t tt = total;
+        int ss = s;
+        int *perr = d_err;
+        const int4 *pl = d_list;
+        int *pp = d_progress;
+        void *args[] = {&m0, &m1, &m2, &m3, &pj, &nj, &tt, &ss, &perr, &pl, &pp};
+        e = cudaLaunchCooperativeKernel((const void *)oz_gemm_kernel, dim3((unsigned)grid), dim3(kThreads), args, smem, st);
+    } else {
+        oz_gemm_kernel<<<(unsigned)grid, kThreads, smem, st>>>(maps[0], maps[1], maps[2], maps[3], d_jobs,
+                                                                (int)jobs.size(), total, s, d_err, d_list, nullptr);
+        e = cudaGetLastError();
+    }
     if (ev1) cudaEventRecord(ev1, st);
     if (e != cudaSuccess) { g_oz_err = cudaGetErrorString(e); return HSDLA_ERR_CUDA; }
     // the job table is read by the kernel: keep the host copy alive until it is consumed
@@ -798,7 +852,8 @@ int64_t ozaki_pipeline_workspace(int s, int64_t twoL, int64_t na, int64_t nt, in
     const int64_t tiles_t = na * ((twoL + kTileM - 1) / kTileM) * ((G + kTileN - 1) / kTileN);
     const int64_t cap = std::max(tiles_t, schedule_capacity_lower(G));
     return 3 * operand_bytes(s, G, Kpad) + operand_bytes(s, nt * twoL, bpad) +
-           round_up(sizeof(OzJob) * (na + 4), 1024) + 4096 + round_up(sizeof(int4) * cap, 1024);
+           round_up(sizeof(OzJob) * (na + 4), 1024) + 4096 + round_up(sizeof(int4) * cap, 1024) +
+           round_up(sizeof(int) * kProgressCap, 1024);
 }
 
 int ozaki_pipeline(OzakiPlan &oz, const OzakiInputs &in, double2 *S, double2 *H, int64_t ldo, void *ws,
@@ -817,6 +872,7 @@ int ozaki_pipeline(OzakiPlan &oz, const OzakiInputs &in, double2 *S, double2 *H,
     OzJob *d_jobs = ar.take<OzJob>(na + 4);
     const int64_t tiles_t = na * ((twoL + kTileM - 1) / kTileM) * ((G + kTileN - 1) / kTileN);
     int4 *d_list = ar.take<int4>(std::max(tiles_t, schedule_capacity_lower(G)));
+    int *d_progress = ar.take<int>(kProgressCap);
     int nl = 0;
     cudaError_t e = slice(in.C, K, nullptr, K, G, twoL, bpad, s, dC, st);
     if (e == cudaSuccess) e = slice(in.C, K, in.w, K, G, twoL, bpad, s, dW, st);
@@ -899,7 +955,7 @@ int ozaki_pipeline(OzakiPlan &oz, const OzakiInputs &in, double2 *S, double2 *H,
         j.el = dC.expo; j.er = which == 0 ? dW.expo : dX.expo;
         jobs.push_back(j);
     }
-    rc = launch_gemm(jobs, maps, s, oz.d_error, d_jobs, st, in.ev_dom0, in.ev_dom1, d_list);
+    rc = launch_gemm(jobs, maps, s, oz.d_error, d_jobs, st, in.ev_dom0, in.ev_dom1, d_list, d_progress);
     nl += 1;
     if (launches) *launches = nl;
     return rc;
@@ -1013,7 +1069,7 @@ extern "C" int hsdla_zherkx_lower_noalloc(int32_t num_slices, int64_t n, int64_t
     if (e != cudaSuccess) { g_oz_err = cudaGetErrorString(e); return HSDLA_ERR_CUDA; }
     const int64_t grid = std::min<int64_t>(tiles, nsm);
     oz_gemm_kernel<<<(unsigned)grid, kThreads, smem, st>>>(dp.map, dq.map, dp.map, dp.map, d_job, 1, tiles, s, d_err,
-                                                            nullptr);
+                                                            nullptr, nullptr);
     e = cudaGetLastError();
     int herr = 0;
     if (e == cudaSuccess) e = cudaMemcpyAsync(&herr, d_err, sizeof(int), cudaMemcpyDeviceToHost, st);
