@@ -672,13 +672,13 @@ int64_t job_tiles(const OzJob &j) {
 // triangle jobs of equal size (S and H of one k-point) are walked together in square super-
 // blocks of super_block() tiles, the jobs' tiles of one (tm, tn) adjacent (they share the
 // left operand); full jobs (T application) go job by job, tile columns outermost.
-// Super-block edge in tiles; HSDLA_SCHED_SUPERBLOCK overrides.  The default 0 means one block
-// spanning the whole triangle, i.e. row-major order with the jobs' tiles of one (tm, tn)
-// adjacent: on the 8000-column FLAPW workload it beat 4-, 8- and 16-tile super-blocks by
-// 7-10% (a row of tiles then shares one left panel across ~60 concurrent CTAs).
+// Super-block edge in tiles; HSDLA_SCHED_SUPERBLOCK overrides (0 = row-major over the whole
+// triangle).  With the CTAs in lockstep, 8 x 8 super-blocks cut the S/H launch of the
+// 8000-column FLAPW workload from 378 ms (row-major) to 355 ms: a wave then reads ~16 left and
+// ~16 right panels instead of ~2 left and ~120 right ones.
 int64_t super_block() {
     static const int64_t b = [] {
-        const int64_t x = env_int("HSDLA_SCHED_SUPERBLOCK", 0);
+        const int64_t x = env_int("HSDLA_SCHED_SUPERBLOCK", 8);
         return x <= 0 ? (int64_t)1 << 30 : x;
     }();
     return b;
