@@ -17,8 +17,10 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <map>
 #include <set>
 #include <string>
+#include <tuple>
 #include <vector>
 
 #include "common.cuh"
@@ -38,6 +40,8 @@ struct hsdla_context {
     int64_t ws_bytes = 0;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr, evs[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
     std::set<hsdla_plan *> plans;   // live plans, destroyed with the context
+    // slice autotuner results: (L, atoms, types, n_G bucket, target) -> (slices, predicted error)
+    std::map<std::tuple<int, int, int, int64_t, double>, std::pair<int, double>> tune_cache;
 };
 
 struct PlanKpoint {
@@ -298,6 +302,15 @@ int autotune_slices(hsdla_plan *pl, double2 *C, cudaStream_t st) {
         if (pl->kps[i].n_g > pl->kps[ik].n_g) ik = i;
     const int64_t G = pl->kps[ik].n_g;
     if (G == 0) { pl->autotune = false; return HSDLA_OK; }
+    // systems of one shape share a dynamic range closely enough to share the choice
+    const auto key = std::make_tuple(pl->L, pl->na, pl->nt, (G + 511) / 512, pl->opts.target_rel_err);
+    const auto hit = ctx->tune_cache.find(key);
+    if (hit != ctx->tune_cache.end()) {
+        pl->oz.num_slices = hit->second.first;
+        pl->est_err = hit->second.second;
+        pl->autotune = false;
+        return HSDLA_OK;
+    }
     const int64_t ns = std::min<int64_t>(G, 384), step = G / ns;
     const int64_t K = pl->twoLa, twoL = 2 * (int64_t)pl->L;
     OzakiPlan probe{};
@@ -374,6 +387,7 @@ int autotune_slices(hsdla_plan *pl, double2 *C, cudaStream_t st) {
     pl->oz.num_slices = s;
     pl->est_err = pred;
     pl->autotune = false;
+    ctx->tune_cache[key] = std::make_pair(s, pred);
     ctx_free(ctx, buf, bytes_sample + bytes_oz);
     ozaki_plan_release(probe);
     return HSDLA_OK;
