@@ -272,8 +272,9 @@ class Context:
                                             ctypes.byref(o), ctypes.byref(rep)))
         return list(out), rep.as_dict()
 
-    def plan(self, sys_, kpoints=None, precision="fp64", num_slices=0, tmats=None, target=0.0):
-        return Plan(self, sys_, sys_.kpoints if kpoints is None else kpoints, precision, num_slices, tmats, target)
+    def plan(self, sys_, kpoints=None, precision="fp64", num_slices=0, tmats=None, target=0.0, use_graph=False):
+        return Plan(self, sys_, sys_.kpoints if kpoints is None else kpoints, precision, num_slices, tmats, target,
+                    use_graph)
 
     def zherkx_lower(self, P, Q=None, w=None, precision="fp64", num_slices=0, out=None, stream=None):
         """Lower triangle of P^H diag(w) Q for device (torch) complex128 K x n matrices
@@ -317,13 +318,13 @@ class Plan:
     """Device-resident plan (``hsdla_plan_create``): inputs uploaded once; ``execute``
     writes H/S into device buffers."""
 
-    def __init__(self, ctx: Context, sys_, kpoints, precision, num_slices, tmats, target=0.0):
+    def __init__(self, ctx: Context, sys_, kpoints, precision, num_slices, tmats, target=0.0, use_graph=False):
         self.ctx = ctx
         self.sys = sys_
         self.kpoints = list(kpoints)
         self._sh = _SysHolder(sys_, tmats)
         self._kh = _KptHolder(self.kpoints)
-        o = _opts(precision, num_slices, target)
+        o = _opts(precision, num_slices, target, int(bool(use_graph)))
         h = ctypes.c_void_p()
         ctx.check(ctx.lib.hsdla_plan_create(ctx.h, ctypes.byref(self._sh.struct), self._kh.arr, len(self.kpoints),
                                             ctypes.byref(o), ctypes.byref(h)))

@@ -133,9 +133,14 @@ __device__ __forceinline__ double2 cmul(double2 a, double2 b) {
     return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
 }
 
+__device__ __forceinline__ int entry_of(const KTable &tab, int64_t gc) {
+    int k = 0;
+    while (k + 1 < tab.nk && tab.e[k + 1].col_begin <= gc) ++k;
+    return k;
+}
+
 template <bool kRot>
-__global__ void __launch_bounds__(kThreads) construct_ab_kernel(DevSystem sys, DevKpoint kp, double2 *C,
-                                                                int64_t ldc, double2 *M, int64_t ldm) {
+__global__ void __launch_bounds__(kThreads) construct_ab_kernel(DevSystem sys, const __grid_constant__ KTable tab) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int L = sys.L, nl = sys.max_lmax + 1, na = sys.num_atoms, nt = sys.num_types;
     const int twoL = 2 * L;
@@ -153,7 +158,13 @@ __global__ void __launch_bounds__(kThreads) construct_ab_kernel(DevSystem sys, D
         while ((l + 1) * (l + 1) <= lm) ++l;
         l_of[lm] = (unsigned char)l;
     }
-    for (int64_t gi = blockIdx.x; gi < kp.n_g; gi += gridDim.x) {
+    const int64_t ldc = tab.ldc, ldm = tab.ldm;
+    for (int64_t gc = blockIdx.x; gc < tab.total_cols; gc += gridDim.x) {
+        const KEntry &ent = tab.e[entry_of(tab, gc)];
+        const DevKpoint &kp = ent.kp;
+        const int64_t gi = gc - ent.col_begin;
+        double2 *C = ent.C;
+        double2 *M = ent.M;
         __syncthreads();
         if (threadIdx.x == 0) {
             const int32_t *gv = kp.g + 3 * gi;
@@ -287,12 +298,17 @@ __global__ void __launch_bounds__(kThreads) construct_ab_kernel(DevSystem sys, D
 
 // X[2L a + r, g] = e^{i 2pi (k+g).tau_a} Z[2L t(a) + r, g]: the per-atom T application rebuilt
 // from the per-type product Z_t = T_t M_t.
-__global__ void __launch_bounds__(kThreads) apply_phase_kernel(DevSystem sys, DevKpoint kp, const double2 *Z,
-                                                               int64_t ldz, double2 *X, int64_t ldx) {
+__global__ void __launch_bounds__(kThreads) apply_phase_kernel(DevSystem sys, const __grid_constant__ KTable tab) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     double2 *ph = reinterpret_cast<double2 *>(smem_raw);       // [na]
     const int twoL = 2 * sys.L, na = sys.num_atoms;
-    for (int64_t gi = blockIdx.x; gi < kp.n_g; gi += gridDim.x) {
+    const int64_t ldz = tab.ldm, ldx = tab.ldc;
+    for (int64_t gc = blockIdx.x; gc < tab.total_cols; gc += gridDim.x) {
+        const KEntry &ent = tab.e[entry_of(tab, gc)];
+        const DevKpoint &kp = ent.kp;
+        const int64_t gi = gc - ent.col_begin;
+        const double2 *Z = ent.Z;
+        double2 *X = ent.X;
         __syncthreads();
         const int32_t *gv = kp.g + 3 * gi;
         const double K0 = kp.k[0] + gv[0], K1 = kp.k[1] + gv[1], K2 = kp.k[2] + gv[2];
@@ -314,35 +330,54 @@ __global__ void __launch_bounds__(kThreads) apply_phase_kernel(DevSystem sys, De
     }
 }
 
-cudaError_t launch_apply_phase(const DevSystem &sys, const DevKpoint &kp, const double2 *Z, int64_t ldz,
-                               double2 *X, int64_t ldx, cudaStream_t st) {
+int sm_count() {
     int dev = 0, nsm = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-    const int64_t grid = std::min<int64_t>(kp.n_g, (int64_t)nsm * 8);
+    return nsm;
+}
+
+cudaError_t launch_apply_phase_multi(const DevSystem &sys, const KTable &tab, cudaStream_t st) {
+    if (tab.total_cols <= 0) return cudaSuccess;
+    const int64_t grid = std::min<int64_t>(tab.total_cols, (int64_t)sm_count() * 8);
     const size_t smem = sizeof(double2) * sys.num_atoms;
-    apply_phase_kernel<<<(unsigned)grid, kThreads, smem, st>>>(sys, kp, Z, ldz, X, ldx);
+    apply_phase_kernel<<<(unsigned)grid, kThreads, smem, st>>>(sys, tab);
     return cudaGetLastError();
+}
+
+cudaError_t launch_apply_phase(const DevSystem &sys, const DevKpoint &kp, const double2 *Z, int64_t ldz,
+                               double2 *X, int64_t ldx, cudaStream_t st) {
+    KTable tab;
+    tab.nk = 1; tab.ldc = ldx; tab.ldm = ldz; tab.total_cols = kp.n_g;
+    tab.e[0] = KEntry{kp, nullptr, nullptr, Z, X, 0};
+    return launch_apply_phase_multi(sys, tab, st);
 }
 
 cudaError_t launch_construct_ab(const DevSystem &sys, const DevKpoint &kp, double2 *C, int64_t ldc,
                                 cudaStream_t st, double2 *M, int64_t ldm) {
+    KTable tab;
+    tab.nk = 1; tab.ldc = ldc; tab.ldm = ldm; tab.total_cols = kp.n_g;
+    tab.e[0] = KEntry{kp, C, M, nullptr, nullptr, 0};
+    return launch_construct_ab_multi(sys, tab, st);
+}
+
+cudaError_t launch_construct_ab_multi(const DevSystem &sys, const KTable &tab, cudaStream_t st) {
+    if (tab.total_cols <= 0) return cudaSuccess;
+    bool anyM = false;
+    for (int k = 0; k < tab.nk; ++k) anyM = anyM || tab.e[k].M;
     const bool rot = sys.atom_rotmat != nullptr;
     const int nl = sys.max_lmax + 1;
     size_t smem = sizeof(double) * 2 * sys.num_types * nl + sizeof(double2) * sys.num_atoms +
                   sizeof(double2) * (rot ? kRotChunk : 1) * sys.L + sys.L + 16;
     smem = (smem + 15) & ~size_t(15);
-    int dev = 0, nsm = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-    const int64_t grid = std::min<int64_t>(kp.n_g, (int64_t)nsm * 8);
+    const int64_t grid = std::min<int64_t>(tab.total_cols, (int64_t)sm_count() * 8);
     if (rot) {
+        if (anyM) return cudaErrorInvalidValue;  // per-type rows exist only when atoms share the rotation
         cudaFuncSetAttribute(construct_ab_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (M) return cudaErrorInvalidValue;     // per-type rows exist only when atoms share the rotation
-        construct_ab_kernel<true><<<(unsigned)grid, kThreads, smem, st>>>(sys, kp, C, ldc, nullptr, 0);
+        construct_ab_kernel<true><<<(unsigned)grid, kThreads, smem, st>>>(sys, tab);
     } else {
         cudaFuncSetAttribute(construct_ab_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        construct_ab_kernel<false><<<(unsigned)grid, kThreads, smem, st>>>(sys, kp, C, ldc, M, ldm);
+        construct_ab_kernel<false><<<(unsigned)grid, kThreads, smem, st>>>(sys, tab);
     }
     return cudaGetLastError();
 }

@@ -43,7 +43,28 @@ struct DevKpoint {
     const int32_t *g;           // [n_g][3]
 };
 
+// A group of k-points handled by one launch per stage (passed by value as a kernel parameter).
+constexpr int kMaxGroup = 64;
+struct KEntry {
+    DevKpoint kp;
+    double2 *C;                 // (2 L a) x n_g, ld KTable::ldc
+    double2 *M;                 // (2 L nt) x n_g, ld KTable::ldm, or nullptr
+    const double2 *Z;           // per-type product, ld KTable::ldm (phase expansion input)
+    double2 *X;                 // per-atom output, ld KTable::ldc (phase expansion output)
+    int64_t col_begin;          // first global column of this k-point
+};
+struct KTable {
+    int nk = 0;
+    int64_t ldc = 0, ldm = 0;
+    int64_t total_cols = 0;
+    KEntry e[kMaxGroup];
+};
+
 // ----------------------------------------------------------- kernels (host)
+// (a) for every k-point of a table in one launch (C always; M when the entries give it)
+cudaError_t launch_construct_ab_multi(const DevSystem &sys, const KTable &tab, cudaStream_t st);
+// X = phase Z for every k-point of a table in one launch
+cudaError_t launch_apply_phase_multi(const DevSystem &sys, const KTable &tab, cudaStream_t st);
 // (a) matching tensors of one k-point into C: (2 L a) x n_g column-major, per-atom [A_a; B_a]
 // Optionally also the phase-free per-type rows M ((2 L nt) x n_g, ld ldm) when no atom carries
 // its own rotation (M_t = C_a e^{-i 2pi K.tau_a} for every atom a of type t).

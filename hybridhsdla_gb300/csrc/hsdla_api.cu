@@ -68,6 +68,27 @@ struct hsdla_plan {
     int64_t jobs_cap = 0;
     std::vector<Fp64Job> h_jobs;
     OzakiPlan oz{};
+    // k-point groups, prepared against the context workspace (re-prepared when it moves)
+    struct Group {
+        std::vector<int> kidx;           // plan k-point indices
+        KTable ktab;                     // construct / phase tables (C, M, Z, X per k-point)
+        OzGroup *oz = nullptr;           // Ozaki engine state
+        Fp64Job *d_jobs_t = nullptr;     // FP64: T application jobs (device, in the workspace)
+        int n_jobs_t = 0;
+        int64_t tiles_t = 0;
+        Fp64Job *d_jobs_sh = nullptr;    // FP64: S/H jobs (device) and their pinned host copy
+        Fp64Job *h_jobs_sh = nullptr;
+        int64_t tiles_sh = 0;
+        void *persist = nullptr;         // prepared tables (not shared with other groups)
+        int64_t persist_bytes = 0;
+    };
+    std::vector<Group> groups;
+    void *prepared_ws = nullptr;
+    int64_t group_ws_bytes = 0;          // workspace of the largest group
+    cudaGraphExec_t graph = nullptr;     // captured execution
+    std::vector<void *> graph_outputs;   // output pointers the graph was captured with
+    cudaStream_t graph_stream = nullptr;
+    bool graph_failed = false;
     bool autotune = false;           // Ozaki slice count still to be chosen from the data
     bool hoist = false;              // T application per type (no atom carries its own rotation)
     double est_err = 0.0;            // autotuner's predicted relative error
@@ -596,15 +617,278 @@ int hsdla_plan_create(hsdla_context *ctx, const hsdla_system *s, const hsdla_kpo
     return HSDLA_OK;
 }
 
+}  // extern "C"
+
+namespace {
+
+// FP64 buffers of one k-point inside a group workspace.
+int64_t kpoint_fp64_bytes(const hsdla_plan *pl, int64_t G) {
+    const int64_t K = pl->twoLa, ldm = 2 * (int64_t)pl->L * pl->nt;
+    const int64_t nCX = pl->opts.precision == HSDLA_PREC_FP64 ? 2 : 1;   // FP64 keeps C and X apart
+    auto r = [](int64_t x) { return (x + 1023) / 1024 * 1024; };        // each buffer is 1 KB aligned
+    int64_t b = nCX * r(K * G * (int64_t)sizeof(double2));
+    if (pl->hoist) b += 2 * r(ldm * G * (int64_t)sizeof(double2));
+    return b;
+}
+
+int64_t group_bytes(const hsdla_plan *pl, const std::vector<int> &kidx) {
+    int64_t b = 0;
+    std::vector<int64_t> G;
+    for (int i : kidx) { b += kpoint_fp64_bytes(pl, pl->kps[i].n_g); G.push_back(pl->kps[i].n_g); }
+    if (pl->opts.precision == HSDLA_PREC_OZAKI_FP8)
+        b += 1024 + ozaki_group_bytes(pl->oz.num_slices, 2 * (int64_t)pl->L, pl->na, pl->nt, G);
+    return b;
+}
+
+int64_t group_persist_bytes(const hsdla_plan *pl, const std::vector<int> &kidx) {
+    std::vector<int64_t> G;
+    for (int i : kidx) G.push_back(pl->kps[i].n_g);
+    if (pl->opts.precision == HSDLA_PREC_OZAKI_FP8)
+        return ozaki_group_persist_bytes(pl->oz.num_slices, 2 * (int64_t)pl->L, pl->na, pl->nt, G);
+    return 4096 + (int64_t)sizeof(Fp64Job) * (int64_t)kidx.size() * (std::max(pl->na, pl->nt) + 4);
+}
+
+// Device-memory budget for one group's workspace: HSDLA_WORKSPACE_BUDGET (bytes) or 60% of the
+// device, reduced to fit the context's memory cap.
+int64_t workspace_budget(hsdla_context *ctx) {
+    int64_t budget = 0;
+    if (const char *v = getenv("HSDLA_WORKSPACE_BUDGET")) budget = strtoll(v, nullptr, 10);
+    if (budget <= 0) {
+        size_t fr = 0, tot = 0;
+        cudaMemGetInfo(&fr, &tot);
+        budget = (int64_t)(0.6 * (double)tot);
+    }
+    if (ctx->mem_cap > 0) budget = std::min(budget, ctx->mem_cap - ctx->mem_used + ctx->ws_bytes);
+    return budget;
+}
+
+// Greedy k-point groups whose workspace fits the budget (at least one k-point per group).
+void form_groups(hsdla_plan *pl, int64_t budget) {
+    pl->groups.clear();
+    std::vector<int> cur;
+    for (int i = 0; i < (int)pl->kps.size(); ++i) {
+        if (pl->kps[i].n_g == 0) continue;
+        std::vector<int> trial = cur;
+        trial.push_back(i);
+        if (!cur.empty() && ((int)trial.size() > kMaxGroup || group_bytes(pl, trial) > budget)) {
+            hsdla_plan::Group g;
+            g.kidx = cur;
+            pl->groups.push_back(g);
+            cur.assign(1, i);
+        } else {
+            cur = trial;
+        }
+    }
+    if (!cur.empty()) {
+        hsdla_plan::Group g;
+        g.kidx = cur;
+        pl->groups.push_back(g);
+    }
+    pl->group_ws_bytes = 0;
+    for (auto &g : pl->groups) pl->group_ws_bytes = std::max(pl->group_ws_bytes, group_bytes(pl, g.kidx));
+}
+
+void release_groups(hsdla_plan *pl) {
+    for (auto &g : pl->groups) {
+        if (g.oz) ozaki_group_destroy(g.oz);
+        if (g.h_jobs_sh) cudaFreeHost(g.h_jobs_sh);
+        if (g.persist) ctx_free(pl->ctx, g.persist, g.persist_bytes);
+        g.oz = nullptr;
+        g.h_jobs_sh = nullptr;
+        g.persist = nullptr;
+    }
+    if (pl->graph) cudaGraphExecDestroy(pl->graph);
+    pl->graph = nullptr;
+    pl->graph_outputs.clear();
+    pl->prepared_ws = nullptr;
+}
+
+// Lay out every group in the workspace and build its launch tables.
+int prepare_groups(hsdla_plan *pl, void *ws, cudaStream_t st) {
+    hsdla_context *ctx = pl->ctx;
+    const int64_t K = pl->twoLa, twoL = 2 * (int64_t)pl->L, ldm = twoL * pl->nt;
+    for (auto &g : pl->groups) {
+        char *p = reinterpret_cast<char *>(ws);
+        auto take = [&](int64_t bytes) { char *r = p; p += (bytes + 1023) / 1024 * 1024; return r; };
+        g.persist_bytes = group_persist_bytes(pl, g.kidx);
+        int rcp = ctx_malloc(ctx, &g.persist, g.persist_bytes);
+        if (rcp) return rcp;
+        char *pp = reinterpret_cast<char *>(g.persist);
+        auto keep = [&](int64_t bytes) { char *r = pp; pp += (bytes + 1023) / 1024 * 1024; return r; };
+        KTable &kt = g.ktab;
+        kt = KTable();
+        kt.nk = (int)g.kidx.size(); kt.ldc = K; kt.ldm = ldm;
+        std::vector<OzKBufs> kb;
+        int64_t col = 0;
+        for (int q = 0; q < kt.nk; ++q) {
+            const PlanKpoint &pk = pl->kps[g.kidx[q]];
+            const int64_t G = pk.n_g;
+            KEntry &e = kt.e[q];
+            e.kp = pk.dk;
+            e.col_begin = col;
+            col += G;
+            e.C = reinterpret_cast<double2 *>(take(K * G * (int64_t)sizeof(double2)));
+            e.X = pl->opts.precision == HSDLA_PREC_FP64 ? reinterpret_cast<double2 *>(take(K * G * (int64_t)sizeof(double2)))
+                                                        : e.C;   // Ozaki: X reuses C once C is sliced
+            e.M = pl->hoist ? reinterpret_cast<double2 *>(take(ldm * G * (int64_t)sizeof(double2))) : nullptr;
+            double2 *Z = pl->hoist ? reinterpret_cast<double2 *>(take(ldm * G * (int64_t)sizeof(double2))) : nullptr;
+            e.Z = Z;
+            OzKBufs b;
+            b.CX = e.C; b.M = e.M; b.Z = Z; b.G = G;
+            kb.push_back(b);
+        }
+        kt.total_cols = col;
+        if (pl->opts.precision == HSDLA_PREC_OZAKI_FP8) {
+            OzGroupDesc d;
+            d.twoL = twoL; d.na = pl->na; d.nt = pl->nt; d.hoist = pl->hoist;
+            d.w = pl->w; d.Tfull = pl->Tfull; d.atom_type = pl->atom_type.data();
+            char *oz_ws = reinterpret_cast<char *>((reinterpret_cast<uintptr_t>(p) + 1023) & ~uintptr_t(1023));
+            int rc = ozaki_group_prepare(pl->oz, d, kb, oz_ws, g.persist, st, &g.oz);
+            if (rc) return set_err(ctx, rc, "group set-up failed: %s", ozaki_last_error());
+        } else {
+            std::vector<Fp64Job> jt, jsh;
+            for (int q = 0; q < kt.nk; ++q) {
+                const KEntry &e = kt.e[q];
+                const int64_t G = pl->kps[g.kidx[q]].n_g;
+                if (pl->hoist) {
+                    for (int t = 0; t < pl->nt; ++t) {
+                        Fp64Job jb{};
+                        jb.P = pl->Tfull + (int64_t)t * twoL * twoL; jb.ldp = twoL;
+                        jb.Q = e.M + twoL * t; jb.ldq = ldm;
+                        jb.out = const_cast<double2 *>(e.Z) + twoL * t; jb.ldo = ldm;
+                        jb.m = twoL; jb.n = G; jb.k = twoL;
+                        jt.push_back(jb);
+                    }
+                } else {
+                    for (int j = 0; j < pl->na; ++j) {
+                        Fp64Job jb{};
+                        jb.P = pl->Tfull + (int64_t)pl->atom_type[j] * twoL * twoL; jb.ldp = twoL;
+                        jb.Q = e.C + twoL * j; jb.ldq = K;
+                        jb.out = e.X + twoL * j; jb.ldo = K;
+                        jb.m = twoL; jb.n = G; jb.k = twoL;
+                        jt.push_back(jb);
+                    }
+                }
+                Fp64Job js{};
+                js.P = e.C; js.ldp = K; js.Q = e.C; js.ldq = K; js.w = pl->w;
+                js.m = G; js.n = G; js.k = K; js.lower = 1;
+                Fp64Job jh = js;
+                jh.Q = e.X; jh.w = nullptr;
+                jsh.push_back(js);
+                jsh.push_back(jh);
+            }
+            g.tiles_t = assign_tiles(jt, 0);
+            g.tiles_sh = assign_tiles(jsh, 0);
+            g.n_jobs_t = (int)jt.size();
+            g.d_jobs_t = reinterpret_cast<Fp64Job *>(keep(sizeof(Fp64Job) * jt.size()));
+            g.d_jobs_sh = reinterpret_cast<Fp64Job *>(keep(sizeof(Fp64Job) * jsh.size()));
+            if (cudaHostAlloc((void **)&g.h_jobs_sh, sizeof(Fp64Job) * jsh.size(), cudaHostAllocDefault) != cudaSuccess) {
+                g.h_jobs_sh = nullptr;
+                return set_err(ctx, HSDLA_ERR_NOMEM, "pinned job table allocation failed");
+            }
+            memcpy(g.h_jobs_sh, jsh.data(), sizeof(Fp64Job) * jsh.size());
+            CUDA_TRY(ctx, cudaMemcpy(g.d_jobs_t, jt.data(), sizeof(Fp64Job) * jt.size(), cudaMemcpyHostToDevice));
+        }
+    }
+    pl->prepared_ws = ws;
+    return HSDLA_OK;
+}
+
+// Point the groups' S/H job tables at this call's outputs (host side; copied in stream order).
+void set_outputs(hsdla_plan *pl, hsdla_cx *const *dH, hsdla_cx *const *dS, const int64_t *ld) {
+    for (auto &g : pl->groups) {
+        const int nk = (int)g.kidx.size();
+        std::vector<double2 *> S(nk), H(nk);
+        std::vector<int64_t> l(nk);
+        for (int q = 0; q < nk; ++q) {
+            S[q] = reinterpret_cast<double2 *>(dS[g.kidx[q]]);
+            H[q] = reinterpret_cast<double2 *>(dH[g.kidx[q]]);
+            l[q] = ld[g.kidx[q]];
+        }
+        if (g.oz) {
+            ozaki_group_set_outputs(g.oz, S.data(), H.data(), l.data());
+        } else {
+            for (int q = 0; q < nk; ++q) {
+                g.h_jobs_sh[2 * q].out = S[q];
+                g.h_jobs_sh[2 * q].ldo = l[q];
+                g.h_jobs_sh[2 * q + 1].out = H[q];
+                g.h_jobs_sh[2 * q + 1].ldo = l[q];
+            }
+        }
+    }
+}
+
+// Algorithmic flops of the S/H launches of one execution (FP8 digit products for Ozaki).
+void run_groups_flop(const hsdla_plan *pl, double *dom_flop) {
+    *dom_flop = 0.0;
+    const double sl = pl->oz.num_slices;
+    for (const auto &g : pl->groups)
+        for (int q = 0; q < g.ktab.nk; ++q) {
+            const double G = (double)g.ktab.e[q].kp.n_g;
+            const double lower = 4.0 * G * (G + 1.0) * (double)pl->twoLa;
+            *dom_flop += 2.0 * lower * (g.oz ? sl * (sl + 1) / 2 : 1.0);
+        }
+}
+
+// Enqueue every group's launches (no host synchronisation: capturable in a CUDA graph).
+int run_groups(hsdla_plan *pl, cudaStream_t st, bool timed, float *ms_ab, float *ms_dom, double *dom_flop) {
+    hsdla_context *ctx = pl->ctx;
+    pl->launches = 0;
+    if (dom_flop) *dom_flop = 0.0;
+    for (auto &g : pl->groups) {
+        if (timed) CUDA_TRY(ctx, cudaEventRecord(ctx->evs[0], st));
+        CUDA_TRY(ctx, launch_construct_ab_multi(pl->dsys, g.ktab, st));
+        pl->launches++;
+        if (timed) CUDA_TRY(ctx, cudaEventRecord(ctx->evs[1], st));
+        for (int q = 0; q < g.ktab.nk; ++q) {
+            const double G = (double)g.ktab.e[q].kp.n_g;
+            const double lower = 4.0 * G * (G + 1.0) * (double)pl->twoLa;
+            const double sl = pl->oz.num_slices;
+            if (dom_flop) *dom_flop += 2.0 * lower * (g.oz ? sl * (sl + 1) / 2 : 1.0);
+        }
+        if (g.oz) {
+            int nl = 0;
+            const int rc = ozaki_group_run(g.oz, pl->dsys, g.ktab, st, timed ? ctx->evs[4] : nullptr,
+                                           timed ? ctx->evs[5] : nullptr, &nl);
+            if (rc) return set_err(ctx, rc, "Ozaki group failed: %s", ozaki_last_error());
+            pl->launches += nl;
+        } else {
+            CUDA_TRY(ctx, launch_fp64_jobs(g.d_jobs_t, g.n_jobs_t, g.tiles_t, st));
+            pl->launches++;
+            if (pl->hoist) {
+                CUDA_TRY(ctx, launch_apply_phase_multi(pl->dsys, g.ktab, st));
+                pl->launches++;
+            }
+            CUDA_TRY(ctx, cudaMemcpyAsync(g.d_jobs_sh, g.h_jobs_sh, sizeof(Fp64Job) * 2 * g.ktab.nk,
+                                          cudaMemcpyHostToDevice, st));
+            if (timed) CUDA_TRY(ctx, cudaEventRecord(ctx->evs[4], st));
+            CUDA_TRY(ctx, launch_fp64_jobs(g.d_jobs_sh, 2 * g.ktab.nk, g.tiles_sh, st));
+            if (timed) CUDA_TRY(ctx, cudaEventRecord(ctx->evs[5], st));
+            pl->launches++;
+        }
+        if (timed) {
+            // stage times need the events: wait for this group (un-graphed runs only)
+            CUDA_TRY(ctx, cudaEventSynchronize(ctx->evs[5]));
+            float a = 0, d = 0;
+            cudaEventElapsedTime(&a, ctx->evs[0], ctx->evs[1]);
+            cudaEventElapsedTime(&d, ctx->evs[4], ctx->evs[5]);
+            *ms_ab += a;
+            *ms_dom += d;
+        }
+    }
+    return HSDLA_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
 int64_t hsdla_plan_workspace_bytes(const hsdla_plan *pl) {
     if (!pl) return 0;
     int64_t ngmax = 0;
     for (auto &k : pl->kps) ngmax = std::max(ngmax, k.n_g);
-    int64_t b = 2 * (int64_t)sizeof(double2) * pl->twoLa * ngmax;   // C and X
-    if (pl->hoist) b += 2 * (int64_t)sizeof(double2) * 2 * pl->L * pl->nt * ngmax + 1024;   // M and Z
-    if (pl->opts.precision == HSDLA_PREC_OZAKI_FP8)
-        b += 1024 + ozaki_pipeline_workspace(pl->oz.num_slices, 2 * (int64_t)pl->L, pl->na, pl->nt, ngmax);
-    return b;
+    // the slice autotuner builds the largest k-point's C at the start of the workspace
+    return std::max(pl->group_ws_bytes, 2 * (int64_t)sizeof(double2) * pl->twoLa * ngmax) + 4096;
 }
 
 void hsdla_plan_destroy(hsdla_plan *pl) {
@@ -612,6 +896,7 @@ void hsdla_plan_destroy(hsdla_plan *pl) {
     hsdla_context *ctx = pl->ctx;
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->stream);
+    release_groups(pl);
     if (pl->d_jobs) ctx_free(ctx, pl->d_jobs, pl->jobs_cap * sizeof(Fp64Job));
     if (pl->tables) ctx_free(ctx, pl->tables, pl->tables_bytes);
     ozaki_plan_release(pl->oz);
@@ -642,125 +927,86 @@ int hsdla_plan_execute(hsdla_plan *pl, hsdla_cx *const *dH, hsdla_cx *const *dS,
         if (ld[i] < pl->kps[i].n_g) return set_err(ctx, HSDLA_ERR_ARG, "ld[%d]=%lld < n_g=%lld", i,
                                                    (long long)ld[i], (long long)pl->kps[i].n_g);
     }
-    int64_t ngmax = 0;
-    for (auto &k : pl->kps) ngmax = std::max(ngmax, k.n_g);
+    int rc;
     void *ws = nullptr;
-    int rc = ctx_workspace(ctx, hsdla_plan_workspace_bytes(pl), &ws);
-    if (rc) return rc;
-    double2 *C = reinterpret_cast<double2 *>(ws);
     if (pl->autotune) {
-        rc = autotune_slices(pl, C, st);
+        int64_t ngmax = 0;
+        for (auto &k : pl->kps) ngmax = std::max(ngmax, k.n_g);
+        rc = ctx_workspace(ctx, 2 * (int64_t)sizeof(double2) * pl->twoLa * ngmax + 4096, &ws);
         if (rc) return rc;
-        rc = ctx_workspace(ctx, hsdla_plan_workspace_bytes(pl), &ws);
+        rc = autotune_slices(pl, reinterpret_cast<double2 *>(ws), st);
         if (rc) return rc;
-        C = reinterpret_cast<double2 *>(ws);
+        release_groups(pl);
+        pl->groups.clear();
     }
-    double2 *X = C + pl->twoLa * ngmax;
-    const int64_t ldm = 2 * (int64_t)pl->L * pl->nt;
-    double2 *Mt = pl->hoist ? X + pl->twoLa * ngmax : nullptr;
-    double2 *Zt = pl->hoist ? Mt + ldm * ngmax : nullptr;
-    char *tail = reinterpret_cast<char *>(pl->hoist ? Zt + ldm * ngmax : X + pl->twoLa * ngmax);
-    // the digit workspace needs 1024-byte alignment (TMA boxes, SW128 atoms)
-    char *oz_ws = reinterpret_cast<char *>((reinterpret_cast<uintptr_t>(tail) + 1023) & ~uintptr_t(1023));
-    const int64_t L = pl->L, twoL = 2 * L, twoLa = pl->twoLa;
-    pl->launches = 0;
-    float ms_ab = 0.f, ms_t = 0.f, ms_c = 0.f, ms_dom = 0.f;
+    if (pl->groups.empty()) form_groups(pl, workspace_budget(ctx));
+    rc = ctx_workspace(ctx, hsdla_plan_workspace_bytes(pl), &ws);
+    if (rc) return rc;
+    if (pl->prepared_ws != ws) {
+        CUDA_TRY(ctx, cudaStreamSynchronize(st));
+        release_groups(pl);
+        rc = prepare_groups(pl, ws, st);
+        if (rc) { release_groups(pl); return rc; }
+    }
+    set_outputs(pl, dH, dS, ld);
+    float ms_ab = 0.f, ms_dom = 0.f;
     double dom_flop = 0.0;
-    CUDA_TRY(ctx, cudaEventRecord(ctx->ev0, st));
-    for (int i = 0; i < nk; ++i) {
-        const int64_t G = pl->kps[i].n_g;
-        if (G == 0) continue;
-        CUDA_TRY(ctx, cudaEventRecord(ctx->evs[0], st));
-        CUDA_TRY(ctx, launch_construct_ab(pl->dsys, pl->kps[i].dk, C, twoLa, st, Mt, ldm));
-        pl->launches++;
-        CUDA_TRY(ctx, cudaEventRecord(ctx->evs[1], st));
-        // (b) X_a = T_a C_a: per type (Z_t = T_t M_t, expanded by the phases) or per atom, one launch
-        pl->h_jobs.clear();
-        if (pl->hoist) {
-            for (int t = 0; t < pl->nt; ++t) {
-                Fp64Job jb{};
-                jb.P = pl->Tfull + (int64_t)t * twoL * twoL; jb.ldp = twoL;
-                jb.Q = Mt + twoL * t; jb.ldq = ldm;
-                jb.out = Zt + twoL * t; jb.ldo = ldm;
-                jb.m = twoL; jb.n = G; jb.k = twoL; jb.lower = 0;
-                pl->h_jobs.push_back(jb);
+    const bool want_graph = pl->opts.use_graph != 0 && !pl->graph_failed;
+    cudaStream_t run_st = want_graph && st == nullptr ? ctx->stream : st;   // the legacy stream cannot capture
+    if (run_st != st) {
+        CUDA_TRY(ctx, cudaEventRecord(ctx->ev0, st));
+        CUDA_TRY(ctx, cudaStreamWaitEvent(run_st, ctx->ev0, 0));
+    }
+    CUDA_TRY(ctx, cudaEventRecord(ctx->evs[2], run_st));
+    if (want_graph) {
+        std::vector<void *> outs;
+        for (int i = 0; i < nk; ++i) { outs.push_back(dH[i]); outs.push_back(dS[i]); }
+        if (pl->graph && (outs != pl->graph_outputs || pl->graph_stream != run_st)) {
+            cudaGraphExecDestroy(pl->graph);
+            pl->graph = nullptr;
+        }
+        if (!pl->graph) {
+            // outputs travel through the pinned job tables, so a graph is re-captured only when the
+            // output pointers or the stream change (the tables' copy nodes read them at launch)
+            cudaGraph_t graph = nullptr;
+            cudaError_t e = cudaStreamBeginCapture(run_st, cudaStreamCaptureModeThreadLocal);
+            if (e == cudaSuccess) {
+                rc = run_groups(pl, run_st, false, nullptr, nullptr, &dom_flop);
+                e = cudaStreamEndCapture(run_st, &graph);
+                if (rc == HSDLA_OK && e == cudaSuccess) e = cudaGraphInstantiate(&pl->graph, graph, 0);
+                if (graph) cudaGraphDestroy(graph);
             }
+            if (rc != HSDLA_OK || e != cudaSuccess) {
+                cudaGetLastError();
+                pl->graph = nullptr;
+                pl->graph_failed = true;     // run un-captured from now on
+            } else {
+                pl->graph_outputs = outs;
+                pl->graph_stream = run_st;
+            }
+        }
+        if (pl->graph) {
+            CUDA_TRY(ctx, cudaGraphLaunch(pl->graph, run_st));
+            if (dom_flop == 0.0) run_groups_flop(pl, &dom_flop);
         } else {
-            for (int j = 0; j < pl->na; ++j) {
-                Fp64Job jb{};
-                jb.P = pl->Tfull + (int64_t)pl->atom_type[j] * twoL * twoL; jb.ldp = twoL;
-                jb.Q = C + twoL * j; jb.ldq = twoLa;
-                jb.w = nullptr;
-                jb.out = X + twoL * j; jb.ldo = twoLa;
-                jb.m = twoL; jb.n = G; jb.k = twoL; jb.lower = 0;
-                pl->h_jobs.push_back(jb);
-            }
-        }
-        if (pl->opts.precision != HSDLA_PREC_FP64) pl->h_jobs.clear();   // the Ozaki pipeline emulates (b) too
-        const int64_t nt_b = assign_tiles(pl->h_jobs, 0);
-        const size_t nb = pl->h_jobs.size();
-        // (c) S and H lower triangles
-        if (pl->opts.precision == HSDLA_PREC_FP64) {
-            Fp64Job js{};
-            js.P = C; js.ldp = twoLa; js.Q = C; js.ldq = twoLa; js.w = pl->w;
-            js.out = reinterpret_cast<double2 *>(dS[i]); js.ldo = ld[i];
-            js.m = G; js.n = G; js.k = twoLa; js.lower = 1;
-            Fp64Job jh = js;
-            jh.Q = X; jh.w = nullptr; jh.out = reinterpret_cast<double2 *>(dH[i]);
-            pl->h_jobs.push_back(js);
-            pl->h_jobs.push_back(jh);
-        }
-        const int64_t nt_c = assign_tiles(pl->h_jobs, nb);
-        if (!pl->h_jobs.empty()) {
-            rc = upload_jobs(pl, st);
+            rc = run_groups(pl, run_st, true, &ms_ab, &ms_dom, &dom_flop);
             if (rc) return rc;
         }
-        if (nb > 0) {
-            CUDA_TRY(ctx, launch_fp64_jobs(pl->d_jobs, (int)nb, nt_b, st));
-            pl->launches++;
-            if (pl->hoist) {
-                CUDA_TRY(ctx, launch_apply_phase(pl->dsys, pl->kps[i].dk, Zt, ldm, X, twoLa, st));
-                pl->launches++;
-            }
-        }
-        CUDA_TRY(ctx, cudaEventRecord(ctx->evs[2], st));
-        const double lower_cflop = 4.0 * (double)G * (double)(G + 1) * (double)twoLa;   // one lower triangle
-        if (pl->opts.precision == HSDLA_PREC_FP64) {
-            CUDA_TRY(ctx, cudaEventRecord(ctx->evs[4], st));
-            CUDA_TRY(ctx, launch_fp64_jobs(pl->d_jobs + nb, (int)(pl->h_jobs.size() - nb), nt_c, st));
-            CUDA_TRY(ctx, cudaEventRecord(ctx->evs[5], st));
-            pl->launches++;
-            dom_flop = 2.0 * lower_cflop;
-        } else {
-            const double s_ = pl->oz.num_slices;
-            dom_flop = 2.0 * lower_cflop * s_ * (s_ + 1) / 2;
-            int nl = 0;
-            OzakiInputs in;
-            in.C = C; in.Tfull = pl->Tfull; in.w = pl->w; in.atom_type = pl->atom_type.data(); in.X = X;
-            in.twoL = twoL; in.na = pl->na; in.nt = pl->nt; in.G = G;
-            in.ev_dom0 = ctx->evs[4]; in.ev_dom1 = ctx->evs[5];
-            if (pl->hoist) { in.M = Mt; in.Z = Zt; in.sys = &pl->dsys; in.kp = &pl->kps[i].dk; }
-            rc = ozaki_pipeline(pl->oz, in, reinterpret_cast<double2 *>(dS[i]), reinterpret_cast<double2 *>(dH[i]),
-                                ld[i], oz_ws, st, &nl);
-            if (rc) return set_err(ctx, rc, "Ozaki contraction failed: %s", ozaki_last_error());
-            pl->launches += nl;
-        }
-        CUDA_TRY(ctx, cudaEventRecord(ctx->evs[3], st));
-        CUDA_TRY(ctx, cudaEventSynchronize(ctx->evs[3]));
-        float a = 0, b = 0, c = 0, d = 0;
-        cudaEventElapsedTime(&a, ctx->evs[0], ctx->evs[1]);
-        cudaEventElapsedTime(&b, ctx->evs[1], ctx->evs[2]);
-        cudaEventElapsedTime(&c, ctx->evs[2], ctx->evs[3]);
-        cudaEventElapsedTime(&d, ctx->evs[4], ctx->evs[5]);
-        ms_ab += a; ms_t += b; ms_c += c; ms_dom = d;
+    } else {
+        rc = run_groups(pl, run_st, true, &ms_ab, &ms_dom, &dom_flop);
+        if (rc) return rc;
     }
-    CUDA_TRY(ctx, cudaEventRecord(ctx->ev1, st));
-    CUDA_TRY(ctx, cudaEventSynchronize(ctx->ev1));
+    CUDA_TRY(ctx, cudaEventRecord(ctx->evs[3], run_st));
+    if (run_st != st) {
+        CUDA_TRY(ctx, cudaEventRecord(ctx->ev1, run_st));
+        CUDA_TRY(ctx, cudaStreamWaitEvent(st, ctx->ev1, 0));
+    }
+    CUDA_TRY(ctx, cudaEventSynchronize(ctx->evs[3]));
     rc = ozaki_check_device_error(pl->oz);
     if (rc) return set_err(ctx, rc, "device-side error: %s", ozaki_last_error());
     if (rep) {
         float ms = 0.f;
-        cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+        cudaEventElapsedTime(&ms, ctx->evs[2], ctx->evs[3]);
         memset(rep, 0, sizeof(*rep));
         rep->ms_total = ms;
         rep->num_kpoints = nk;
@@ -768,8 +1014,7 @@ int hsdla_plan_execute(hsdla_plan *pl, hsdla_cx *const *dH, hsdla_cx *const *dS,
         rep->flop = pl->flop;
         rep->eff_tflops = ms > 0 ? pl->flop / (ms * 1e-3) / 1e12 : 0.0;
         rep->ms_construct_ab = ms_ab;
-        rep->ms_tapply = ms_t;
-        rep->ms_contract = ms_c;
+        rep->ms_contract = ms - ms_ab;
         rep->ms_dominant = ms_dom;
         rep->dominant_flop = dom_flop;
         rep->num_slices = pl->opts.precision == HSDLA_PREC_OZAKI_FP8 ? pl->oz.num_slices : 0;

@@ -474,24 +474,44 @@ __device__ __forceinline__ uint32_t e4m3_of_digit(int d) {
     return sgn | ((e + 7u) << 3) | man;
 }
 
-__global__ void __launch_bounds__(kSliceThreads) oz_slice_kernel(const double2 *__restrict__ Z, int64_t ldz,
-                                                                 const double *__restrict__ v, int64_t Kin,
-                                                                 int64_t ncols, int64_t rpb, int64_t bpad, int s,
-                                                                 uint8_t *__restrict__ digits, int64_t Kpad,
-                                                                 int64_t plane_rows, int32_t *__restrict__ expo,
-                                                                 int64_t pitch) {
-    const int64_t g = blockIdx.x;
+// One slicing launch covers an operand for every k-point of a group: the k-points' columns
+// are stacked as consecutive rows of each digit plane (row0 of an entry = its first row).
+struct SliceEntry {
+    const double2 *Z;          // source K x ncols, column-major, ld SliceTab::ldz
+    int64_t ncols;
+    int64_t row0;
+};
+struct SliceTab {
+    int nk = 0;
+    int s = 0;
+    int64_t ldz = 0, Kin = 0, rpb = 0, bpad = 0;
+    const double *v = nullptr;          // optional per-row weights (K)
+    uint8_t *digits = nullptr;
+    int64_t Kpad = 0, plane_rows = 0, pitch = 0;
+    int32_t *expo = nullptr;            // exponent of each plane row
+    SliceEntry e[kMaxGroup];
+};
+
+__global__ void __launch_bounds__(kSliceThreads) oz_slice_kernel(const __grid_constant__ SliceTab tab) {
+    const int64_t r = blockIdx.x;           // plane row
+    int k = 0;
+    while (k + 1 < tab.nk && tab.e[k + 1].row0 <= r) ++k;
+    const int64_t g = r - tab.e[k].row0;
+    const bool live = g >= 0 && g < tab.e[k].ncols;
+    const double2 *Zc = tab.e[k].Z + tab.ldz * (live ? g : 0);
+    const double *v = tab.v;
+    const int64_t Kin = tab.Kin, rpb = tab.rpb, bpad = tab.bpad, Kpad = tab.Kpad, pitch = tab.pitch;
+    const int64_t plane_rows = tab.plane_rows;
+    const int s = tab.s;
     __shared__ double red[kSliceThreads / 32];
     __shared__ int e_sh;
-    const bool live = g < ncols;
     // pass 1: column max of max(|re|, |im|) * v
     double mx = 0.0;
     if (live) {
-        const double2 *col = Z + ldz * g;
-        for (int64_t k = threadIdx.x; k < Kin; k += blockDim.x) {
-            const double2 z = col[k];
+        for (int64_t kk = threadIdx.x; kk < Kin; kk += blockDim.x) {
+            const double2 z = Zc[kk];
             double a = fmax(fabs(z.x), fabs(z.y));
-            if (v) a *= v[k];
+            if (v) a *= v[kk];
             mx = fmax(mx, a);
         }
     }
@@ -504,7 +524,7 @@ __global__ void __launch_bounds__(kSliceThreads) oz_slice_kernel(const double2 *
         int e = 0;
         if (m > 0.0) frexp(m, &e);                 // m < 2^e
         e_sh = e;
-        if (g < plane_rows) expo[g] = e;
+        tab.expo[r] = e;
     }
     __syncthreads();
     const int e = e_sh;
@@ -516,47 +536,41 @@ __global__ void __launch_bounds__(kSliceThreads) oz_slice_kernel(const double2 *
 #pragma unroll
         for (int u = 0; u < kSliceVec; ++u) {
             const int64_t kp = kp0 + u;
-            const int64_t b = kp / bpad, r = kp - b * bpad;
-            const int64_t k = b * rpb + r;
+            const int64_t b = kp / bpad, rr = kp - b * bpad;
+            const int64_t kk = b * rpb + rr;
             xr[u] = 0; xi[u] = 0;
-            if (live && b < nb && r < rpb && k < Kin) {
-                const double2 z = Z[ldz * g + k];
-                const double sc = v ? base_scale * v[k] : base_scale;
+            if (live && b < nb && rr < rpb && kk < Kin) {
+                const double2 z = Zc[kk];
+                const double sc = v ? base_scale * v[kk] : base_scale;
                 xr[u] = __double2ll_rn(z.x * sc);
                 xi[u] = __double2ll_rn(z.y * sc);
             }
         }
-        // digits from the least significant: d_i = ((X + 16) mod 32) - 16, X = (X - d_i) / 32
-        uint32_t lo_r[kOzMaxSlices], hi_r[kOzMaxSlices], lo_i[kOzMaxSlices], hi_i[kOzMaxSlices];
+        // digits from the least significant: d_i = ((X + 16) mod 32) - 16, X = (X - d_i) / 32,
+        // written plane by plane (8 consecutive bytes per thread and plane)
+        uint8_t *row = tab.digits + r * pitch + kp0;
+        const int64_t plane = plane_rows * pitch;
 #pragma unroll
-        for (int i = 0; i < kOzMaxSlices; ++i) { lo_r[i] = hi_r[i] = lo_i[i] = hi_i[i] = 0u; }
+        for (int i = kOzMaxSlices - 1; i >= 0; --i) {
+            if (i >= s) continue;
+            uint32_t lr = 0u, hr = 0u, li = 0u, hi = 0u;
 #pragma unroll
-        for (int u = 0; u < kSliceVec; ++u) {
-            long long a = xr[u], b = xi[u];
-#pragma unroll
-            for (int i = kOzMaxSlices - 1; i >= 0; --i) {
-                if (i >= s) continue;
+            for (int u = 0; u < kSliceVec; ++u) {
                 int da, db;
                 if (i == 0) {
-                    da = (int)a; db = (int)b;
+                    da = (int)xr[u]; db = (int)xi[u];
                 } else {
-                    da = (int)(((a + 16) & 31) - 16);
-                    db = (int)(((b + 16) & 31) - 16);
-                    a = (a - da) >> 5;
-                    b = (b - db) >> 5;
+                    da = (int)(((xr[u] + 16) & 31) - 16);
+                    db = (int)(((xi[u] + 16) & 31) - 16);
+                    xr[u] = (xr[u] - da) >> 5;
+                    xi[u] = (xi[u] - db) >> 5;
                 }
                 const uint32_t ea = e4m3_of_digit(da) << (8 * (u & 3));
                 const uint32_t eb = e4m3_of_digit(db) << (8 * (u & 3));
-                if (u < 4) { lo_r[i] |= ea; lo_i[i] |= eb; } else { hi_r[i] |= ea; hi_i[i] |= eb; }
+                if (u < 4) { lr |= ea; li |= eb; } else { hr |= ea; hi |= eb; }
             }
-        }
-#pragma unroll
-        for (int i = 0; i < kOzMaxSlices; ++i) {
-            if (i >= s) continue;
-            uint8_t *pr = digits + ((int64_t)(2 * i) * plane_rows + g) * pitch + kp0;
-            uint8_t *pi = digits + ((int64_t)(2 * i + 1) * plane_rows + g) * pitch + kp0;
-            *reinterpret_cast<uint2 *>(pr) = make_uint2(lo_r[i], hi_r[i]);
-            *reinterpret_cast<uint2 *>(pi) = make_uint2(lo_i[i], hi_i[i]);
+            *reinterpret_cast<uint2 *>(row + (int64_t)(2 * i) * plane) = make_uint2(lr, hr);
+            *reinterpret_cast<uint2 *>(row + (int64_t)(2 * i + 1) * plane) = make_uint2(li, hi);
         }
     }
 }
@@ -655,11 +669,23 @@ void carve_operand(Arena &a, DigitOperand &d, int s, int64_t rows, int64_t Kpad)
     d.expo = a.take<int32_t>(d.plane_rows);
 }
 
+SliceTab slice_table(const double2 *Z, int64_t ldz, const double *v, int64_t Kin, int64_t ncols, int64_t rpb,
+                     int64_t bpad, int s, const DigitOperand &d) {
+    SliceTab t;
+    t.nk = 1; t.s = s; t.ldz = ldz; t.Kin = Kin; t.rpb = rpb; t.bpad = bpad; t.v = v;
+    t.digits = d.digits; t.Kpad = d.Kpad; t.plane_rows = d.plane_rows; t.pitch = d.pitch; t.expo = d.expo;
+    t.e[0] = SliceEntry{Z, ncols, 0};
+    return t;
+}
+
+cudaError_t slice_launch(const SliceTab &t, cudaStream_t st) {
+    oz_slice_kernel<<<(unsigned)t.plane_rows, kSliceThreads, 0, st>>>(t);
+    return cudaGetLastError();
+}
+
 cudaError_t slice(const double2 *Z, int64_t ldz, const double *v, int64_t Kin, int64_t ncols, int64_t rpb,
                   int64_t bpad, int s, DigitOperand &d, cudaStream_t st) {
-    oz_slice_kernel<<<(unsigned)d.plane_rows, kSliceThreads, 0, st>>>(Z, ldz, v, Kin, ncols, rpb, bpad, s, d.digits,
-                                                                       d.Kpad, d.plane_rows, d.expo, d.pitch);
-    return cudaGetLastError();
+    return slice_launch(slice_table(Z, ldz, v, Kin, ncols, rpb, bpad, s, d), st);
 }
 
 int64_t job_tiles(const OzJob &j) {
@@ -844,120 +870,332 @@ int ozaki_herkx(OzakiPlan &oz, const double2 *P, int64_t ldp, const double2 *Q, 
     return rc;
 }
 
-// Full pipeline for one k-point: slices of C, wC, T, the Ozaki T application
-// X = T C (FP64 out), slices of X, then the S and H lower-triangle tiles in one launch.
-int64_t ozaki_pipeline_workspace(int s, int64_t twoL, int64_t na, int64_t nt, int64_t G) {
+// ---------------------------------------------------------------- k-point groups
+// A group is a set of k-points whose digit operands are resident together.  Its digit planes
+// stack the k-points' columns as consecutive rows, so one tensor map per operand covers every
+// k-point, one slicing launch per operand covers the group, and one oz_gemm launch runs the T
+// application and one the S/H products of all k-points.  Everything but the output pointers
+// is prepared once; a run only enqueues launches (it can be captured in a CUDA graph).
+struct OzGroup {
+    int s = 0, nk = 0;
+    bool hoist = false;
+    int64_t twoL = 0, na = 0, nt = 0, K = 0, bpad = 0, Kpad = 0, rows = 0;
+    std::vector<OzKBufs> kb;
+    std::vector<int64_t> row0;
+    DigitOperand dC, dW, dX, dM, dT;
+    SliceTab tC, tW, tM, tX;
+    CUtensorMap maps_t[4], maps_sh[4];
+    OzJob *d_jobs_t = nullptr, *d_jobs_sh = nullptr, *h_jobs_sh = nullptr;
+    int n_jobs_t = 0, n_jobs_sh = 0;
+    int4 *d_list_t = nullptr, *d_list_sh = nullptr;
+    int64_t tiles_t = 0, tiles_sh = 0;
+    int *d_progress = nullptr;
+    int *d_err = nullptr;
+};
+
+namespace {
+
+int64_t group_rows(const std::vector<int64_t> &G) {
+    int64_t r = 0;
+    for (int64_t g : G) r += round_up(std::max<int64_t>(g, 1), kTileM);
+    return r + kTileM;
+}
+
+int upload_schedule(std::vector<OzJob> &jobs, OzJob *d_jobs, int4 *d_list, int64_t &tiles) {
+    int64_t total = 0;
+    for (auto &j : jobs) {
+        j.tiles_n = (j.n + kTileN - 1) / kTileN;
+        j.tile_begin = total;
+        total += job_tiles(j);
+    }
+    std::vector<int4> list;
+    build_schedule(jobs, list);
+    if ((int64_t)list.size() != total) { g_oz_err = "tile schedule size mismatch"; return HSDLA_ERR_ARG; }
+    cudaError_t e = cudaMemcpy(d_jobs, jobs.data(), sizeof(OzJob) * jobs.size(), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && total > 0)
+        e = cudaMemcpy(d_list, list.data(), sizeof(int4) * list.size(), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) { g_oz_err = cudaGetErrorString(e); return HSDLA_ERR_CUDA; }
+    tiles = total;
+    return HSDLA_OK;
+}
+
+// Launch of a prepared job table (no host synchronisation; capturable).
+cudaError_t launch_prepared(const CUtensorMap *maps, int s, int *d_err, const OzJob *d_jobs, int n_jobs,
+                            int64_t total, const int4 *d_list, int *d_progress, cudaStream_t st) {
+    if (total <= 0) return cudaSuccess;
+    const size_t smem = (size_t)kStages * kStageBytes + 1024;
+    cudaError_t e = cudaFuncSetAttribute(oz_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    int dev = 0, nsm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    const int64_t grid = std::min<int64_t>(total, nsm);
+    const bool lockstep = d_progress && grid > 1 && grid <= kProgressCap && env_int("HSDLA_LOCKSTEP", 1) != 0;
+    if (lockstep) {
+        const int64_t g4 = (grid + 3) / 4 * 4;
+        e = cudaMemsetAsync(d_progress, 0, sizeof(int) * grid, st);
+        if (e == cudaSuccess && g4 > grid) e = cudaMemsetAsync(d_progress + grid, 0x7F, sizeof(int) * (g4 - grid), st);
+        if (e != cudaSuccess) return e;
+        CUtensorMap m0 = maps[0], m1 = maps[1], m2 = maps[2], m3 = maps[3];
+        const OzJob *pj = d_jobs;
+        int nj = n_jobs;
+        int64_t tt = total;
+        int ss = s;
+        int *perr = d_err;
+        const int4 *pl = d_list;
+        int *pp = d_progress;
+        void *args[] = {&m0, &m1, &m2, &m3, &pj, &nj, &tt, &ss, &perr, &pl, &pp};
+        return cudaLaunchCooperativeKernel((const void *)oz_gemm_kernel, dim3((unsigned)grid), dim3(kThreads), args,
+                                           smem, st);
+    }
+    oz_gemm_kernel<<<(unsigned)grid, kThreads, smem, st>>>(maps[0], maps[1], maps[2], maps[3], d_jobs, n_jobs, total,
+                                                            s, d_err, d_list, nullptr);
+    return cudaGetLastError();
+}
+
+}  // namespace
+
+// Run-time scratch of a group (digit planes and exponents, rewritten by every run; groups of a
+// plan share it) and its persistent part (T digits, job tables, tile schedules, lockstep slots).
+int64_t ozaki_group_bytes(int s, int64_t twoL, int64_t na, int64_t nt, const std::vector<int64_t> &G) {
+    const int64_t bpad = round_up(twoL, kKBlock), Kpad = bpad * na, rows = group_rows(G);
+    const int64_t dig = round_up(2 * s * rows * (Kpad + pitch_pad()), 1024) + round_up(4 * rows, 1024);
+    return 3 * dig + 4096;
+}
+
+int64_t ozaki_group_persist_bytes(int s, int64_t twoL, int64_t na, int64_t nt, const std::vector<int64_t> &G) {
     const int64_t bpad = round_up(twoL, kKBlock);
-    const int64_t Kpad = bpad * na;
-    const int64_t tiles_t = na * ((twoL + kTileM - 1) / kTileM) * ((G + kTileN - 1) / kTileN);
-    const int64_t cap = std::max(tiles_t, schedule_capacity_lower(G));
-    return 3 * operand_bytes(s, G, Kpad) + operand_bytes(s, nt * twoL, bpad) +
-           round_up(sizeof(OzJob) * (na + 4), 1024) + 4096 + round_up(sizeof(int4) * cap, 1024) +
-           round_up(sizeof(int) * kProgressCap, 1024);
+    const int64_t nk = (int64_t)G.size();
+    int64_t tiles_t = 0, tiles_sh = 0;
+    for (int64_t g : G) {
+        const int64_t T = (g + kTileN - 1) / kTileN;
+        tiles_t += std::max(na, nt) * ((twoL + kTileM - 1) / kTileM) * T;
+        tiles_sh += T * (T + 1);
+    }
+    return operand_bytes(s, nt * twoL, bpad) + round_up(sizeof(OzJob) * nk * (std::max(na, nt) + 2), 1024) +
+           round_up(sizeof(OzJob) * 2 * nk, 1024) + round_up(sizeof(int4) * (tiles_t + 1), 1024) +
+           round_up(sizeof(int4) * (tiles_sh + 1), 1024) + round_up(sizeof(int) * kProgressCap, 1024) + 8192;
+}
+
+int ozaki_group_prepare(OzakiPlan &oz, const OzGroupDesc &d, const std::vector<OzKBufs> &kb, void *ws,
+                        void *persist, cudaStream_t st, OzGroup **out) {
+    *out = nullptr;
+    if (kb.empty() || (int)kb.size() > kMaxGroup) { g_oz_err = "group size out of range"; return HSDLA_ERR_ARG; }
+    auto *g = new OzGroup();
+    g->s = oz.num_slices;
+    g->nk = (int)kb.size();
+    g->hoist = d.hoist;
+    g->twoL = d.twoL; g->na = d.na; g->nt = d.nt;
+    g->K = d.twoL * d.na;
+    g->bpad = round_up(d.twoL, kKBlock);
+    g->Kpad = g->bpad * d.na;
+    g->kb = kb;
+    g->d_err = oz.d_error;
+    std::vector<int64_t> G;
+    for (auto &k : kb) G.push_back(k.G);
+    g->rows = group_rows(G);
+    int64_t r0 = 0;
+    for (int64_t x : G) { g->row0.push_back(r0); r0 += round_up(std::max<int64_t>(x, 1), kTileM); }
+    const int s = g->s;
+    Arena ar{reinterpret_cast<char *>(ws)};
+    Arena keep{reinterpret_cast<char *>(persist)};
+    auto carve_rows = [&](DigitOperand &o, int64_t kpad) {
+        o.plane_rows = g->rows;
+        o.Kpad = kpad;
+        o.pitch = kpad + pitch_pad();
+        o.digits = ar.take<uint8_t>(2 * s * o.plane_rows * o.pitch);
+        o.expo = ar.take<int32_t>(o.plane_rows);
+    };
+    carve_rows(g->dC, g->Kpad);
+    carve_rows(g->dW, g->Kpad);
+    carve_rows(g->dX, g->Kpad);
+    carve_operand(keep, g->dT, s, d.nt * d.twoL, g->bpad);
+    // the M digits (per-type rows, K = bpad nt) borrow the X digit region, free until X is sliced
+    g->dM.plane_rows = g->rows;
+    g->dM.Kpad = g->bpad * d.nt;
+    g->dM.pitch = g->dM.Kpad + pitch_pad();
+    g->dM.digits = g->dX.digits;
+    g->dM.expo = g->dX.expo;
+    const int64_t nk = g->nk;
+    int64_t tiles_t = 0, tiles_sh = 0;
+    for (int64_t x : G) {
+        const int64_t T = (x + kTileN - 1) / kTileN;
+        tiles_t += std::max(d.na, d.nt) * ((d.twoL + kTileM - 1) / kTileM) * T;
+        tiles_sh += T * (T + 1);
+    }
+    g->d_jobs_t = keep.take<OzJob>(nk * (std::max(d.na, d.nt) + 2));
+    g->d_jobs_sh = keep.take<OzJob>(2 * nk);
+    g->d_list_t = keep.take<int4>(tiles_t + 1);
+    g->d_list_sh = keep.take<int4>(tiles_sh + 1);
+    g->d_progress = keep.take<int>(kProgressCap);
+    int rc = HSDLA_OK;
+    auto fail = [&](int code) { ozaki_group_destroy(g); return code; };
+    if (cudaHostAlloc((void **)&g->h_jobs_sh, sizeof(OzJob) * 2 * nk, cudaHostAllocDefault) != cudaSuccess) {
+        g->h_jobs_sh = nullptr;
+        g_oz_err = "pinned job table allocation failed";
+        return fail(HSDLA_ERR_NOMEM);
+    }
+    // slicing tables of the group's operands
+    auto table = [&](const DigitOperand &o, int64_t ldz, const double *v, int64_t Kin, int which) {
+        SliceTab t;
+        t.nk = g->nk; t.s = s; t.ldz = ldz; t.Kin = Kin; t.rpb = d.twoL; t.bpad = g->bpad; t.v = v;
+        t.digits = o.digits; t.Kpad = o.Kpad; t.plane_rows = o.plane_rows; t.pitch = o.pitch; t.expo = o.expo;
+        for (int k = 0; k < g->nk; ++k) {
+            const double2 *src = which == 1 ? kb[k].M : kb[k].CX;
+            t.e[k] = SliceEntry{src, kb[k].G, g->row0[k]};
+        }
+        return t;
+    };
+    g->tC = table(g->dC, g->K, nullptr, g->K, 0);
+    g->tW = table(g->dW, g->K, d.w, g->K, 0);
+    g->tX = table(g->dX, g->K, nullptr, g->K, 0);
+    if (d.hoist) g->tM = table(g->dM, d.twoL * d.nt, nullptr, d.twoL * d.nt, 1);
+    // T digits once: they do not change between runs
+    cudaError_t e = slice(d.Tfull, d.twoL, nullptr, d.twoL, d.nt * d.twoL, d.twoL, g->bpad, s, g->dT, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) { g_oz_err = cudaGetErrorString(e); return fail(HSDLA_ERR_CUDA); }
+    rc = make_map(g->dC, s);
+    if (!rc) rc = make_map(g->dW, s);
+    if (!rc) rc = make_map(g->dX, s);
+    if (!rc) rc = make_map(g->dT, s);
+    if (!rc && d.hoist) rc = make_map(g->dM, s);
+    if (rc) return fail(rc);
+    // (b) T application jobs
+    std::vector<OzJob> jt;
+    for (int k = 0; k < g->nk; ++k) {
+        if (d.hoist) {
+            for (int64_t t = 0; t < d.nt; ++t) {
+                OzJob j;
+                memset(&j, 0, sizeof(j));
+                j.lmap = 3; j.rmap = 0;
+                j.lplane = g->dT.plane_rows; j.rplane = g->dM.plane_rows;
+                j.lrow0 = t * d.twoL; j.rrow0 = g->row0[k];
+                j.rk0 = t * g->bpad;
+                j.nkb = g->bpad / kKBlock;
+                j.m = d.twoL; j.n = kb[k].G;
+                j.out = kb[k].Z + d.twoL * t; j.ldo = d.twoL * d.nt;
+                j.el = g->dT.expo + t * d.twoL; j.er = g->dM.expo + g->row0[k];
+                jt.push_back(j);
+            }
+        } else {
+            for (int64_t a = 0; a < d.na; ++a) {
+                const int64_t t = d.atom_type[a];
+                OzJob j;
+                memset(&j, 0, sizeof(j));
+                j.lmap = 3; j.rmap = 0;
+                j.lplane = g->dT.plane_rows; j.rplane = g->dC.plane_rows;
+                j.lrow0 = t * d.twoL; j.rrow0 = g->row0[k];
+                j.rk0 = a * g->bpad;
+                j.nkb = g->bpad / kKBlock;
+                j.m = d.twoL; j.n = kb[k].G;
+                j.out = kb[k].CX + d.twoL * a; j.ldo = g->K;
+                j.el = g->dT.expo + t * d.twoL; j.er = g->dC.expo + g->row0[k];
+                jt.push_back(j);
+            }
+        }
+    }
+    g->n_jobs_t = (int)jt.size();
+    rc = upload_schedule(jt, g->d_jobs_t, g->d_list_t, g->tiles_t);
+    if (rc) return fail(rc);
+    g->maps_t[0] = d.hoist ? g->dM.map : g->dC.map;
+    g->maps_t[1] = g->maps_t[0]; g->maps_t[2] = g->maps_t[0]; g->maps_t[3] = g->dT.map;
+    // (c) S and H jobs; outputs are patched per run
+    std::vector<OzJob> jsh;
+    for (int k = 0; k < g->nk; ++k)
+        for (int which = 0; which < 2; ++which) {
+            OzJob j;
+            memset(&j, 0, sizeof(j));
+            j.lmap = 0; j.rmap = which == 0 ? 1 : 2; j.lower = 1;
+            j.lplane = g->dC.plane_rows; j.rplane = which == 0 ? g->dW.plane_rows : g->dX.plane_rows;
+            j.lrow0 = g->row0[k]; j.rrow0 = g->row0[k];
+            j.nkb = g->Kpad / kKBlock;
+            j.m = kb[k].G; j.n = kb[k].G;
+            j.el = g->dC.expo + g->row0[k];
+            j.er = (which == 0 ? g->dW.expo : g->dX.expo) + g->row0[k];
+            jsh.push_back(j);
+        }
+    g->n_jobs_sh = (int)jsh.size();
+    rc = upload_schedule(jsh, g->d_jobs_sh, g->d_list_sh, g->tiles_sh);
+    if (rc) return fail(rc);
+    memcpy(g->h_jobs_sh, jsh.data(), sizeof(OzJob) * jsh.size());
+    g->maps_sh[0] = g->dC.map; g->maps_sh[1] = g->dW.map; g->maps_sh[2] = g->dX.map; g->maps_sh[3] = g->dC.map;
+    *out = g;
+    return HSDLA_OK;
+}
+
+void ozaki_group_set_outputs(OzGroup *g, double2 *const *S, double2 *const *H, const int64_t *ld) {
+    for (int k = 0; k < g->nk; ++k) {
+        g->h_jobs_sh[2 * k].out = S[k];
+        g->h_jobs_sh[2 * k].ldo = ld[k];
+        g->h_jobs_sh[2 * k + 1].out = H[k];
+        g->h_jobs_sh[2 * k + 1].ldo = ld[k];
+    }
+}
+
+int ozaki_group_run(OzGroup *g, const DevSystem &sys, const KTable &ktab, cudaStream_t st, cudaEvent_t ev0,
+                    cudaEvent_t ev1, int *launches) {
+    int nl = 0;
+    cudaError_t e = slice_launch(g->tC, st);
+    if (e == cudaSuccess) e = slice_launch(g->tW, st);
+    nl += 2;
+    if (e == cudaSuccess && g->hoist) { e = slice_launch(g->tM, st); nl += 1; }
+    if (e == cudaSuccess)
+        e = launch_prepared(g->maps_t, g->s, g->d_err, g->d_jobs_t, g->n_jobs_t, g->tiles_t, g->d_list_t, nullptr, st);
+    nl += 1;
+    if (e == cudaSuccess && g->hoist) { e = launch_apply_phase_multi(sys, ktab, st); nl += 1; }
+    if (e == cudaSuccess) e = slice_launch(g->tX, st);
+    nl += 1;
+    // the S/H job table travels from pinned memory in stream order (a graph replays the copy)
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(g->d_jobs_sh, g->h_jobs_sh, sizeof(OzJob) * g->n_jobs_sh, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess && ev0) e = cudaEventRecord(ev0, st);
+    if (e == cudaSuccess)
+        e = launch_prepared(g->maps_sh, g->s, g->d_err, g->d_jobs_sh, g->n_jobs_sh, g->tiles_sh, g->d_list_sh,
+                            g->d_progress, st);
+    nl += 1;
+    if (e == cudaSuccess && ev1) e = cudaEventRecord(ev1, st);
+    if (launches) *launches = nl;
+    if (e != cudaSuccess) { g_oz_err = cudaGetErrorString(e); return HSDLA_ERR_CUDA; }
+    return HSDLA_OK;
+}
+
+void ozaki_group_destroy(OzGroup *g) {
+    if (!g) return;
+    if (g->h_jobs_sh) cudaFreeHost(g->h_jobs_sh);
+    delete g;
+}
+
+// One k-point through a temporary group (the slice autotuner's probe).
+int64_t ozaki_pipeline_workspace(int s, int64_t twoL, int64_t na, int64_t nt, int64_t G) {
+    const std::vector<int64_t> g{G};
+    return ozaki_group_bytes(s, twoL, na, nt, g) + ozaki_group_persist_bytes(s, twoL, na, nt, g) + 2048;
 }
 
 int ozaki_pipeline(OzakiPlan &oz, const OzakiInputs &in, double2 *S, double2 *H, int64_t ldo, void *ws,
                    cudaStream_t st, int *launches) {
-    const int s = oz.num_slices;
-    const int64_t twoL = in.twoL, na = in.na, nt = in.nt, G = in.G;
-    const int64_t K = twoL * na;
-    const int64_t bpad = round_up(twoL, kKBlock);
-    const int64_t Kpad = bpad * na;
-    Arena ar{reinterpret_cast<char *>(ws)};
-    DigitOperand dC, dW, dX, dT;
-    carve_operand(ar, dC, s, G, Kpad);
-    carve_operand(ar, dW, s, G, Kpad);
-    carve_operand(ar, dX, s, G, Kpad);
-    carve_operand(ar, dT, s, nt * twoL, bpad);
-    OzJob *d_jobs = ar.take<OzJob>(na + 4);
-    const int64_t tiles_t = na * ((twoL + kTileM - 1) / kTileM) * ((G + kTileN - 1) / kTileN);
-    int4 *d_list = ar.take<int4>(std::max(tiles_t, schedule_capacity_lower(G)));
-    int *d_progress = ar.take<int>(kProgressCap);
-    int nl = 0;
-    cudaError_t e = slice(in.C, K, nullptr, K, G, twoL, bpad, s, dC, st);
-    if (e == cudaSuccess) e = slice(in.C, K, in.w, K, G, twoL, bpad, s, dW, st);
-    if (e == cudaSuccess) e = slice(in.Tfull, twoL, nullptr, twoL, nt * twoL, twoL, bpad, s, dT, st);
-    if (e != cudaSuccess) { g_oz_err = cudaGetErrorString(e); return HSDLA_ERR_CUDA; }
-    nl += 3;
-    int rc = make_map(dC, s);
-    if (!rc) rc = make_map(dW, s);
-    if (!rc) rc = make_map(dX, s);
-    if (!rc) rc = make_map(dT, s);
+    OzGroupDesc d;
+    d.twoL = in.twoL; d.na = in.na; d.nt = in.nt; d.hoist = in.M != nullptr;
+    d.w = in.w; d.Tfull = in.Tfull; d.atom_type = in.atom_type;
+    std::vector<OzKBufs> kb(1);
+    // the probe keeps C and X apart: C is its input, X is written by the T application
+    kb[0].CX = const_cast<double2 *>(in.C);
+    kb[0].M = const_cast<double2 *>(in.M);
+    kb[0].Z = in.Z;
+    kb[0].G = in.G;
+    OzGroup *g = nullptr;
+    const int64_t scratch = ozaki_group_bytes(oz.num_slices, in.twoL, in.na, in.nt, std::vector<int64_t>{in.G});
+    char *persist = reinterpret_cast<char *>(ws) + (scratch + 1023) / 1024 * 1024;
+    int rc = ozaki_group_prepare(oz, d, kb, ws, persist, st, &g);
     if (rc) return rc;
-    CUtensorMap maps[4] = {dC.map, dW.map, dX.map, dT.map};
-    std::vector<OzJob> jobs;
-    if (in.M) {
-        // (b) per type: Z_t = T_t M_t, then X_a = phase_a Z_t.  The M digits borrow the X digit
-        // region, which is free until X is sliced.
-        DigitOperand dM;
-        dM.plane_rows = dX.plane_rows;
-        dM.Kpad = bpad * nt;
-        dM.pitch = dM.Kpad + pitch_pad();
-        dM.digits = dX.digits;
-        dM.expo = dX.expo;
-        e = slice(in.M, twoL * nt, nullptr, twoL * nt, G, twoL, bpad, s, dM, st);
-        if (e != cudaSuccess) { g_oz_err = cudaGetErrorString(e); return HSDLA_ERR_CUDA; }
-        nl += 1;
-        rc = make_map(dM, s);
-        if (rc) return rc;
-        CUtensorMap tmaps[4] = {dM.map, dM.map, dM.map, dT.map};
-        for (int64_t t = 0; t < nt; ++t) {
-            OzJob j;
-            memset(&j, 0, sizeof(j));
-            j.lmap = 3; j.rmap = 0; j.lower = 0;
-            j.lplane = dT.plane_rows; j.rplane = dM.plane_rows;
-            j.lrow0 = t * twoL; j.rrow0 = 0;
-            j.lk0 = 0; j.rk0 = t * bpad;
-            j.nkb = bpad / kKBlock;
-            j.m = twoL; j.n = G;
-            j.out = in.Z + twoL * t; j.ldo = twoL * nt;
-            j.el = dT.expo + t * twoL; j.er = dM.expo;
-            jobs.push_back(j);
-        }
-        rc = launch_gemm(jobs, tmaps, s, oz.d_error, d_jobs, st, nullptr, nullptr, d_list);
-        if (rc) return rc;
-        e = launch_apply_phase(*in.sys, *in.kp, in.Z, twoL * nt, in.X, K, st);
-        if (e != cudaSuccess) { g_oz_err = cudaGetErrorString(e); return HSDLA_ERR_CUDA; }
-        nl += 2;
-    } else {
-    // (b) X_a = T_t C_a for every atom: left = T digits (rows = T columns of type t), right = C digits
-    for (int64_t a = 0; a < na; ++a) {
-        OzJob j;
-        memset(&j, 0, sizeof(j));
-        const int64_t t = in.atom_type[a];
-        j.lmap = 3; j.rmap = 0; j.lower = 0;
-        j.lplane = dT.plane_rows; j.rplane = dC.plane_rows;
-        j.lrow0 = t * twoL; j.rrow0 = 0;
-        j.lk0 = 0; j.rk0 = a * bpad;
-        j.nkb = bpad / kKBlock;
-        j.m = twoL; j.n = G;
-        j.out = in.X + twoL * a; j.ldo = K;
-        j.el = dT.expo + t * twoL; j.er = dC.expo;
-        jobs.push_back(j);
-    }
-    rc = launch_gemm(jobs, maps, s, oz.d_error, d_jobs, st, nullptr, nullptr, d_list);
-    if (rc) return rc;
-    nl += 1;
-    }
-    e = slice(in.X, K, nullptr, K, G, twoL, bpad, s, dX, st);
-    if (e != cudaSuccess) { g_oz_err = cudaGetErrorString(e); return HSDLA_ERR_CUDA; }
-    nl += 1;
-    // (c) S = C^H (w C), H = C^H X: lower-triangle tiles of both in one launch
-    jobs.clear();
-    for (int which = 0; which < 2; ++which) {
-        OzJob j;
-        memset(&j, 0, sizeof(j));
-        j.lmap = 0; j.rmap = which == 0 ? 1 : 2; j.lower = 1;
-        j.lplane = dC.plane_rows; j.rplane = which == 0 ? dW.plane_rows : dX.plane_rows;
-        j.nkb = Kpad / kKBlock;
-        j.m = G; j.n = G;
-        j.out = which == 0 ? S : H; j.ldo = ldo;
-        j.el = dC.expo; j.er = which == 0 ? dW.expo : dX.expo;
-        jobs.push_back(j);
-    }
-    rc = launch_gemm(jobs, maps, s, oz.d_error, d_jobs, st, in.ev_dom0, in.ev_dom1, d_list, d_progress);
-    nl += 1;
-    if (launches) *launches = nl;
+    double2 *Sp[1] = {S}, *Hp[1] = {H};
+    int64_t ld[1] = {ldo};
+    ozaki_group_set_outputs(g, Sp, Hp, ld);
+    KTable kt;
+    kt.nk = 1; kt.ldc = in.twoL * in.na; kt.ldm = in.twoL * in.nt; kt.total_cols = in.G;
+    if (in.kp) kt.e[0] = KEntry{*in.kp, nullptr, nullptr, in.Z, kb[0].CX, 0};
+    rc = ozaki_group_run(g, in.sys ? *in.sys : DevSystem{}, kt, st, in.ev_dom0, in.ev_dom1, launches);
+    if (rc == HSDLA_OK && cudaStreamSynchronize(st) != cudaSuccess) rc = HSDLA_ERR_CUDA;
+    ozaki_group_destroy(g);
     return rc;
 }
 

@@ -1,6 +1,8 @@
 // Ozaki-split FP64 contraction on the FP8 (e4m3) tensor cores of sm_103a.
 #pragma once
 
+#include <vector>
+
 #include "common.cuh"
 
 namespace hsdla {
@@ -34,6 +36,33 @@ struct OzakiInputs {
     const DevSystem *sys = nullptr;
     const DevKpoint *kp = nullptr;
 };
+
+// ---- k-point groups (prepared once per plan, run per execution; runs are graph-capturable)
+struct OzKBufs {
+    double2 *CX = nullptr;   // FP64 C of the k-point; reused for X once C is sliced (K x G, ld K)
+    double2 *M = nullptr;    // per-type rows M (2L nt x G), hoisted T application only
+    double2 *Z = nullptr;    // per-type products Z (2L nt x G), hoisted T application only
+    int64_t G = 0;
+};
+struct OzGroupDesc {
+    int64_t twoL = 0, na = 0, nt = 0;
+    bool hoist = false;
+    const double *w = nullptr;             // S row weights (K)
+    const double2 *Tfull = nullptr;        // per-type 2L x 2L blocks
+    const int32_t *atom_type = nullptr;    // host [na]
+};
+struct OzGroup;
+// scratch: rewritten by every run (may be shared by the groups of a plan); persist: owned by
+// the group for its lifetime (T digits, job tables, schedules)
+int64_t ozaki_group_bytes(int s, int64_t twoL, int64_t na, int64_t nt, const std::vector<int64_t> &G);
+int64_t ozaki_group_persist_bytes(int s, int64_t twoL, int64_t na, int64_t nt, const std::vector<int64_t> &G);
+int ozaki_group_prepare(OzakiPlan &oz, const OzGroupDesc &d, const std::vector<OzKBufs> &kb, void *ws,
+                        void *persist, cudaStream_t st, OzGroup **out);
+void ozaki_group_set_outputs(OzGroup *g, double2 *const *S, double2 *const *H, const int64_t *ld);
+// Enqueues the group's launches (slices, T application, phases, S/H products); no host sync.
+int ozaki_group_run(OzGroup *g, const DevSystem &sys, const KTable &ktab, cudaStream_t st, cudaEvent_t ev0,
+                    cudaEvent_t ev1, int *launches);
+void ozaki_group_destroy(OzGroup *g);
 
 int ozaki_plan_init(OzakiPlan &oz, int num_slices, double target);
 void ozaki_plan_release(OzakiPlan &oz);
