@@ -63,7 +63,7 @@ def _hs_parity(res, s, kps, tol=TOL):
 def test_create_hs_fp64_matches_oracle(ctx, cfg):
     s = synth.make_system(cfg)
     res, rep = ctx.create_hs(s, precision="fp64")
-    assert rep["kernel_launches"] >= 3 * len(s.kpoints)
+    assert rep["kernel_launches"] >= 3          # construct, T application, S/H (k-points batched)
     _hs_parity(res, s, s.kpoints)
 
 
