@@ -648,15 +648,17 @@ int64_t group_persist_bytes(const hsdla_plan *pl, const std::vector<int> &kidx) 
     return 4096 + (int64_t)sizeof(Fp64Job) * (int64_t)kidx.size() * (std::max(pl->na, pl->nt) + 4);
 }
 
-// Device-memory budget for one group's workspace: HSDLA_WORKSPACE_BUDGET (bytes) or 60% of the
-// device, reduced to fit the context's memory cap.
+// Device-memory budget for one group's workspace: HSDLA_WORKSPACE_BUDGET (bytes), else 85% of
+// what is free now (plus the workspace this context already holds) less 2 GiB, reduced to fit
+// the context's memory cap.
 int64_t workspace_budget(hsdla_context *ctx) {
     int64_t budget = 0;
     if (const char *v = getenv("HSDLA_WORKSPACE_BUDGET")) budget = strtoll(v, nullptr, 10);
     if (budget <= 0) {
         size_t fr = 0, tot = 0;
         cudaMemGetInfo(&fr, &tot);
-        budget = (int64_t)(0.6 * (double)tot);
+        budget = (int64_t)(0.85 * (double)(fr + (size_t)ctx->ws_bytes)) - ((int64_t)2 << 30);
+        budget = std::max<int64_t>(budget, (int64_t)1 << 30);
     }
     if (ctx->mem_cap > 0) budget = std::min(budget, ctx->mem_cap - ctx->mem_used + ctx->ws_bytes);
     return budget;

@@ -98,3 +98,27 @@ def test_batched_c0_ozaki_multi_kpoint(ctx):
     torch.cuda.synchronize()
     _check(_host(outs), base, kps)
     pl.close()
+
+
+def test_c3_subset_ozaki_graph_vs_fp64(ctx):
+    """Batching form (c3: 64 atoms, lmax 8, n_G ~6300): two k-points, graph-captured Ozaki
+    against the batched FP64 path on the GPU, and one k-point against the oracle."""
+    import torch
+    s = synth.make_system("c3")
+    kps = s.kpoints[:2]
+    oz = ctx.plan(s, kpoints=kps, precision="ozaki", num_slices=0, use_graph=True)
+    oo = oz.alloc_outputs()
+    oz.execute(oo)
+    rep = oz.execute(oo)
+    fp = ctx.plan(s, kpoints=kps, precision="fp64")
+    of = fp.alloc_outputs()
+    fp.execute(of)
+    torch.cuda.synchronize()
+    for (h1, s1), (h2, s2) in zip(_host(oo), _host(of)):
+        for X, R in ((h1, h2), (s1, s2)):
+            fro, mx = oracle.lower_errors(X, R)
+            assert fro < TOL and mx < TOL, (fro, mx)
+    assert rep["num_slices"] >= 9
+    _check(_host(of)[:1], s, kps[:1])
+    oz.close()
+    fp.close()
