@@ -81,6 +81,7 @@ struct hsdla_plan {
         int64_t tiles_sh = 0;
         void *persist = nullptr;         // prepared tables (not shared with other groups)
         int64_t persist_bytes = 0;
+        cudaEvent_t ev_dom[2] = {nullptr, nullptr};   // around the S/H launch (graph runs too)
     };
     std::vector<Group> groups;
     void *prepared_ws = nullptr;
@@ -695,6 +696,8 @@ void release_groups(hsdla_plan *pl) {
         if (g.oz) ozaki_group_destroy(g.oz);
         if (g.h_jobs_sh) cudaFreeHost(g.h_jobs_sh);
         if (g.persist) ctx_free(pl->ctx, g.persist, g.persist_bytes);
+        for (auto &e : g.ev_dom) if (e) cudaEventDestroy(e);
+        g.ev_dom[0] = g.ev_dom[1] = nullptr;
         g.oz = nullptr;
         g.h_jobs_sh = nullptr;
         g.persist = nullptr;
@@ -715,6 +718,8 @@ int prepare_groups(hsdla_plan *pl, void *ws, cudaStream_t st) {
         g.persist_bytes = group_persist_bytes(pl, g.kidx);
         int rcp = ctx_malloc(ctx, &g.persist, g.persist_bytes);
         if (rcp) return rcp;
+        CUDA_TRY(ctx, cudaEventCreate(&g.ev_dom[0]));
+        CUDA_TRY(ctx, cudaEventCreate(&g.ev_dom[1]));
         char *pp = reinterpret_cast<char *>(g.persist);
         auto keep = [&](int64_t bytes) { char *r = pp; pp += (bytes + 1023) / 1024 * 1024; return r; };
         KTable &kt = g.ktab;
@@ -820,6 +825,25 @@ void set_outputs(hsdla_plan *pl, hsdla_cx *const *dH, hsdla_cx *const *dS, const
     }
 }
 
+// Event record that becomes an external event-record node under stream capture.
+cudaError_t record_event(cudaEvent_t ev, cudaStream_t st) {
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    cudaStreamIsCapturing(st, &cs);
+    return cs == cudaStreamCaptureStatusActive ? cudaEventRecordWithFlags(ev, st, cudaEventRecordExternal)
+                                               : cudaEventRecord(ev, st);
+}
+
+// Device time of the S/H launches of the last execution (all groups; after it completed).
+float dominant_ms(const hsdla_plan *pl) {
+    float tot = 0.f;
+    for (const auto &g : pl->groups) {
+        float d = 0.f;
+        if (g.ev_dom[0] && cudaEventElapsedTime(&d, g.ev_dom[0], g.ev_dom[1]) == cudaSuccess) tot += d;
+    }
+    cudaGetLastError();
+    return tot;
+}
+
 // Algorithmic flops of the S/H launches of one execution (FP8 digit products for Ozaki).
 void run_groups_flop(const hsdla_plan *pl, double *dom_flop) {
     *dom_flop = 0.0;
@@ -850,8 +874,7 @@ int run_groups(hsdla_plan *pl, cudaStream_t st, bool timed, float *ms_ab, float 
         }
         if (g.oz) {
             int nl = 0;
-            const int rc = ozaki_group_run(g.oz, pl->dsys, g.ktab, st, timed ? ctx->evs[4] : nullptr,
-                                           timed ? ctx->evs[5] : nullptr, &nl);
+            const int rc = ozaki_group_run(g.oz, pl->dsys, g.ktab, st, g.ev_dom[0], g.ev_dom[1], &nl);
             if (rc) return set_err(ctx, rc, "Ozaki group failed: %s", ozaki_last_error());
             pl->launches += nl;
         } else {
@@ -863,19 +886,17 @@ int run_groups(hsdla_plan *pl, cudaStream_t st, bool timed, float *ms_ab, float 
             }
             CUDA_TRY(ctx, cudaMemcpyAsync(g.d_jobs_sh, g.h_jobs_sh, sizeof(Fp64Job) * 2 * g.ktab.nk,
                                           cudaMemcpyHostToDevice, st));
-            if (timed) CUDA_TRY(ctx, cudaEventRecord(ctx->evs[4], st));
+            CUDA_TRY(ctx, record_event(g.ev_dom[0], st));
             CUDA_TRY(ctx, launch_fp64_jobs(g.d_jobs_sh, 2 * g.ktab.nk, g.tiles_sh, st));
-            if (timed) CUDA_TRY(ctx, cudaEventRecord(ctx->evs[5], st));
+            CUDA_TRY(ctx, record_event(g.ev_dom[1], st));
             pl->launches++;
         }
         if (timed) {
             // stage times need the events: wait for this group (un-graphed runs only)
-            CUDA_TRY(ctx, cudaEventSynchronize(ctx->evs[5]));
-            float a = 0, d = 0;
+            CUDA_TRY(ctx, cudaEventSynchronize(g.ev_dom[1]));
+            float a = 0;
             cudaEventElapsedTime(&a, ctx->evs[0], ctx->evs[1]);
-            cudaEventElapsedTime(&d, ctx->evs[4], ctx->evs[5]);
             *ms_ab += a;
-            *ms_dom += d;
         }
     }
     return HSDLA_OK;
@@ -1017,7 +1038,7 @@ int hsdla_plan_execute(hsdla_plan *pl, hsdla_cx *const *dH, hsdla_cx *const *dS,
         rep->eff_tflops = ms > 0 ? pl->flop / (ms * 1e-3) / 1e12 : 0.0;
         rep->ms_construct_ab = ms_ab;
         rep->ms_contract = ms - ms_ab;
-        rep->ms_dominant = ms_dom;
+        rep->ms_dominant = dominant_ms(pl);
         rep->dominant_flop = dom_flop;
         rep->num_slices = pl->opts.precision == HSDLA_PREC_OZAKI_FP8 ? pl->oz.num_slices : 0;
         rep->est_rel_err = pl->est_err;

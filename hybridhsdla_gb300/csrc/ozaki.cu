@@ -1132,6 +1132,15 @@ void ozaki_group_set_outputs(OzGroup *g, double2 *const *S, double2 *const *H, c
     }
 }
 
+// Events around the S/H launch; under stream capture they become external event-record nodes
+// so that a replayed graph still times the launch.
+static cudaError_t record(cudaEvent_t ev, cudaStream_t st) {
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    cudaStreamIsCapturing(st, &cs);
+    return cs == cudaStreamCaptureStatusActive ? cudaEventRecordWithFlags(ev, st, cudaEventRecordExternal)
+                                               : cudaEventRecord(ev, st);
+}
+
 int ozaki_group_run(OzGroup *g, const DevSystem &sys, const KTable &ktab, cudaStream_t st, cudaEvent_t ev0,
                     cudaEvent_t ev1, int *launches) {
     int nl = 0;
@@ -1148,12 +1157,12 @@ int ozaki_group_run(OzGroup *g, const DevSystem &sys, const KTable &ktab, cudaSt
     // the S/H job table travels from pinned memory in stream order (a graph replays the copy)
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(g->d_jobs_sh, g->h_jobs_sh, sizeof(OzJob) * g->n_jobs_sh, cudaMemcpyHostToDevice, st);
-    if (e == cudaSuccess && ev0) e = cudaEventRecord(ev0, st);
+    if (e == cudaSuccess && ev0) e = record(ev0, st);
     if (e == cudaSuccess)
         e = launch_prepared(g->maps_sh, g->s, g->d_err, g->d_jobs_sh, g->n_jobs_sh, g->tiles_sh, g->d_list_sh,
                             g->d_progress, st);
     nl += 1;
-    if (e == cudaSuccess && ev1) e = cudaEventRecord(ev1, st);
+    if (e == cudaSuccess && ev1) e = record(ev1, st);
     if (launches) *launches = nl;
     if (e != cudaSuccess) { g_oz_err = cudaGetErrorString(e); return HSDLA_ERR_CUDA; }
     return HSDLA_OK;
