@@ -280,7 +280,7 @@ def run_ours(args):
     fp8_peak = 2.0 * peaks["bf16_tflops"]
     dom = float(np.median(dom_ms))
     achieved = dominant_flop / (dom * 1e-3) / 1e12
-    traffic = _traffic_from_profile()
+    traffic = _traffic_from_profile() if args.workload == "c2" else None
     roof = {"bound": "tensor", "achieved": achieved, "peak": fp8_peak, "unit": "TFLOP/s",
             "frac": achieved / fp8_peak, "traffic": traffic,
             "kernel": "oz_gemm_kernel (S and H lower-triangle digit products)",
