@@ -80,7 +80,7 @@ class ReportStruct(ctypes.Structure):
 EXPORTS = ["hsdla_context_create", "hsdla_context_destroy", "hsdla_last_error", "hsdla_set_mem_cap",
            "hsdla_prepare_tmat", "hsdla_create_hs", "hsdla_plan_create", "hsdla_plan_execute",
            "hsdla_plan_workspace_bytes", "hsdla_plan_destroy", "hsdla_plan_construct_ab",
-           "hsdla_zherkx_lower", "hsdla_zherkx_lower_noalloc"]
+           "hsdla_zherkx_lower", "hsdla_zherkx_lower_noalloc", "hsdla_contract_ab"]
 
 _lib = None
 
@@ -124,6 +124,10 @@ def load(build_if_missing: bool = True):
     L.hsdla_plan_construct_ab.argtypes = [vp, ctypes.c_int32, vp, vp]
     L.hsdla_zherkx_lower.argtypes = [vp, ctypes.c_int32, ctypes.c_int32, ctypes.c_int64, ctypes.c_int64, vp,
                                      ctypes.c_int64, vp, ctypes.c_int64, vp, vp, ctypes.c_int64, vp]
+    L.hsdla_contract_ab.argtypes = [vp, ctypes.c_int32, ctypes.c_int32, ctypes.c_int64, _cxp, _cxp, _ip,
+                                    ctypes.POINTER(_cxp), ctypes.POINTER(_cxp), ctypes.POINTER(_cxp), _ip,
+                                    ctypes.c_int32, _dp, _cxp, _cxp, ctypes.c_int64, ctypes.POINTER(OptsStruct),
+                                    ctypes.POINTER(ReportStruct)]
     L.hsdla_zherkx_lower_noalloc.argtypes = [ctypes.c_int32, ctypes.c_int64, ctypes.c_int64, vp, ctypes.c_int64, vp,
                                              ctypes.c_int64, vp, vp, ctypes.c_int64, vp]
     _lib = L
@@ -271,6 +275,30 @@ class Context:
         self.check(self.lib.hsdla_create_hs(self.h, ctypes.byref(sh.struct), kh.arr, nk, Hp, Sp, ld,
                                             ctypes.byref(o), ctypes.byref(rep)))
         return list(out), rep.as_dict()
+
+    def contract_ab(self, d, precision="fp64", num_slices=0):
+        """``create_HS2_stripped_v2`` drop-in (``hsdla_contract_ab``): H, S (lower triangles,
+        upper zero) from a :class:`hybridhsdla_gb300.flapw_data.DataIn` (caller-built A, B,
+        per-atom T blocks).  Returns (H, S, report)."""
+        A = np.asfortranarray(d.A, np.complex128)
+        B = np.asfortranarray(d.B, np.complex128)
+        a, G = d.a, d.G
+        sizes = np.ascontiguousarray([[t.shape[0] for t in blk] for blk in d.blocks], np.int32).reshape(-1)
+        keep = [[np.asfortranarray(t, np.complex128) for t in blk] for blk in d.blocks]
+        paa = (_cxp * a)(*[k[0].ctypes.data_as(_cxp) for k in keep])
+        pab = (_cxp * a)(*[k[1].ctypes.data_as(_cxp) for k in keep])
+        pbb = (_cxp * a)(*[k[2].ctypes.data_as(_cxp) for k in keep])
+        lmaxs = np.ascontiguousarray(d.lmaxs, np.int32)
+        un = np.ascontiguousarray(d.sqrt_u_norms, np.float64)
+        H = np.empty((G, G), np.complex128, order="F")
+        S = np.empty((G, G), np.complex128, order="F")
+        o = _opts(precision, num_slices)
+        rep = ReportStruct()
+        self.check(self.lib.hsdla_contract_ab(self.h, d.L, a, G, A.ctypes.data_as(_cxp), B.ctypes.data_as(_cxp),
+                                              sizes.ctypes.data_as(_ip), paa, pab, pbb, lmaxs.ctypes.data_as(_ip),
+                                              d.max_lmax, un.ctypes.data_as(_dp), H.ctypes.data_as(_cxp),
+                                              S.ctypes.data_as(_cxp), max(1, G), ctypes.byref(o), ctypes.byref(rep)))
+        return H, S, rep.as_dict()
 
     def plan(self, sys_, kpoints=None, precision="fp64", num_slices=0, tmats=None, target=0.0, use_graph=False):
         return Plan(self, sys_, sys_.kpoints if kpoints is None else kpoints, precision, num_slices, tmats, target,

@@ -92,6 +92,7 @@ struct hsdla_plan {
     bool graph_failed = false;
     bool autotune = false;           // Ozaki slice count still to be chosen from the data
     bool hoist = false;              // T application per type (no atom carries its own rotation)
+    bool external = false;           // C is supplied by the caller (contraction-only entry)
     double est_err = 0.0;            // autotuner's predicted relative error
     int launches = 0;
 };
@@ -863,8 +864,10 @@ int run_groups(hsdla_plan *pl, cudaStream_t st, bool timed, float *ms_ab, float 
     if (dom_flop) *dom_flop = 0.0;
     for (auto &g : pl->groups) {
         if (timed) CUDA_TRY(ctx, cudaEventRecord(ctx->evs[0], st));
-        CUDA_TRY(ctx, launch_construct_ab_multi(pl->dsys, g.ktab, st));
-        pl->launches++;
+        if (!pl->external) {
+            CUDA_TRY(ctx, launch_construct_ab_multi(pl->dsys, g.ktab, st));
+            pl->launches++;
+        }
         if (timed) CUDA_TRY(ctx, cudaEventRecord(ctx->evs[1], st));
         for (int q = 0; q < g.ktab.nk; ++q) {
             const double G = (double)g.ktab.e[q].kp.n_g;
@@ -1045,6 +1048,161 @@ int hsdla_plan_execute(hsdla_plan *pl, hsdla_cx *const *dH, hsdla_cx *const *dS,
         rep->kernel_launches = pl->launches;
     }
     return HSDLA_OK;
+}
+
+int hsdla_contract_ab(hsdla_context *ctx, int32_t L, int32_t a, int64_t G, const hsdla_cx *A, const hsdla_cx *B,
+                      const int32_t *t_sizes, const hsdla_cx *const *t_aa, const hsdla_cx *const *t_ab,
+                      const hsdla_cx *const *t_bb, const int32_t *lmaxs, int32_t max_lmax, const double *sqrt_u_norms,
+                      hsdla_cx *H, hsdla_cx *S, int64_t ld, const hsdla_opts *opts, hsdla_report *rep) {
+    using cx = std::complex<double>;
+    if (!ctx) return HSDLA_ERR_ARG;
+    CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+    if (L < 1 || a < 1 || G < 0 || max_lmax < 0 || max_lmax > kMaxLmax || (max_lmax + 1) * (max_lmax + 1) != L)
+        return set_err(ctx, HSDLA_ERR_ARG, "L=%d must equal (max_lmax+1)^2 with max_lmax=%d <= %d", L, max_lmax,
+                       kMaxLmax);
+    if (G == 0) return HSDLA_OK;
+    if (!A || !B || !t_sizes || !t_aa || !t_ab || !t_bb || !lmaxs || !sqrt_u_norms || !H || !S || ld < G)
+        return set_err(ctx, HSDLA_ERR_ARG, "a required pointer is NULL or ld < n_g");
+    const int nl = max_lmax + 1;
+    const int64_t twoL = 2 * (int64_t)L;
+    std::vector<cx> tf_all((size_t)a * twoL * twoL, 0.0);
+    std::vector<double> w(twoL * a), wsq(twoL * a);
+    for (int j = 0; j < a; ++j) {
+        const int na_ = t_sizes[3 * j], nab = t_sizes[3 * j + 1], nb = t_sizes[3 * j + 2];
+        if (na_ < 0 || nab < 0 || nb < 0 || na_ > L || nab > L || nb > L || lmaxs[j] < 0 || lmaxs[j] > max_lmax)
+            return set_err(ctx, HSDLA_ERR_ARG, "atom %d: T sizes (%d, %d, %d) or lmax %d out of range", j, na_, nab, nb,
+                           lmaxs[j]);
+        const cx *aa = reinterpret_cast<const cx *>(t_aa[j]);
+        const cx *ab = reinterpret_cast<const cx *>(t_ab[j]);
+        const cx *bb = reinterpret_cast<const cx *>(t_bb[j]);
+        if ((na_ && !aa) || (nab && !ab) || (nb && !bb)) return set_err(ctx, HSDLA_ERR_ARG, "atom %d: T block NULL", j);
+        cx *T = tf_all.data() + (size_t)j * twoL * twoL;
+        // zhemm('L') reads the lower triangles of T_AA and T_BB (h_and_s_stripped_v2.cpp:202,345);
+        // zgemm('C') the whole T_AB (:209); blocks smaller than L are zero-padded, which is what
+        // the reference's row compaction (X_height, :211-230) amounts to
+        for (int c = 0; c < na_; ++c)
+            for (int r = 0; r < na_; ++r) T[r + twoL * c] = (r >= c) ? aa[r + na_ * c] : std::conj(aa[c + na_ * r]);
+        for (int c = 0; c < nb; ++c)
+            for (int r = 0; r < nb; ++r)
+                T[(L + r) + twoL * (L + c)] = (r >= c) ? bb[r + nb * c] : std::conj(bb[c + nb * r]);
+        for (int c = 0; c < nab; ++c)
+            for (int r = 0; r < nab; ++r) {
+                T[r + twoL * (L + c)] = ab[r + nab * c];
+                T[(L + c) + twoL * r] = std::conj(ab[r + nab * c]);
+            }
+        for (int l = 0; l < nl; ++l) {
+            const double su = sqrt_u_norms[j * nl + l];
+            for (int lm = l * l; lm < (l + 1) * (l + 1); ++lm) {
+                w[twoL * j + lm] = 1.0; wsq[twoL * j + lm] = 1.0;
+                // rows above the atom's lmax are left unset by apply_u_norm_s (:64-86) while B is 0 there
+                const double u = (l <= lmaxs[j]) ? su * su : 0.0;
+                w[twoL * j + L + lm] = u; wsq[twoL * j + L + lm] = std::sqrt(u);
+            }
+        }
+    }
+    for (const cx &v : tf_all)
+        if (!std::isfinite(v.real()) || !std::isfinite(v.imag())) return set_err(ctx, HSDLA_ERR_INPUT, "T not finite");
+    if (!finite_all(sqrt_u_norms, (int64_t)a * nl)) return set_err(ctx, HSDLA_ERR_INPUT, "u norms not finite");
+    // ---- an external plan: every atom its own type, per-atom T application, C from the caller
+    auto *pl = new hsdla_plan();
+    pl->ctx = ctx;
+    if (opts) pl->opts = *opts;
+    if (pl->opts.precision != HSDLA_PREC_FP64 && pl->opts.precision != HSDLA_PREC_OZAKI_FP8) {
+        delete pl;
+        return set_err(ctx, HSDLA_ERR_ARG, "unknown precision %d", pl->opts.precision);
+    }
+    if (pl->opts.target_rel_err <= 0.0) pl->opts.target_rel_err = 1e-13;
+    pl->L = L; pl->na = a; pl->nt = a; pl->max_lmax = max_lmax;
+    pl->hoist = false;
+    pl->external = true;
+    pl->twoLa = twoL * a;
+    pl->atom_type.resize(a);
+    for (int j = 0; j < a; ++j) pl->atom_type[j] = j;
+    const int64_t bytes = ((int64_t)sizeof(double2) * tf_all.size() + 255) / 256 * 256 + 2 * 8 * pl->twoLa + 512;
+    int rc = ctx_malloc(ctx, &pl->tables, bytes);
+    if (rc) { delete pl; return rc; }
+    pl->tables_bytes = bytes;
+    ctx->plans.insert(pl);
+    char *dp = reinterpret_cast<char *>(pl->tables);
+    pl->Tfull = reinterpret_cast<double2 *>(dp);
+    pl->w = reinterpret_cast<double *>(dp + ((int64_t)sizeof(double2) * tf_all.size() + 255) / 256 * 256);
+    pl->wsqrt = pl->w + pl->twoLa;
+    PlanKpoint pk;
+    pk.n_g = G;
+    pk.dk.n_g = G;
+    pl->kps.push_back(pk);
+    pl->flop = 20.0 * (double)G * G * L * a + 24.0 * (double)L * L * a * G;
+    cudaStream_t st = ctx->stream;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    void *dout = nullptr, *ws = nullptr;
+    auto done = [&](int code) {
+        cudaStreamSynchronize(st);
+        if (dout) ctx_free(ctx, dout, 2 * G * G * (int64_t)sizeof(double2));
+        hsdla_plan_destroy(pl);
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        return code;
+    };
+    cudaEventRecord(e0, st);
+    if (cudaMemcpyAsync(pl->Tfull, tf_all.data(), sizeof(double2) * tf_all.size(), cudaMemcpyHostToDevice, st) !=
+            cudaSuccess ||
+        cudaMemcpyAsync(pl->w, w.data(), 8 * pl->twoLa, cudaMemcpyHostToDevice, st) != cudaSuccess ||
+        cudaMemcpyAsync(pl->wsqrt, wsq.data(), 8 * pl->twoLa, cudaMemcpyHostToDevice, st) != cudaSuccess ||
+        cudaStreamSynchronize(st) != cudaSuccess)
+        return done(set_err(ctx, HSDLA_ERR_CUDA, "table upload failed"));
+    if (pl->opts.precision == HSDLA_PREC_OZAKI_FP8) {
+        // no sampling autotune without the physics inputs: num_slices = 0 means the default
+        rc = ozaki_plan_init(pl->oz, pl->opts.num_slices, pl->opts.target_rel_err);
+        if (rc) return done(set_err(ctx, rc, "bad slice count"));
+    }
+    form_groups(pl, workspace_budget(ctx));
+    rc = ctx_workspace(ctx, hsdla_plan_workspace_bytes(pl), &ws);
+    if (rc) return done(rc);
+    rc = prepare_groups(pl, ws, st);
+    if (rc) return done(rc);
+    rc = ctx_malloc(ctx, &dout, 2 * G * G * (int64_t)sizeof(double2));
+    if (rc) return done(rc);
+    hsdla_cx *dH = reinterpret_cast<hsdla_cx *>(dout), *dS = dH + G * G;
+    const int64_t ldd = G;
+    // A, B (L x a x G, column-major) straight into C's per-atom [A_a; B_a] row blocks
+    const KEntry &e = pl->groups[0].ktab.e[0];
+    if (cudaMemsetAsync(dout, 0, 2 * G * G * sizeof(double2), st) != cudaSuccess ||
+        cudaMemcpy2DAsync(e.C, twoL * sizeof(double2), A, L * sizeof(double2), L * sizeof(double2), (size_t)a * G,
+                          cudaMemcpyHostToDevice, st) != cudaSuccess ||
+        cudaMemcpy2DAsync(e.C + L, twoL * sizeof(double2), B, L * sizeof(double2), L * sizeof(double2), (size_t)a * G,
+                          cudaMemcpyHostToDevice, st) != cudaSuccess)
+        return done(set_err(ctx, HSDLA_ERR_CUDA, "A/B upload failed"));
+    set_outputs(pl, &dH, &dS, &ldd);
+    float ms_ab = 0.f, ms_dom = 0.f;
+    double dom_flop = 0.0;
+    rc = run_groups(pl, st, true, &ms_ab, &ms_dom, &dom_flop);
+    if (rc) return done(rc);
+    if (cudaMemcpy2DAsync(H, ld * sizeof(hsdla_cx), dH, G * sizeof(hsdla_cx), G * sizeof(hsdla_cx), G,
+                          cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+        cudaMemcpy2DAsync(S, ld * sizeof(hsdla_cx), dS, G * sizeof(hsdla_cx), G * sizeof(hsdla_cx), G,
+                          cudaMemcpyDeviceToHost, st) != cudaSuccess)
+        return done(set_err(ctx, HSDLA_ERR_CUDA, "H/S download failed"));
+    cudaEventRecord(e1, st);
+    if (cudaStreamSynchronize(st) != cudaSuccess) return done(set_err(ctx, HSDLA_ERR_CUDA, "sync failed"));
+    rc = ozaki_check_device_error(pl->oz);
+    if (rc) return done(set_err(ctx, rc, "device-side error: %s", ozaki_last_error()));
+    if (rep) {
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        memset(rep, 0, sizeof(*rep));
+        rep->ms_total = ms;
+        rep->ms_per_kpoint = ms;
+        rep->num_kpoints = 1;
+        rep->flop = pl->flop;
+        rep->eff_tflops = ms > 0 ? pl->flop / (ms * 1e-3) / 1e12 : 0.0;
+        rep->ms_dominant = dominant_ms(pl);
+        rep->dominant_flop = dom_flop;
+        rep->num_slices = pl->opts.precision == HSDLA_PREC_OZAKI_FP8 ? pl->oz.num_slices : 0;
+        rep->kernel_launches = pl->launches;
+    }
+    return done(HSDLA_OK);
 }
 
 int hsdla_create_hs(hsdla_context *ctx, const hsdla_system *s, const hsdla_kpoint *kpts, int32_t nk,

@@ -144,6 +144,22 @@ int hsdla_create_hs(hsdla_context *ctx, const hsdla_system *sys, const hsdla_kpo
                     hsdla_cx *const *H, hsdla_cx *const *S, const int64_t *ld,
                     const hsdla_opts *opts, hsdla_report *report);
 
+/* Contraction-only drop-in for create_HS2_stripped_v2(L, a, G, A, B, H, S, T, l_maxs, max_lmax,
+ * u_norms, method, W) (flapw_opt/src/h_and_s_stripped_v2.cpp:100-382,
+ * flapw_opt/src/include/acc/h_and_s_stripped.h:24): H and S from caller-built matching tensors.
+ * A, B: HOST L x a x G complex (column-major cube, element (lm, atom, g) at lm + L atom + L a g),
+ * L = (max_lmax+1)^2.  Per atom j: t_sizes[3j..3j+2] = (aa_size, ab_size, bb_size) and the
+ * column-major blocks t_aa[j], t_ab[j], t_bb[j] (the reference's myTMat; T_AA/T_BB through their
+ * lower triangles, smaller blocks act zero-padded).  lmaxs[a], sqrt_u_norms[a][max_lmax+1] =
+ * sqrt(||udot_l||^2) as the reference packs them (h_and_s.cpp:700-715).  H, S: HOST G x G,
+ * leading dimension ld; lower triangles written, upper triangles set to zero.  With Ozaki
+ * precision, num_slices = 0 selects the default slice count (no sampling autotune here). */
+int hsdla_contract_ab(hsdla_context *ctx, int32_t L, int32_t num_atoms, int64_t n_g, const hsdla_cx *A,
+                      const hsdla_cx *B, const int32_t *t_sizes, const hsdla_cx *const *t_aa,
+                      const hsdla_cx *const *t_ab, const hsdla_cx *const *t_bb, const int32_t *lmaxs,
+                      int32_t max_lmax, const double *sqrt_u_norms, hsdla_cx *H, hsdla_cx *S, int64_t ld,
+                      const hsdla_opts *opts, hsdla_report *report);
+
 /* Device-resident execution: a plan uploads the system and the k-point lists once and owns
  * the device workspace (A/B tensors, T blocks, digit slices). */
 int hsdla_plan_create(hsdla_context *ctx, const hsdla_system *sys, const hsdla_kpoint *kpts, int32_t nk,

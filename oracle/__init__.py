@@ -246,3 +246,53 @@ def lower_errors(X: np.ndarray, X_ref: np.ndarray) -> Tuple[float, float]:
     fro = float(np.linalg.norm(d) / max(np.linalg.norm(Rl), 1e-300))
     mx = float(np.abs(d).max() / max(np.abs(Rl).max(), 1e-300))
     return fro, mx
+
+
+def stripped_v2(L, a, A, B, blocks, lmaxs, max_lmax, sqrt_u_norms):
+    """``create_HS2_stripped_v2`` (h_and_s_stripped_v2.cpp:100-382) call by call for general
+    per-atom T block sizes, including its row compaction of X, B and A (``X_height`` at
+    :211-230, ``X_nhpd_height`` at :319-347).  A, B: (L*a, G) Fortran-ordered; blocks: per
+    atom (aa, ab, bb) square complex arrays; sqrt_u_norms: (a, max_lmax+1).  Returns lower
+    triangles (H, S)."""
+    from scipy.linalg import blas
+    A = np.array(A, order="F", copy=True)
+    B = np.array(B, order="F", copy=True)
+    La, G = A.shape
+    S = blas.zherk(1.0, A, trans=2, lower=1)
+    lin = np.zeros(La)
+    for at in range(a):
+        for l in range(int(lmaxs[at]) + 1):
+            lin[at * L + l * l: at * L + (l + 1) ** 2] = sqrt_u_norms[at][l]
+    W = np.asfortranarray(B * lin[:, None])
+    S = blas.zherk(1.0, W, beta=1.0, c=S, trans=2, lower=1, overwrite_c=1)
+    X = np.zeros((La, G), np.complex128, order="F")
+    xh = 0
+    for at in range(a):
+        aa, ab, bb = blocks[at]
+        nbb, nab = bb.shape[0], ab.shape[0]
+        tmp = np.zeros((L, G), np.complex128, order="F")
+        if nbb:
+            tmp[:nbb] = blas.zhemm(0.5, np.asfortranarray(bb), np.asfortranarray(B[at * L: at * L + nbb]),
+                                   side=0, lower=1)
+        if nab:
+            tmp[:nab] += blas.zgemm(1.0, np.asfortranarray(ab), np.asfortranarray(A[at * L: at * L + nab]),
+                                    trans_a=2)
+        n = max(nab, nbb)
+        X[xh: xh + n] = tmp[:n]
+        if xh != at * L:
+            B[xh: xh + n] = B[at * L: at * L + n].copy()
+        xh += n
+    H = blas.zher2k(1.0, B[:xh], X[:xh], trans=2, lower=1) if xh else np.zeros((G, G), np.complex128)
+    xn = 0
+    X2 = np.zeros((La, G), np.complex128, order="F")
+    for at in range(a):
+        aa = blocks[at][0]
+        n = aa.shape[0]
+        if xn != at * L:
+            A[xn: xn + n] = A[at * L: at * L + n].copy()
+        if n:
+            X2[xn: xn + n] = blas.zhemm(1.0, np.asfortranarray(aa), np.asfortranarray(A[xn: xn + n]), side=0, lower=1)
+        xn += n
+    if xn:
+        H = H + np.tril(blas.zgemm(1.0, A[:xn], X2[:xn], trans_a=2))
+    return np.tril(H), np.tril(S)
