@@ -62,6 +62,9 @@ def lib():
         L.oracle_construct_ab.restype = ctypes.c_int
         L.oracle_prepare_tmat.argtypes = [ctypes.c_int, ctypes.c_int, dp, dp, dp, dp, dp, dp, dp, dp, dp]
         L.oracle_prepare_tmat.restype = ctypes.c_int
+        L.oracle_radfun.argtypes = [ctypes.c_int, ctypes.c_double, dp, ctypes.c_int, ctypes.c_double,
+                                    ctypes.c_double, dp]
+        L.oracle_radfun.restype = ctypes.c_int
         L.oracle_hs_naive.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int64, dp, dp,
                                       dp, dp, dp, dp, dp, dp, ctypes.c_int]
         _lib = L
@@ -296,3 +299,69 @@ def stripped_v2(L, a, A, B, blocks, lmaxs, max_lmax, sqrt_u_norms):
     if xn:
         H = H + np.tril(blas.zgemm(1.0, A[:xn], X2[:xn], trans_a=2))
     return np.tril(H), np.tril(S)
+
+
+# --------------------------------------------------------------- Fleur-dump golden
+def radfun(l: int, e: float, vr: np.ndarray, rmt: float, dx: float) -> np.ndarray:
+    """(u, u', udot, udot', ||udot||^2) at R_MT from Fleur's scalar-relativistic radial
+    solver (``radfun.f``/``radsra.f``/``radsrd.F``/``intgr.F``, restated in oracle.cpp)."""
+    vr = np.ascontiguousarray(vr, np.float64)
+    out = np.zeros(5)
+    rc = lib().oracle_radfun(int(l), float(e), _dp(vr), vr.size, float(rmt), float(dx), _dp(out))
+    if rc:
+        raise ValueError("radfun: bad mesh")
+    return out
+
+
+GOLDEN_FLEUR = os.path.join(os.path.dirname(_HERE), "tests", "golden", "fleur_two_atoms.npz")
+
+
+def _unpack_lower(v: np.ndarray, n: int) -> np.ndarray:
+    M = np.zeros((n, n), v.dtype)
+    M[np.tril_indices(n)] = v
+    return M
+
+
+def fleur_golden(path: str = GOLDEN_FLEUR):
+    """The two-atom Fleur dump as (System, KPoint, H_fleur, S_fleur).
+
+    Follows ``FleurData::populate_atomdata`` (``flapw_opt/src/FleurData.cpp:41-72``): per-type
+    meshes, potentials, cutoffs and energies; rotations ``mrot * rec_basis`` (``:446-456``);
+    the cell volume ``det(real_basis)`` (``:46``); matching values from the radial solver
+    per (type, l <= lmax) (``AtomData.cpp:73-88``); raw T matrices with the T_AB assembly of
+    ``types_helper.cpp:41-61`` (lower T_AB, upper from T_BA^H).  H_fleur and S_fleur are
+    Fleur's packed lower triangles unpacked row by row (``tests/flapw_verify.py:68-82``)
+    into the lower triangle of a G x G matrix (upper zero).
+    """
+    from hybridhsdla_gb300 import synth
+    d = np.load(path)
+    nt = d["lmax"].size
+    nl = int(d["lmax"].max()) + 1
+    L = nl * nl
+    u = np.zeros((nt, nl, 5))
+    for t in range(nt):
+        vr = d["potential"][t][:int(d["mesh_num"][t])]
+        for l in range(int(d["lmax"][t]) + 1):
+            u[t, l] = radfun(l, d["energies"][t][l], vr, d["mesh_rmt"][t], d["mesh_dx"][t])
+    taa = np.zeros((nt, L, L), np.complex128)
+    tbb = np.zeros((nt, L, L), np.complex128)
+    tab = np.zeros((nt, L, L), np.complex128)
+    for t in range(nt):
+        taa[t] = _unpack_lower(d["t%d_aa_lower" % t], L)
+        tbb[t] = _unpack_lower(d["t%d_bb_lower" % t], L)
+        lo = _unpack_lower(d["t%d_ab_lower" % t], L)
+        ba = _unpack_lower(d["t%d_ba_lower" % t], L)
+        tab[t] = lo + np.triu(ba.conj().T, 1)
+    bmat = d["rec_basis"]
+    rot = np.einsum("aij,jk->aik", d["atom_mrot"].astype(np.float64), bmat)
+    s = synth.System(real_basis=d["real_basis"], bmat=bmat, vol_cell=float(np.linalg.det(d["real_basis"])),
+                     atom_type=d["atom_type"].astype(np.int32), atom_pos=d["atom_pos"],
+                     atom_rotmat=rot, type_rmt=d["mesh_rmt"].copy(), type_lmax=d["lmax"].astype(np.int32),
+                     type_lmax_nonsph=d["lmax_nonsph"].astype(np.int32),
+                     u=u[:, :, 0].copy(), u_dr=u[:, :, 1].copy(), dE_u=u[:, :, 2].copy(),
+                     dE_u_dr=u[:, :, 3].copy(), dE_u_norm=u[:, :, 4].copy(),
+                     energies=d["energies"][:, :nl].copy(), taa_raw=taa, tbb_raw=tbb, tab_raw=tab,
+                     kpoints=[synth.KPoint(k=d["k_point"].copy(), g=d["g_mesh"].astype(np.int32))],
+                     name="fleur_two_atoms")
+    ng = d["g_mesh"].shape[0]
+    return s, s.kpoints[0], _unpack_lower(d["H_packed"], ng), _unpack_lower(d["S_packed"], ng)

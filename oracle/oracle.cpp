@@ -14,6 +14,11 @@
 //   TMat / zero_nonsph / augment_tmats
 //               flapw_opt/src/types_helper.cpp:41-90, flapw_opt/src/AtomData.cpp:95-145
 //   naive S, H  flapw_opt/src/h_and_s.cpp:88-162
+//   radfun      flapw_opt/external/compat/fleur/radfun.f:3-58, radsra.f:10-139,
+//               radsrd.F:31-169, intgr.F:68-126 (intgr0), constants.f:15-25;
+//               the call convention of flapw_opt/external/compat/libflerp.f90:50-90
+//               (r0 = R_MT exp(dx (1 - n))).  Only the Fleur-dump golden test uses it:
+//               the GPU library takes the boundary values as inputs.
 //
 // The reference's Fortran is compiled with -fdefault-real-8 / -r8, so every
 // REAL is a double and every COMPLEX a double complex; these restatements use
@@ -315,6 +320,192 @@ void oracle_hs_naive(int L, int num_atoms, int max_lmax, int64_t n_g, const doub
             H[G + n_g * Gp] = h;
         }
     }
+}
+
+// ---------------------------------------------------------------- radial solver
+// intgr0 (intgr.F:68-126): definite integral of y on the logarithmic mesh r_i = r0 e^{h(i-1)},
+// a power-law start on [0, r0], 7-point Lagrange steps up to the point n0 where the
+// Simpson-type 7-point rule (weights 41,216,27,272,27,216,41 / 140) takes over.
+static double intgr0(const double *y, double r0, double h, int jri) {
+    static const double lag[5][7] = {
+        {19087., 65112., -46461., 37504., -20211., 6312., -863.},
+        {-863., 25128., 46989., -16256., 7299., -2088., 271.},
+        {271., -2760., 30819., 37504., -6771., 1608., -191.},
+        {-191., 1608., -6771., 37504., 30819., -2760., 271.},
+        {271., -2088., 7299., -16256., 46989., 25128., -863.}};
+    static const double w7[7] = {41., 216., 27., 272., 27., 216., 41.};
+    double z = 0.0;
+    if (y[0] * y[1] > 0.0) {
+        const double alpha = 1.0 + std::log(y[1] / y[0]) / h;
+        if (alpha > 0.0) z = r0 * y[0] / alpha;
+    }
+    const int nsteps = (jri - 1) / 6;
+    int n0 = jri - 6 * nsteps;           // 1-based start of the 7-point rule
+    const double dr = std::exp(h);
+    double r[7];
+    r[0] = r0;
+    for (int i = 1; i < 7; ++i) r[i] = dr * r[i - 1];
+    if (n0 > 1) {
+        double yr[7];
+        for (int i = 0; i < 7; ++i) yr[i] = r[i] * y[i];
+        for (int j = 0; j < n0 - 1; ++j) {
+            double d = 0.0;
+            for (int i = 0; i < 7; ++i) d += lag[j][i] * yr[i];
+            z += h * d / 60480.;
+        }
+    }
+    r[0] = r[n0 - 1];
+    for (int m = 0; m < nsteps; ++m) {
+        for (int i = 1; i < 7; ++i) r[i] = dr * r[i - 1];
+        double d = 0.0;
+        for (int i = 0; i < 7; ++i) d += (h * w7[i] * r[i] / 140.) * y[n0 - 1 + i];
+        z += d;
+        n0 += 6;
+        r[0] = r[6];
+    }
+    return z;
+}
+
+// Scalar-relativistic outward integration of (p, q) = (r u, c^-1 r u_small) at energy e
+// (radsra.f:10-139) and of its energy derivative (pe, qe) (radsrd.F:31-169, with the
+// relativistic correction factor (1 + fl1/(c rm)^2) of the RELATIVISTIC_CORRECTIONS build):
+// 4th-order Runge-Kutta for the first five steps, then the 6-step Adams-Bashforth
+// predictor / Adams-Moulton corrector (at most five corrector sweeps, relative tolerance 1e-6).
+// vr = r V(r) on the n-point mesh ending at rmt.  out = {u(R), u'(R), udot(R), udot'(R),
+// <udot|udot>} (the rad_match fields u, u_dr, dE_u, dE_u_dr, dE_u_norm).
+int oracle_radfun(int l, double e, const double *vr, int n, double rmt, double h, double *out) {
+    if (n < 13 || !(h > 0.0) || !(rmt > 0.0)) return -1;
+    const double c = 137.0359895;          // constants.f:22, Hartree units
+    const double cin = 1.0 / c, cin2 = cin * cin;
+    const double r0 = rmt * std::exp(h * (1 - n));
+    const double fl1 = (double)l * (l + 1);
+    const double dr = std::exp(h), drh = std::sqrt(dr);
+    const double eps = 1e-6;
+    std::vector<double> p(n), q(n), pp(n), qp(n), pe(n), qe(n);
+    // ---- u at e
+    double s = std::sqrt(fl1 + 1 - cin2 * vr[0] * vr[0]) - 1.;
+    double rm = 2. * r0 + cin2 * (r0 * e - vr[0]);
+    p[0] = std::pow(r0, l + 1);
+    q[0] = s * p[0] / rm;
+    pp[0] = rm * q[0] + p[0];
+    qp[0] = (fl1 / rm + vr[0] - r0 * e) * p[0] - q[0];
+    double r = r0;
+    for (int i = 0; i < 5; ++i) {
+        const double rh2 = drh * r, rh = dr * r;
+        const double sk1 = h * pp[i], sl1 = h * qp[i];
+        double rve = 0.5 * (vr[i] + vr[i + 1]) - rh2 * e;
+        rm = 2. * rh2 - cin2 * rve;
+        double yn = p[i] + 0.5 * sk1, zn = q[i] + 0.5 * sl1;
+        const double sk2 = h * (rm * zn + yn), sl2 = h * ((fl1 / rm + rve) * yn - zn);
+        yn = p[i] + 0.5 * sk2; zn = q[i] + 0.5 * sl2;
+        const double sk3 = h * (rm * zn + yn), sl3 = h * ((fl1 / rm + rve) * yn - zn);
+        rve = vr[i + 1] - rh * e;
+        rm = 2. * rh - cin2 * rve;
+        yn = p[i] + sk3; zn = q[i] + sl3;
+        const double sk4 = h * (rm * zn + yn), sl4 = h * ((fl1 / rm + rve) * yn - zn);
+        p[i + 1] = p[i] + (sk1 + 2. * sk2 + 2. * sk3 + sk4) / 6.;
+        q[i + 1] = q[i] + (sl1 + 2. * sl2 + 2. * sl3 + sl4) / 6.;
+        pp[i + 1] = rm * q[i + 1] + p[i + 1];
+        qp[i + 1] = (fl1 / rm + rve) * p[i + 1] - q[i + 1];
+        r = rh;
+    }
+    for (int i = 5; i < n - 1; ++i) {
+        r = r * dr;
+        double p0 = p[i] + h * (4277. * pp[i] - 7923. * pp[i - 1] + 9982. * pp[i - 2] - 7298. * pp[i - 3] +
+                                2877. * pp[i - 4] - 475. * pp[i - 5]) / 1440.;
+        double q0 = q[i] + h * (4277. * qp[i] - 7923. * qp[i - 1] + 9982. * qp[i - 2] - 7298. * qp[i - 3] +
+                                2877. * qp[i - 4] - 475. * qp[i - 5]) / 1440.;
+        const double rve = vr[i + 1] - r * e;
+        rm = 2. * r - cin2 * rve;
+        double p1p = rm * q0 + p0, q1p = (fl1 / rm + rve) * p0 - q0, p1 = p0, q1 = q0;
+        for (int it = 0; it < 5; ++it) {
+            p1 = p[i] + h * (475. * p1p + 1427. * pp[i] - 798. * pp[i - 1] + 482. * pp[i - 2] - 173. * pp[i - 3] +
+                             27. * pp[i - 4]) / 1440.;
+            q1 = q[i] + h * (475. * q1p + 1427. * qp[i] - 798. * qp[i - 1] + 482. * qp[i - 2] - 173. * qp[i - 3] +
+                             27. * qp[i - 4]) / 1440.;
+            p1p = rm * q1 + p1;
+            q1p = (fl1 / rm + rve) * p1 - q1;
+            const double erp = std::fabs(p1 - p0) / (std::fabs(p1) + std::fabs(h * p1p));
+            const double erq = std::fabs(q1 - q0) / (std::fabs(q1) + std::fabs(h * p1p));
+            if (erp < eps && erq < eps) break;
+            p0 = p1;
+            q0 = q1;
+        }
+        p[i + 1] = p1; q[i + 1] = q1; pp[i + 1] = p1p; qp[i + 1] = q1p;
+    }
+    for (int i = 0; i < n; ++i) q[i] = cin * q[i];
+    std::vector<double> y(n);
+    for (int i = 0; i < n; ++i) y[i] = p[i] * p[i] + q[i] * q[i];
+    double t = 1.0 / std::sqrt(intgr0(y.data(), r0, h, n));
+    const double us = t * p[n - 1] / r;
+    const double dus = t * (pp[n - 1] - p[n - 1]) / (r * r);
+    for (int i = 0; i < n; ++i) { p[i] *= t; q[i] *= t; }
+    // ---- udot at e (orthogonalised to u)
+    auto corr = [&](double rmv) { return 1. + cin2 * fl1 / (rmv * rmv); };
+    rm = 2. * r0 + cin2 * (r0 * e - vr[0]);
+    pe[0] = 0; qe[0] = 0;
+    pp[0] = r0 * cin * q[0];
+    qp[0] = -r0 * p[0] * corr(rm);
+    r = r0;
+    for (int i = 0; i < 5; ++i) {
+        const double rh2 = drh * r, rh = dr * r;
+        const double sk1 = h * pp[i], sl1 = h * qp[i];
+        double rve = 0.5 * (vr[i] + vr[i + 1]) - rh2 * e;
+        rm = 2. * rh2 - cin2 * rve;
+        double yn = pe[i] + 0.5 * sk1, zn = qe[i] + 0.5 * sl1;
+        const double t1 = 0.5 * rh2 * cin * (q[i] + q[i + 1]);
+        const double t2 = 0.5 * rh2 * (p[i] + p[i + 1]) * corr(rm);
+        const double sk2 = h * (rm * zn + yn + t1), sl2 = h * ((fl1 / rm + rve) * yn - zn - t2);
+        yn = pe[i] + 0.5 * sk2; zn = qe[i] + 0.5 * sl2;
+        const double sk3 = h * (rm * zn + yn + t1), sl3 = h * ((fl1 / rm + rve) * yn - zn - t2);
+        rve = vr[i + 1] - rh * e;
+        rm = 2. * rh - cin2 * rve;
+        yn = pe[i] + sk3; zn = qe[i] + sl3;
+        const double sk4 = h * (rm * zn + yn + rh * cin * q[i + 1]);
+        const double sl4 = h * ((fl1 / rm + rve) * yn - zn - rh * p[i + 1] * corr(rm));
+        pe[i + 1] = pe[i] + (sk1 + 2. * sk2 + 2. * sk3 + sk4) / 6.;
+        qe[i + 1] = qe[i] + (sl1 + 2. * sl2 + 2. * sl3 + sl4) / 6.;
+        pp[i + 1] = rm * qe[i + 1] + pe[i + 1] + rh * cin * q[i + 1];
+        qp[i + 1] = (fl1 / rm + rve) * pe[i + 1] - qe[i + 1] - rh * p[i + 1] * corr(rm);
+        r = rh;
+    }
+    for (int i = 5; i < n - 1; ++i) {
+        r = r * dr;
+        double p0 = pe[i] + h * (4277. * pp[i] - 7923. * pp[i - 1] + 9982. * pp[i - 2] - 7298. * pp[i - 3] +
+                                 2877. * pp[i - 4] - 475. * pp[i - 5]) / 1440.;
+        double q0 = qe[i] + h * (4277. * qp[i] - 7923. * qp[i - 1] + 9982. * qp[i - 2] - 7298. * qp[i - 3] +
+                                 2877. * qp[i - 4] - 475. * qp[i - 5]) / 1440.;
+        const double rve = vr[i + 1] - r * e;
+        rm = 2. * r - cin2 * rve;
+        const double t1 = cin * r * q[i + 1];
+        const double t2 = r * p[i + 1] * corr(rm);
+        double p1p = rm * q0 + p0 + t1, q1p = (fl1 / rm + rve) * p0 - q0 - t2, p1 = p0, q1 = q0;
+        for (int it = 0; it < 5; ++it) {
+            p1 = pe[i] + h * (475. * p1p + 1427. * pp[i] - 798. * pp[i - 1] + 482. * pp[i - 2] - 173. * pp[i - 3] +
+                              27. * pp[i - 4]) / 1440.;
+            q1 = qe[i] + h * (475. * q1p + 1427. * qp[i] - 798. * qp[i - 1] + 482. * qp[i - 2] - 173. * qp[i - 3] +
+                              27. * qp[i - 4]) / 1440.;
+            p1p = rm * q1 + p1 + t1;
+            q1p = (fl1 / rm + rve) * p1 - q1 - t2;
+            const double erp = std::fabs(p1 - p0) / (std::fabs(p1) + std::fabs(h * p1p));
+            const double erq = std::fabs(q1 - q0) / (std::fabs(q1) + std::fabs(h * p1p));
+            if (erp < eps && erq < eps) break;
+            p0 = p1;
+            q0 = q1;
+        }
+        pe[i + 1] = p1; qe[i + 1] = q1; pp[i + 1] = p1p; qp[i + 1] = q1p;
+    }
+    for (int i = 0; i < n; ++i) qe[i] = cin * qe[i];
+    for (int i = 0; i < n; ++i) y[i] = p[i] * pe[i] + q[i] * qe[i];
+    t = intgr0(y.data(), r0, h, n);
+    double dud = (pp[n - 1] - pe[n - 1]) / (r * r);
+    for (int i = 0; i < n; ++i) { pe[i] -= t * p[i]; qe[i] -= t * q[i]; }
+    const double ud = pe[n - 1] / r;
+    dud = dud - t * dus;
+    for (int i = 0; i < n; ++i) y[i] = pe[i] * pe[i] + qe[i] * qe[i];
+    const double ddn = intgr0(y.data(), r0, h, n);
+    out[0] = us; out[1] = dus; out[2] = ud; out[3] = dud; out[4] = ddn;
+    return 0;
 }
 
 }  // extern "C"
