@@ -14,12 +14,16 @@ leg import this package; the GPU library never does.
   ``zhemm`` loop (``:321-349``) and, in place of MKL's ``zgemmt``, a ``zgemm``
   whose lower triangle is kept (``:362``).
 
-Parity status: the reference cannot be built here (Fortran, HDF5, Armadillo and
-MKL are absent) and its own tests pin no numeric value on this path, so this
-oracle is pinned by closed forms (spherical Bessel functions, spherical
-harmonics from scipy) and by the agreement of the BLAS sequence with the naive
-formulas -- not by outputs of the reference itself ("parity unpinned" against
-the reference binary).
+Parity status: PINNED against the reference's own known-answer data.  The reference's
+only golden vector for this path is Fleur's muffin-tin H and S for the two-atom sample
+(``flapw_opt/tests/sample_input/two_atoms/fleur_dump.h5``; extracted into
+``tests/golden/fleur_two_atoms.npz`` by ``tests/golden/make_fleur_golden.py``).
+``fleur_golden`` below rebuilds the reference's inputs from that dump (radial solver
+``oracle_radfun``, T assembly, rotations) and the oracle reproduces Fleur's H and S to
+about 3e-15 relative Frobenius (``tests/test_fleur_golden.py``).  The reference binary itself
+cannot be built here (Fortran, HDF5, Armadillo and MKL are absent), so there is no
+``_ref`` build; the closed-form checks of the special functions and the agreement of the
+BLAS sequence with the naive formulas are pinned as well.
 """
 from __future__ import annotations
 
