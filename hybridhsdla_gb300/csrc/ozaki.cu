@@ -27,7 +27,7 @@
 // re + 128 im) FP32 accumulators), warp-specialised: one TMA producer warp
 // (SW128 K-major 128x128-byte boxes, 64 KB per stage, 3 stages), one MMA warp
 // (single elected issuer, tcgen05.commit to release stages and publish
-// accumulators), four epilogue warps (tcgen05.ld 32x32b, FP64 recombination,
+// accumulators), eight epilogue warps (tcgen05.ld 32x32b, FP64 recombination,
 // coalesced read-modify-write of the L2-resident output tile).  Every mbarrier
 // wait is bounded by a clock64 budget; on expiry the kernel records an error
 // word, stops issuing work, waits (bounded) for its in-flight copies and MMAs,
@@ -54,11 +54,13 @@ constexpr int kTileN = 128;          // output complex columns per tile
 constexpr int kKBlock = 128;         // contraction bytes (e4m3 values) per stage
 constexpr int kStages = 3;
 constexpr int kStageBytes = 4 * kTileM * kKBlock;   // Ar, Ai, Br, Bi boxes
-constexpr int kThreads = 192;        // warp 0 TMA, warp 1 MMA, warps 2..5 epilogue
+constexpr int kThreads = 320;        // warp 0 TMA, warp 1 MMA, warps 2..9 epilogue
+constexpr int kEpiWarps = 8;         // two per TMEM lane quadrant, each drains half the columns
 constexpr long long kWaitCycles = 2000000000LL;    // ~1 s at 2 GHz
 constexpr int kExactTerms = 1 << 24;                // FP32 exact-integer bound
 constexpr int kSyncEvery = 64;                      // stages per lockstep epoch (cooperative launches)
 constexpr int kRetired = 0x7F7F7F7F;                // progress value of a CTA that has no work left
+constexpr int kErrWords = 8;                        // error word + diagnostics of the first expired wait
 
 struct OzJob {
     int32_t lmap, rmap;        // tensor-map index (0..3) of the left / right digit operand
@@ -215,13 +217,13 @@ __host__ __device__ __forceinline__ int64_t chunk_kblocks(int pairs) {
     return c < 1 ? 1 : c;
 }
 
-// Loose grid-wide lockstep for cooperative launches: every CTA publishes its stage epoch, and a
-// producer may run at most one epoch ahead of the slowest CTA.  All persistent CTAs walk
+// Loose grid-wide lockstep for cooperative launches: every producer publishes its stage epoch in
+// its slot (one per CTA, or per CTA pair), and may run at most one epoch ahead of the slowest.  All persistent CTAs walk
 // identical stage sequences, so staying within an epoch keeps the operand panels they share
 // resident in L2 (left to themselves, CTAs drift apart by far more than L2 can hold).
 // Bounded: on expiry the CTA raises the abort flag and records the error word.
-__device__ bool grid_lockstep(int *progress, int n, int epoch, volatile int *abort_flag, int *err) {
-    atomicExch(progress + blockIdx.x, epoch);
+__device__ bool grid_lockstep(int *progress, int n, int epoch, volatile int *abort_flag, int *err, int slot) {
+    atomicExch(progress + slot, epoch);
     const long long t0 = clock64();
     while (true) {
         int mn = kRetired;
@@ -235,6 +237,38 @@ __device__ bool grid_lockstep(int *progress, int n, int epoch, volatile int *abo
             *abort_flag = 1;
             atomicCAS(err, 0, kDevTimeout * 16 + 5);
             return false;
+        }
+    }
+}
+
+// Drain 32 accumulator columns of one output row: out += w (re, im) (plain store on the first unit
+// of a tile), times 2^(e_row + e_col) on the last.  Loads are grouped 16 at a time ahead of the
+// stores (the compiler cannot reorder a load past a store to a possibly aliasing column), so a
+// drain costs a few L2 round trips per 32 columns instead of one per column.
+constexpr int kDrainBatch = 8;
+__device__ __forceinline__ void drain32(const OzJob &j, int64_t row, int64_t col0, const uint32_t (&vre)[32],
+                                        const uint32_t (&vim)[32], double wt, bool first, bool last, int erow) {
+#pragma unroll
+    for (int h = 0; h < 32; h += kDrainBatch) {
+        double2 o[kDrainBatch];
+#pragma unroll
+        for (int cc = 0; cc < kDrainBatch; ++cc) {
+            const int64_t col = col0 + h + cc;
+            const bool live = col < j.n && !(j.lower && row < col);
+            o[cc] = (live && !first) ? __ldcg(j.out + row + j.ldo * col) : make_double2(0.0, 0.0);
+        }
+#pragma unroll
+        for (int cc = 0; cc < kDrainBatch; ++cc) {
+            const int64_t col = col0 + h + cc;
+            if (col >= j.n || (j.lower && row < col)) continue;
+            double re = (double)__uint_as_float(vre[h + cc]) * wt + o[cc].x;
+            double im = (double)__uint_as_float(vim[h + cc]) * wt + o[cc].y;
+            if (last) {
+                const double sc = ldexp(1.0, erow + j.er[col]);
+                re *= sc;
+                im *= sc;
+            }
+            j.out[row + j.ldo * col] = make_double2(re, im);
         }
     }
 }
@@ -266,7 +300,7 @@ __global__ void __launch_bounds__(kThreads, 1)
 
     if (threadIdx.x == 0) {
         for (int i = 0; i < kStages; ++i) { mbar_init(&bars.full[i], 1); mbar_init(&bars.empty[i], 1); }
-        for (int i = 0; i < 2; ++i) { mbar_init(&bars.tfull[i], 1); mbar_init(&bars.tempty[i], 128); }
+        for (int i = 0; i < 2; ++i) { mbar_init(&bars.tfull[i], 1); mbar_init(&bars.tempty[i], 32 * kEpiWarps); }
         abort_flag = 0;
         asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
         for (int i = 0; i < 4; ++i) asm volatile("prefetch.tensormap [%0];\n" ::"l"((uint64_t)map_of(i)) : "memory");
@@ -302,7 +336,7 @@ __global__ void __launch_bounds__(kThreads, 1)
                                 const int jj = t - i;
                                 if (progress && issued > 0 && issued % kSyncEvery == 0 &&
                                     !grid_lockstep(progress, (int)gridDim.x, (int)(issued / kSyncEvery), &abort_flag,
-                                                   err)) { ok = false; break; }
+                                                   err, (int)blockIdx.x)) { ok = false; break; }
                                 if (!mbar_wait(&bars.empty[stage], phase ^ 1, &abort_flag, err, 1)) { ok = false; break; }
                                 unsigned char *st = smem + stage * kStageBytes;
                                 mbar_expect_tx(&bars.full[stage], kStageBytes);
@@ -392,8 +426,9 @@ __global__ void __launch_bounds__(kThreads, 1)
             }
         }
     } else {
-        // ------------------------------------------------------------ epilogue (warps 2..5)
+        // ------------------------------------------------------------ epilogue (warps 2..9)
         const int q = warp & 3;                      // TMEM lane quadrant of this warp
+        const int cbeg = ((warp - 2) >> 2) * (kTileN / 2);   // its half of the columns
         const int r_in_tile = q * 32 + lane;
         int64_t unit = 0;
         bool ok = true;
@@ -416,35 +451,16 @@ __global__ void __launch_bounds__(kThreads, 1)
                     tc_fence_after();
                     const uint32_t tbase = tmem_base + ((uint32_t)(q * 32) << 16) + buf * 256;
 #pragma unroll 1
-                    for (int c0 = 0; c0 < kTileN; c0 += 32) {
+                    for (int c0 = cbeg; c0 < cbeg + kTileN / 2; c0 += 32) {
                         uint32_t vre[32], vim[32];
                         tmem_ld32(tbase + c0, vre);
                         tmem_ld32(tbase + 128 + c0, vim);
                         tmem_ld_wait();
-                        if (c0 + 32 >= kTileN) {
+                        if (c0 + 32 >= cbeg + kTileN / 2) {
                             tc_fence_before();
                             mbar_arrive(&bars.tempty[buf]);
                         }
-                        if (!row_ok) continue;
-#pragma unroll
-                        for (int cc = 0; cc < 32; ++cc) {
-                            const int64_t col = tn * kTileN + c0 + cc;
-                            if (col >= j.n || (j.lower && row < col)) continue;
-                            double2 *p = j.out + row + j.ldo * col;
-                            double re = (double)__uint_as_float(vre[cc]) * wt;
-                            double im = (double)__uint_as_float(vim[cc]) * wt;
-                            if (!first) {
-                                const double2 o = *p;
-                                re += o.x;
-                                im += o.y;
-                            }
-                            if (last) {
-                                const double sc = ldexp(1.0, erow + j.er[col]);
-                                re *= sc;
-                                im *= sc;
-                            }
-                            *p = make_double2(re, im);
-                        }
+                        if (row_ok) drain32(j, row, tn * kTileN + c0, vre, vim, wt, first, last, erow);
                     }
                     ++unit;
                 }
@@ -456,6 +472,294 @@ __global__ void __launch_bounds__(kThreads, 1)
     if (warp == 1) {
         tc_fence_after();
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;\n" ::"r"(tmem_base) : "memory");
+    }
+}
+
+// ------------------------------------------------------- CTA-pair products
+// The S/H launch on 2-CTA tiles: a cluster of two CTAs (one per SM) computes a 256 x 256
+// output tile with tcgen05.mma.cta_group::2 (M = 256, N = 256).  Each CTA stages its own half
+// of the left operand (128 rows) and its own half of the right operand (128 rows) per k-block,
+// so an MMA of twice the 1-CTA tile's flops reads the same 8 KB of shared memory per SM, and TMA
+// writes half the bytes per flop.  Each CTA's TMEM holds its 128 output rows x (256 re + 256 im)
+// FP32 columns (single-buffered: an exact-accumulation unit runs ~10^5 cycles, its drain a few
+// 10^3).  Roles:
+//   leader (cluster rank 0): TMA for its halves, expect_tx for both CTAs' bytes on its full
+//     barrier, the single MMA issuer, commits multicast to both CTAs' empty / tfull barriers;
+//   peer (rank 1): TMA for its halves completing on the leader's full barrier (.cta_group::2);
+//   both: eight epilogue warps drain their own TMEM rows and arrive on the leader's tempty.
+// Every wait is bounded as in oz_gemm_kernel; both CTAs meet at a cluster barrier before TMEM
+// is freed, so no CTA exits while its shared memory or TMEM can still be addressed by the other.
+constexpr int kPairTile = 256;
+constexpr int kPairSmemSlack = 32768;      // keeps every descriptor-addressed byte inside the allocation
+
+__device__ __forceinline__ uint32_t cluster_rank() {
+    uint32_t r;
+    asm volatile("mov.u32 %0, %%cluster_ctarank;\n" : "=r"(r));
+    return r;
+}
+__device__ __forceinline__ uint32_t cluster_size() {
+    uint32_t r;
+    asm volatile("mov.u32 %0, %%cluster_nctarank;\n" : "=r"(r));
+    return r;
+}
+__device__ __forceinline__ uint32_t mapa_rank(uint32_t saddr, uint32_t rank) {
+    uint32_t r;
+    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;\n" : "=r"(r) : "r"(saddr), "r"(rank));
+    return r;
+}
+__device__ __forceinline__ void cluster_sync_all() {
+    asm volatile("barrier.cluster.arrive.release.aligned;\nbarrier.cluster.wait.acquire.aligned;\n" ::: "memory");
+}
+__device__ __forceinline__ void mbar_arrive_remote(uint32_t cluster_addr) {
+    asm volatile("mbarrier.arrive.release.cluster.shared::cluster.b64 _, [%0];\n" ::"r"(cluster_addr) : "memory");
+}
+__device__ __forceinline__ void tma_load_2d_pair(void *dst, const CUtensorMap *map, uint32_t bar_cluster, int x,
+                                                 int y) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.cta_group::2.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4}], "
+        "[%2];\n" ::"r"(smem_u32(dst)),
+        "l"((uint64_t)map), "r"(bar_cluster), "r"(x), "r"(y)
+        : "memory");
+}
+__host__ __device__ constexpr uint32_t idesc_f8_pair(bool negA) {
+    return (1u << 4) | ((negA ? 1u : 0u) << 13) | ((uint32_t)(kPairTile >> 3) << 17) |
+           ((uint32_t)(kPairTile >> 4) << 24);
+}
+__device__ __forceinline__ void mma_f8_pair(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                            uint32_t accumulate) {
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::2.kind::f8f6f4 [%0], %1, %2, %3, p;\n}\n" ::"r"(
+            d_tmem),
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+        : "memory");
+}
+__device__ __forceinline__ void mma_commit_pair(uint64_t *bar) {
+    const uint16_t both = 3;
+    asm volatile(
+        "tcgen05.commit.cta_group::2.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64 [%0], %1;\n" ::"r"(
+            smem_u32(bar)),
+        "h"(both)
+        : "memory");
+}
+
+struct __align__(8) PairBarriers {
+    uint64_t full[kStages];      // leader: both CTAs' bytes of a stage landed
+    uint64_t empty[kStages];     // each CTA: the stage's MMAs completed (multicast commit)
+    uint64_t tfull;              // each CTA: the unit's accumulator is complete (multicast commit)
+    uint64_t tempty;             // leader: 16 epilogue warps (both CTAs) drained the accumulator
+};
+
+__global__ void __launch_bounds__(kThreads, 1)
+    oz_pair_kernel(const __grid_constant__ CUtensorMap map0, const __grid_constant__ CUtensorMap map1,
+                   const __grid_constant__ CUtensorMap map2, const __grid_constant__ CUtensorMap map3,
+                   const OzJob *__restrict__ jobs, int num_jobs, int64_t total_tiles, int s, int *err,
+                   const int4 *__restrict__ tile_list, int *progress) {
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    unsigned char *smem = reinterpret_cast<unsigned char *>(
+        (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    __shared__ PairBarriers bars;
+    __shared__ uint32_t tmem_base_sh;
+    __shared__ volatile int abort_flag;
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    // launched as clusters of two or not at all: nothing below (the pair TMEM allocation above
+    // all) is valid otherwise
+    if (cluster_size() != 2) {
+        if (threadIdx.x == 0) atomicCAS(err, 0, kDevBadInput * 16 + 6);
+        return;
+    }
+    const uint32_t rank = cluster_rank();
+    const bool leader = rank == 0;
+    // bounded wait that records where it expired (first failure wins)
+    auto pwait = [&](uint64_t *bar, uint32_t parity, int where, int stage_, int count) -> bool {
+        if (mbar_wait(bar, parity, &abort_flag, err, where)) return true;
+        if (atomicCAS(err + 7, 0, 1) == 0) {
+            err[1] = blockIdx.x; err[2] = (int)rank; err[3] = stage_; err[4] = (int)parity; err[5] = count;
+        }
+        return false;
+    };
+    const int64_t pair = blockIdx.x >> 1, npairs = gridDim.x >> 1;
+    auto map_of = [&](int i) -> const CUtensorMap * {
+        return i == 0 ? &map0 : i == 1 ? &map1 : i == 2 ? &map2 : &map3;
+    };
+
+    if (threadIdx.x == 0) {
+        for (int i = 0; i < kStages; ++i) { mbar_init(&bars.full[i], 1); mbar_init(&bars.empty[i], 1); }
+        mbar_init(&bars.tfull, 1);
+        mbar_init(&bars.tempty, 2 * kEpiWarps);
+        abort_flag = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+        for (int i = 0; i < 4; ++i) asm volatile("prefetch.tensormap [%0];\n" ::"l"((uint64_t)map_of(i)) : "memory");
+    }
+    if (warp == 1) {
+        // collective over the pair: one warp of each CTA
+        asm volatile("tcgen05.alloc.cta_group::2.sync.aligned.shared::cta.b32 [%0], 512;\n" ::"r"(smem_u32(&tmem_base_sh))
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::2.sync.aligned;\n" ::: "memory");
+    }
+    tc_fence_before();
+    __syncthreads();
+    cluster_sync_all();          // barriers of both CTAs initialised before any remote arrival
+    tc_fence_after();
+    const uint32_t tmem_base = tmem_base_sh;
+    const uint32_t full0_leader = mapa_rank(smem_u32(&bars.full[0]), 0);
+    const uint32_t tempty_leader = mapa_rank(smem_u32(&bars.tempty), 0);
+    const int64_t half = (int64_t)rank * (kPairTile / 2);
+
+    if (warp == 0) {
+        // ------------------------------------------------------------ TMA producers (both CTAs)
+        if (lane == 0) {
+            int stage = 0;
+            uint32_t phase = 0;
+            int64_t issued = 0;
+            bool ok = true;
+            for (int64_t tile = pair; ok && tile < total_tiles; tile += npairs) {
+                int64_t tm, tn;
+                const OzJob &j = resolve_tile(jobs, num_jobs, tile_list, tile, tm, tn);
+                const CUtensorMap *lm = map_of(j.lmap), *rm = map_of(j.rmap);
+                for (int t = 2; ok && t <= s + 1; ++t) {
+                    const int ilo = max(1, t - s), ihi = min(s, t - 1);
+                    const int64_t ck = chunk_kblocks(ihi - ilo + 1);
+                    for (int64_t cb = 0; ok && cb < j.nkb; cb += ck) {
+                        const int64_t ce = min(j.nkb, cb + ck);
+                        for (int64_t kb = cb; ok && kb < ce; ++kb) {
+                            for (int i = ilo; i <= ihi; ++i) {
+                                const int jj = t - i;
+                                if (leader && progress && issued > 0 && issued % kSyncEvery == 0 &&
+                                    !grid_lockstep(progress, (int)npairs, (int)(issued / kSyncEvery), &abort_flag,
+                                                   err, (int)pair)) { ok = false; break; }
+                                if (!pwait(&bars.empty[stage], phase ^ 1, 1, stage, (int)issued)) { ok = false; break; }
+                                unsigned char *st = smem + stage * kStageBytes;
+                                if (leader) mbar_expect_tx(&bars.full[stage], 2 * kStageBytes);
+                                const uint32_t fb = full0_leader + stage * 8;
+                                const int xl = (int)(j.lk0 + kb * kKBlock), xr = (int)(j.rk0 + kb * kKBlock);
+                                const int64_t yl = j.lrow0 + tm * kPairTile + half, yr = j.rrow0 + tn * kPairTile + half;
+                                tma_load_2d_pair(st, lm, fb, xl, (int)((2 * (i - 1)) * j.lplane + yl));
+                                tma_load_2d_pair(st + 16384, lm, fb, xl, (int)((2 * (i - 1) + 1) * j.lplane + yl));
+                                tma_load_2d_pair(st + 32768, rm, fb, xr, (int)((2 * (jj - 1)) * j.rplane + yr));
+                                tma_load_2d_pair(st + 49152, rm, fb, xr, (int)((2 * (jj - 1) + 1) * j.rplane + yr));
+                                ++issued;
+                                if (++stage == kStages) { stage = 0; phase ^= 1; }
+                            }
+                        }
+                    }
+                }
+            }
+            if (leader && progress) atomicExch(progress + pair, kRetired);
+            // Before exit every stage this CTA issued must have been consumed: its bytes landed and
+            // the MMA commit that frees it (multicast, possibly remote) arrived.  Normally these
+            // waits return at once; after an abort they are bounded.
+            for (int q = 0; q < kStages && issued > 0; ++q) {
+                if (--stage < 0) { stage = kStages - 1; phase ^= 1; }
+                mbar_drain_wait(&bars.empty[stage], phase);
+                --issued;
+            }
+        }
+    } else if (warp == 1) {
+        // ------------------------------------------------------------ MMA issuer (leader only)
+        if (lane == 0 && leader) {
+            int stage = 0;
+            uint32_t phase = 0;
+            int64_t unit = 0;
+            bool ok = true;
+            const uint32_t id_pos = idesc_f8_pair(false), id_neg = idesc_f8_pair(true);
+            const uint32_t sbase = smem_u32(smem);
+            const uint32_t d_re = tmem_base, d_im = tmem_base + kPairTile;
+            for (int64_t tile = pair; ok && tile < total_tiles; tile += npairs) {
+                int64_t tm_, tn_;
+                const OzJob &j = resolve_tile(jobs, num_jobs, tile_list, tile, tm_, tn_);
+                for (int t = 2; ok && t <= s + 1; ++t) {
+                    const int ilo = max(1, t - s), ihi = min(s, t - 1);
+                    const int64_t ck = chunk_kblocks(ihi - ilo + 1);
+                    for (int64_t cb = 0; ok && cb < j.nkb; cb += ck) {
+                        const int64_t ce = min(j.nkb, cb + ck);
+                        if (!pwait(&bars.tempty, (uint32_t)((unit & 1) ^ 1), 2, stage, (int)unit)) { ok = false; break; }
+                        tc_fence_after();
+                        bool first = true;
+                        for (int64_t kb = cb; ok && kb < ce; ++kb) {
+                            for (int i = ilo; i <= ihi; ++i) {
+                                if (!pwait(&bars.full[stage], phase, 3, stage, (int)unit)) { ok = false; break; }
+                                tc_fence_after();
+                                const uint32_t a_re = sbase + stage * kStageBytes, a_im = a_re + 16384;
+                                const uint32_t b_re = a_re + 32768, b_im = a_re + 49152;
+#pragma unroll
+                                for (int kk = 0; kk < kKBlock / 32; ++kk) {
+                                    const uint32_t off = kk * 32;
+                                    const uint32_t acc = first ? 0u : 1u;
+                                    mma_f8_pair(d_re, sw128_desc(a_re + off), sw128_desc(b_re + off), id_pos, acc);
+                                    mma_f8_pair(d_re, sw128_desc(a_im + off), sw128_desc(b_im + off), id_pos, 1u);
+                                    mma_f8_pair(d_im, sw128_desc(a_re + off), sw128_desc(b_im + off), id_pos, acc);
+                                    mma_f8_pair(d_im, sw128_desc(a_im + off), sw128_desc(b_re + off), id_neg, 1u);
+                                    first = false;
+                                }
+                                mma_commit_pair(&bars.empty[stage]);
+                                if (++stage == kStages) { stage = 0; phase ^= 1; }
+                            }
+                        }
+                        if (!ok) break;
+                        mma_commit_pair(&bars.tfull);
+                        ++unit;
+                    }
+                }
+            }
+            if (!ok) {
+                // a partially issued unit may still be running: commit it and wait (bounded)
+                mma_commit_pair(&bars.tfull);
+                mbar_drain_wait(&bars.tfull, (uint32_t)(unit & 1));
+            } else if (unit > 0) {
+                // the last unit's MMAs and both CTAs' drains of it
+                mbar_drain_wait(&bars.tfull, (uint32_t)((unit - 1) & 1));
+                mbar_drain_wait(&bars.tempty, (uint32_t)((unit - 1) & 1));
+            }
+        }
+    } else {
+        // ------------------------------------------------------------ epilogue (warps 2..9, both CTAs)
+        const int q = warp & 3;                      // TMEM lane quadrant of this warp
+        const int cbeg = ((warp - 2) >> 2) * (kPairTile / 2);   // its half of the columns
+        const int r_in_tile = (int)half + q * 32 + lane;
+        int64_t unit = 0;
+        bool ok = true;
+        for (int64_t tile = pair; ok && tile < total_tiles; tile += npairs) {
+            int64_t tm, tn;
+            const OzJob &j = resolve_tile(jobs, num_jobs, tile_list, tile, tm, tn);
+            const int64_t row = tm * kPairTile + r_in_tile;
+            const bool row_ok = row < j.m;
+            const int erow = row_ok ? j.el[row] : 0;
+            for (int t = 2; ok && t <= s + 1; ++t) {
+                const int ilo = max(1, t - s), ihi = min(s, t - 1);
+                const int64_t ck = chunk_kblocks(ihi - ilo + 1);
+                const double wt = ldexp(1.0, 2 - 5 * t);
+                for (int64_t cb = 0; ok && cb < j.nkb; cb += ck) {
+                    const bool first = (t == 2 && cb == 0);
+                    const bool last = (t == s + 1 && cb + ck >= j.nkb);
+                    if (!pwait(&bars.tfull, (uint32_t)(unit & 1), 4, warp, (int)unit)) { ok = false; break; }
+                    tc_fence_after();
+                    const uint32_t tbase = tmem_base + ((uint32_t)(q * 32) << 16);
+#pragma unroll 1
+                    for (int c0 = cbeg; c0 < cbeg + kPairTile / 2; c0 += 32) {
+                        uint32_t vre[32], vim[32];
+                        tmem_ld32(tbase + c0, vre);
+                        tmem_ld32(tbase + kPairTile + c0, vim);
+                        tmem_ld_wait();
+                        if (c0 + 32 >= cbeg + kPairTile / 2) {
+                            tc_fence_before();
+                            __syncwarp();
+                            if (lane == 0) mbar_arrive_remote(tempty_leader);
+                        }
+                        if (row_ok) drain32(j, row, tn * kPairTile + c0, vre, vim, wt, first, last, erow);
+                    }
+                    ++unit;
+                }
+            }
+        }
+    }
+    tc_fence_before();
+    __syncwarp();
+    __syncthreads();
+    cluster_sync_all();          // neither CTA frees TMEM or exits while the other may address it
+    if (warp == 1) {
+        tc_fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::2.sync.aligned.b32 %0, 512;\n" ::"r"(tmem_base) : "memory");
     }
 }
 
@@ -688,9 +992,15 @@ cudaError_t slice(const double2 *Z, int64_t ldz, const double *v, int64_t Kin, i
     return slice_launch(slice_table(Z, ldz, v, Kin, ncols, rpb, bpad, s, d), st);
 }
 
-int64_t job_tiles(const OzJob &j) {
-    const int64_t tm = (j.m + kTileM - 1) / kTileM, tn = (j.n + kTileN - 1) / kTileN;
+int64_t job_tiles(const OzJob &j, int64_t tile = kTileM) {
+    const int64_t tm = (j.m + tile - 1) / tile, tn = (j.n + tile - 1) / tile;
     return j.lower ? tm * (tm + 1) / 2 : tm * tn;
+}
+
+// The S/H launch runs on CTA pairs (256 x 256 tiles) unless HSDLA_PAIR=0.
+bool use_pair() {
+    static const bool b = env_int("HSDLA_PAIR", 1) != 0;
+    return b;
 }
 
 // Host-built tile schedule.  Persistent CTAs take tiles g, g + grid, ... so tiles that are
@@ -702,16 +1012,16 @@ int64_t job_tiles(const OzJob &j) {
 // triangle).  With the CTAs in lockstep, 8 x 8 super-blocks cut the S/H launch of the
 // 8000-column FLAPW workload from 378 ms (row-major) to 355 ms: a wave then reads ~16 left and
 // ~16 right panels instead of ~2 left and ~120 right ones.
-int64_t super_block() {
-    static const int64_t b = [] {
-        const int64_t x = env_int("HSDLA_SCHED_SUPERBLOCK", 8);
-        return x <= 0 ? (int64_t)1 << 30 : x;
-    }();
-    return b;
+// On 256 x 256 pair tiles the default edge is 4 (the same panel span).
+int64_t super_block(int64_t tile) {
+    static const int64_t b = env_int("HSDLA_SCHED_SUPERBLOCK", 0);
+    if (b < 0) return (int64_t)1 << 30;
+    if (b > 0) return b;
+    return tile == kTileN ? 8 : 4;
 }
 
-void build_schedule(const std::vector<OzJob> &jobs, std::vector<int4> &list) {
-    const int64_t kSuperBlock = super_block();
+void build_schedule(const std::vector<OzJob> &jobs, std::vector<int4> &list, int64_t tile = kTileN) {
+    const int64_t kSuperBlock = super_block(tile);
     list.clear();
     std::vector<char> done(jobs.size(), 0);
     for (size_t a = 0; a < jobs.size(); ++a) {
@@ -721,7 +1031,7 @@ void build_schedule(const std::vector<OzJob> &jobs, std::vector<int4> &list) {
             std::vector<int> group;
             for (size_t b = a; b < jobs.size(); ++b)
                 if (!done[b] && jobs[b].lower && jobs[b].n == ja.n) { group.push_back((int)b); done[b] = 1; }
-            const int64_t T = (ja.n + kTileN - 1) / kTileN;
+            const int64_t T = (ja.n + tile - 1) / tile;
             for (int64_t I = 0; I < T; I += kSuperBlock)
                 for (int64_t J = 0; J <= I; J += kSuperBlock)
                     for (int64_t tm = I; tm < std::min(T, I + kSuperBlock); ++tm)
@@ -729,7 +1039,7 @@ void build_schedule(const std::vector<OzJob> &jobs, std::vector<int4> &list) {
                             for (int g : group) list.push_back(make_int4(g, (int)tm, (int)tn, 0));
         } else {
             done[a] = 1;
-            const int64_t tmn = (ja.m + kTileM - 1) / kTileM, tnn = (ja.n + kTileN - 1) / kTileN;
+            const int64_t tmn = (ja.m + tile - 1) / tile, tnn = (ja.n + tile - 1) / tile;
             for (int64_t tn = 0; tn < tnn; ++tn)
                 for (int64_t tm = 0; tm < tmn; ++tm) list.push_back(make_int4((int)a, (int)tm, (int)tn, 0));
         }
@@ -806,8 +1116,8 @@ int ozaki_plan_init(OzakiPlan &oz, int num_slices, double target) {
     oz.num_slices = num_slices;
     oz.target = target;
     if (!oz.d_error) {
-        if (cudaMalloc(&oz.d_error, sizeof(int)) != cudaSuccess) { g_oz_err = "cudaMalloc"; return HSDLA_ERR_NOMEM; }
-        cudaMemset(oz.d_error, 0, sizeof(int));
+        if (cudaMalloc(&oz.d_error, kErrWords * sizeof(int)) != cudaSuccess) { g_oz_err = "cudaMalloc"; return HSDLA_ERR_NOMEM; }
+        cudaMemset(oz.d_error, 0, kErrWords * sizeof(int));
     }
     return HSDLA_OK;
 }
@@ -819,14 +1129,17 @@ void ozaki_plan_release(OzakiPlan &oz) {
 
 int ozaki_check_device_error(OzakiPlan &oz) {
     if (!oz.d_error) return HSDLA_OK;
-    int h = 0;
-    if (cudaMemcpy(&h, oz.d_error, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess) return HSDLA_ERR_CUDA;
+    int w[kErrWords] = {};
+    if (cudaMemcpy(w, oz.d_error, sizeof(w), cudaMemcpyDeviceToHost) != cudaSuccess) return HSDLA_ERR_CUDA;
+    const int h = w[0];
     if (h != 0) {
-        static char buf[96];
-        snprintf(buf, sizeof(buf), "device wait expired (code %d, role %d)", h / 16, h % 16);
+        static char buf[192];
+        snprintf(buf, sizeof(buf),
+                 "device wait expired (code %d, role %d; block %d rank %d stage %d phase %d count %d)", h / 16,
+                 h % 16, w[1], w[2], w[3], w[4], w[5]);
         g_oz_err = buf;
-        cudaMemset(oz.d_error, 0, sizeof(int));
-        return HSDLA_ERR_TIMEOUT;
+        cudaMemset(oz.d_error, 0, sizeof(w));
+        return h / 16 == kDevBadInput ? HSDLA_ERR_CUDA : HSDLA_ERR_TIMEOUT;
     }
     return HSDLA_OK;
 }
@@ -891,6 +1204,7 @@ struct OzGroup {
     int64_t tiles_t = 0, tiles_sh = 0;
     int *d_progress = nullptr;
     int *d_err = nullptr;
+    bool pair = false;          // S/H on CTA-pair tiles
 };
 
 namespace {
@@ -901,15 +1215,15 @@ int64_t group_rows(const std::vector<int64_t> &G) {
     return r + kTileM;
 }
 
-int upload_schedule(std::vector<OzJob> &jobs, OzJob *d_jobs, int4 *d_list, int64_t &tiles) {
+int upload_schedule(std::vector<OzJob> &jobs, OzJob *d_jobs, int4 *d_list, int64_t &tiles, int64_t tile = kTileN) {
     int64_t total = 0;
     for (auto &j : jobs) {
-        j.tiles_n = (j.n + kTileN - 1) / kTileN;
+        j.tiles_n = (j.n + tile - 1) / tile;
         j.tile_begin = total;
-        total += job_tiles(j);
+        total += job_tiles(j, tile);
     }
     std::vector<int4> list;
-    build_schedule(jobs, list);
+    build_schedule(jobs, list, tile);
     if ((int64_t)list.size() != total) { g_oz_err = "tile schedule size mismatch"; return HSDLA_ERR_ARG; }
     cudaError_t e = cudaMemcpy(d_jobs, jobs.data(), sizeof(OzJob) * jobs.size(), cudaMemcpyHostToDevice);
     if (e == cudaSuccess && total > 0)
@@ -917,6 +1231,56 @@ int upload_schedule(std::vector<OzJob> &jobs, OzJob *d_jobs, int4 *d_list, int64
     if (e != cudaSuccess) { g_oz_err = cudaGetErrorString(e); return HSDLA_ERR_CUDA; }
     tiles = total;
     return HSDLA_OK;
+}
+
+// Launch of a prepared pair-tile job table: clusters of two CTAs, one per SM, as many pairs as
+// can be resident (at most one per tile); cooperative when the lockstep slots are given.
+cudaError_t launch_pair(const CUtensorMap *maps, int s, int *d_err, const OzJob *d_jobs, int n_jobs, int64_t total,
+                        const int4 *d_list, int *d_progress, cudaStream_t st) {
+    if (total <= 0) return cudaSuccess;
+    const size_t smem = (size_t)kStages * kStageBytes + kPairSmemSlack + 1024;
+    cudaError_t e = cudaFuncSetAttribute(oz_pair_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute at[2];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = 2;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.blockDim = dim3(kThreads);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    static int max_pairs = 0;
+    if (max_pairs == 0) {
+        cfg.gridDim = dim3(2);
+        int nc = 0;
+        e = cudaOccupancyMaxActiveClusters(&nc, (const void *)oz_pair_kernel, &cfg);
+        if (e != cudaSuccess) return e;
+        if (nc < 1) return cudaErrorInvalidConfiguration;
+        max_pairs = nc;
+    }
+    const int64_t pairs = std::min<int64_t>(total, max_pairs);
+    cfg.gridDim = dim3((unsigned)(2 * pairs));
+    const bool lockstep = d_progress && pairs > 1 && pairs <= kProgressCap && env_int("HSDLA_LOCKSTEP", 1) != 0;
+    if (lockstep) {
+        const int64_t g4 = (pairs + 3) / 4 * 4;
+        e = cudaMemsetAsync(d_progress, 0, sizeof(int) * pairs, st);
+        if (e == cudaSuccess && g4 > pairs) e = cudaMemsetAsync(d_progress + pairs, 0x7F, sizeof(int) * (g4 - pairs), st);
+        if (e != cudaSuccess) return e;
+        // cooperative: the launch waits until every pair can be resident (the lockstep needs
+        // that); HSDLA_COOPERATIVE=0 drops the attribute for profilers that cannot replay a
+        // cooperative cluster launch (on an otherwise idle GPU the grid is resident anyway, and
+        // the lockstep waits stay bounded)
+        if (env_int("HSDLA_COOPERATIVE", 1) != 0) {
+            at[1].id = cudaLaunchAttributeCooperative;
+            at[1].val.cooperative = 1;
+            cfg.numAttrs = 2;
+        }
+    }
+    return cudaLaunchKernelEx(&cfg, oz_pair_kernel, maps[0], maps[1], maps[2], maps[3], d_jobs, n_jobs, total, s,
+                              d_err, d_list, lockstep ? d_progress : (int *)nullptr);
 }
 
 // Launch of a prepared job table (no host synchronisation; capturable).
@@ -1115,7 +1479,8 @@ int ozaki_group_prepare(OzakiPlan &oz, const OzGroupDesc &d, const std::vector<O
             jsh.push_back(j);
         }
     g->n_jobs_sh = (int)jsh.size();
-    rc = upload_schedule(jsh, g->d_jobs_sh, g->d_list_sh, g->tiles_sh);
+    g->pair = use_pair();
+    rc = upload_schedule(jsh, g->d_jobs_sh, g->d_list_sh, g->tiles_sh, g->pair ? kPairTile : kTileN);
     if (rc) return fail(rc);
     memcpy(g->h_jobs_sh, jsh.data(), sizeof(OzJob) * jsh.size());
     g->maps_sh[0] = g->dC.map; g->maps_sh[1] = g->dW.map; g->maps_sh[2] = g->dX.map; g->maps_sh[3] = g->dC.map;
@@ -1159,8 +1524,10 @@ int ozaki_group_run(OzGroup *g, const DevSystem &sys, const KTable &ktab, cudaSt
         e = cudaMemcpyAsync(g->d_jobs_sh, g->h_jobs_sh, sizeof(OzJob) * g->n_jobs_sh, cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess && ev0) e = record(ev0, st);
     if (e == cudaSuccess)
-        e = launch_prepared(g->maps_sh, g->s, g->d_err, g->d_jobs_sh, g->n_jobs_sh, g->tiles_sh, g->d_list_sh,
-                            g->d_progress, st);
+        e = g->pair ? launch_pair(g->maps_sh, g->s, g->d_err, g->d_jobs_sh, g->n_jobs_sh, g->tiles_sh, g->d_list_sh,
+                                  g->d_progress, st)
+                    : launch_prepared(g->maps_sh, g->s, g->d_err, g->d_jobs_sh, g->n_jobs_sh, g->tiles_sh,
+                                      g->d_list_sh, g->d_progress, st);
     nl += 1;
     if (e == cudaSuccess && ev1) e = record(ev1, st);
     if (launches) *launches = nl;
