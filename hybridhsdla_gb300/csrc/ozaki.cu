@@ -33,6 +33,7 @@
 // word, stops issuing work, waits (bounded) for its in-flight copies and MMAs,
 // frees TMEM and returns.
 #include <cuda.h>
+#include <cuda_fp8.h>
 
 #include <algorithm>
 #include <cstdio>
@@ -766,17 +767,17 @@ __global__ void __launch_bounds__(kThreads, 1)
 // --------------------------------------------------------------- slicing
 // Digit planes of Z (Kin x ncols, column-major, ld ldz) with optional row weights v:
 // padded contraction layout: source rows [b*rpb, (b+1)*rpb) land at [b*bpad, b*bpad + rpb).
-constexpr int kSliceThreads = 256;
+//
+// One CTA per plane row (= source column), 512 threads and one CTA per SM, which keeps the
+// column set in flight (152 x <= 0.5 MB) inside L2: pass 1 reads the column from HBM for its
+// exponent, pass 2 re-reads it from L2 and writes the digits.  Digit extraction without carries:
+// with B = 16 (1 + 32 + ... + 32^(s-2)), the balanced digits d_i in [-16, 15] (i >= 2) of X are
+// the 5-bit fields of U = X + B minus 16, and the top digit is U >> 5(s-1) in [-16, 16]; digits
+// are encoded two at a time by the hardware f32 -> e4m3x2 conversion (exact for |d| <= 16).
+// A dual table slices the same source twice in one pass (C unweighted and W = C with row
+// weights), reading the source once.
+constexpr int kSliceThreads = 512;
 constexpr int kSliceVec = 8;       // consecutive contraction bytes per thread and plane
-
-__device__ __forceinline__ uint32_t e4m3_of_digit(int d) {
-    const uint32_t sgn = d < 0 ? 0x80u : 0u;
-    const uint32_t a = (uint32_t)(d < 0 ? -d : d);
-    if (a == 0) return 0u;
-    const uint32_t e = 31u - __clz(a);             // 0..4
-    const uint32_t man = ((a << 3) >> e) & 7u;
-    return sgn | ((e + 7u) << 3) | man;
-}
 
 // One slicing launch covers an operand for every k-point of a group: the k-points' columns
 // are stacked as consecutive rows of each digit plane (row0 of an entry = its first row).
@@ -793,88 +794,119 @@ struct SliceTab {
     uint8_t *digits = nullptr;
     int64_t Kpad = 0, plane_rows = 0, pitch = 0;
     int32_t *expo = nullptr;            // exponent of each plane row
+    // dual: a second digit operand of the same geometry from the same source with weights v2
+    const double *v2 = nullptr;
+    uint8_t *digits2 = nullptr;
+    int32_t *expo2 = nullptr;
     SliceEntry e[kMaxGroup];
 };
 
-__global__ void __launch_bounds__(kSliceThreads) oz_slice_kernel(const __grid_constant__ SliceTab tab) {
+__device__ __forceinline__ uint32_t pack4_e4m3(int d0, int d1, int d2, int d3) {
+    const uint32_t lo = __nv_cvt_float2_to_fp8x2(make_float2((float)d0, (float)d1), __NV_SATFINITE, __NV_E4M3);
+    const uint32_t hi = __nv_cvt_float2_to_fp8x2(make_float2((float)d2, (float)d3), __NV_SATFINITE, __NV_E4M3);
+    return lo | (hi << 16);
+}
+
+// plane i (0 = most significant) of U = X + B
+__device__ __forceinline__ int digit_of(long long U, int i, int s) {
+    if (i == 0) return (int)(U >> (5 * (s - 1)));
+    return (int)(((unsigned long long)U >> (5 * (s - 1 - i))) & 31ull) - 16;
+}
+
+// digit planes 2i + part (part 0 = real, 1 = imaginary) of 8 consecutive contraction bytes
+__device__ __forceinline__ void write_part(const long long (&x)[kSliceVec], int part, int s, uint8_t *row,
+                                          int64_t plane) {
+#pragma unroll
+    for (int i = 0; i < kOzMaxSlices; ++i) {
+        if (i >= s) break;
+        int d[kSliceVec];
+#pragma unroll
+        for (int u = 0; u < kSliceVec; ++u) d[u] = digit_of(x[u], i, s);
+        *reinterpret_cast<uint2 *>(row + (int64_t)(2 * i + part) * plane) =
+            make_uint2(pack4_e4m3(d[0], d[1], d[2], d[3]), pack4_e4m3(d[4], d[5], d[6], d[7]));
+    }
+}
+
+__device__ __forceinline__ void write_planes(const long long (&ur)[kSliceVec], const long long (&ui)[kSliceVec], int s,
+                                             uint8_t *row, int64_t plane) {
+    write_part(ur, 0, s, row, plane);
+    write_part(ui, 1, s, row, plane);
+}
+
+__device__ __forceinline__ double block_max(double m, double *red) {
+    for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
+    __syncthreads();
+    double r = 0.0;
+    for (int i = 0; i < kSliceThreads / 32; ++i) r = fmax(r, red[i]);
+    return r;
+}
+
+template <bool kDual>
+__global__ void __launch_bounds__(kSliceThreads, 1) oz_slice_kernel(const __grid_constant__ SliceTab tab) {
     const int64_t r = blockIdx.x;           // plane row
     int k = 0;
     while (k + 1 < tab.nk && tab.e[k + 1].row0 <= r) ++k;
     const int64_t g = r - tab.e[k].row0;
     const bool live = g >= 0 && g < tab.e[k].ncols;
     const double2 *Zc = tab.e[k].Z + tab.ldz * (live ? g : 0);
-    const double *v = tab.v;
-    const int64_t Kin = tab.Kin, rpb = tab.rpb, bpad = tab.bpad, Kpad = tab.Kpad, pitch = tab.pitch;
-    const int64_t plane_rows = tab.plane_rows;
+    const double *v = tab.v, *v2 = tab.v2;
+    const int Kin = (int)tab.Kin, rpb = (int)tab.rpb, bpad = (int)tab.bpad, Kpad = (int)tab.Kpad;
+    const int64_t pitch = tab.pitch, plane_rows = tab.plane_rows;
     const int s = tab.s;
-    __shared__ double red[kSliceThreads / 32];
-    __shared__ int e_sh;
-    // pass 1: column max of max(|re|, |im|) * v
-    double mx = 0.0;
+    __shared__ double red[2][kSliceThreads / 32];
+    // pass 1: column max of max(|re|, |im|) (times the row weight)
+    double mx = 0.0, mx2 = 0.0;
     if (live) {
-        for (int64_t kk = threadIdx.x; kk < Kin; kk += blockDim.x) {
+        for (int kk = threadIdx.x; kk < Kin; kk += kSliceThreads) {
             const double2 z = Zc[kk];
-            double a = fmax(fabs(z.x), fabs(z.y));
-            if (v) a *= v[kk];
-            mx = fmax(mx, a);
+            const double a = fmax(fabs(z.x), fabs(z.y));
+            mx = fmax(mx, v ? a * v[kk] : a);
+            if (kDual) mx2 = fmax(mx2, a * v2[kk]);
         }
     }
-    for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = mx;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        double m = 0.0;
-        for (int i = 0; i < kSliceThreads / 32; ++i) m = fmax(m, red[i]);
-        int e = 0;
-        if (m > 0.0) frexp(m, &e);                 // m < 2^e
-        e_sh = e;
-        tab.expo[r] = e;
+    int e = 0, e2 = 0;
+    const double m = block_max(mx, red[0]);
+    if (m > 0.0) frexp(m, &e);              // m < 2^e
+    if (kDual) {
+        const double m2 = block_max(mx2, red[1]);
+        if (m2 > 0.0) frexp(m2, &e2);
     }
-    __syncthreads();
-    const int e = e_sh;
-    const int top = 5 * s - 1;                     // X = rint(z 2^(5s-1)), |z| < 1
-    const double base_scale = ldexp(1.0, top - e);
-    const int64_t nb = Kpad / bpad;
-    for (int64_t kp0 = (int64_t)threadIdx.x * kSliceVec; kp0 < Kpad; kp0 += (int64_t)blockDim.x * kSliceVec) {
+    if (threadIdx.x == 0) {
+        tab.expo[r] = e;
+        if (kDual) tab.expo2[r] = e2;
+    }
+    const int top = 5 * s - 1;              // X = rint(z 2^(5s-1)), |z| < 1
+    const double base = ldexp(1.0, top - e), base2 = ldexp(1.0, top - e2);
+    long long B = 0;
+    for (int p = 0; p < s - 1; ++p) B |= 16ll << (5 * p);
+    const int nb = Kpad / bpad;
+    const int64_t plane = plane_rows * pitch;
+    for (int kp0 = threadIdx.x * kSliceVec; kp0 < Kpad; kp0 += kSliceThreads * kSliceVec) {
+        // a chunk never straddles a contraction block (bpad is a multiple of kSliceVec)
+        const int b = kp0 / bpad, rr0 = kp0 - b * bpad;
+        // number of live values of this chunk (a prefix: the block tail and Kin cut it from above)
+        const int nv = live && b < nb ? max(0, min(min(kSliceVec, rpb - rr0), Kin - (b * rpb + rr0))) : 0;
+        const double2 *zc = Zc + b * rpb + rr0;
         long long xr[kSliceVec], xi[kSliceVec];
 #pragma unroll
         for (int u = 0; u < kSliceVec; ++u) {
-            const int64_t kp = kp0 + u;
-            const int64_t b = kp / bpad, rr = kp - b * bpad;
-            const int64_t kk = b * rpb + rr;
-            xr[u] = 0; xi[u] = 0;
-            if (live && b < nb && rr < rpb && kk < Kin) {
-                const double2 z = Zc[kk];
-                const double sc = v ? base_scale * v[kk] : base_scale;
-                xr[u] = __double2ll_rn(z.x * sc);
-                xi[u] = __double2ll_rn(z.y * sc);
-            }
+            const double2 z = u < nv ? zc[u] : make_double2(0.0, 0.0);
+            const double sc = (v && u < nv) ? base * v[b * rpb + rr0 + u] : base;
+            xr[u] = B + __double2ll_rn(z.x * sc);
+            xi[u] = B + __double2ll_rn(z.y * sc);
         }
-        // digits from the least significant: d_i = ((X + 16) mod 32) - 16, X = (X - d_i) / 32,
-        // written plane by plane (8 consecutive bytes per thread and plane)
-        uint8_t *row = tab.digits + r * pitch + kp0;
-        const int64_t plane = plane_rows * pitch;
-#pragma unroll
-        for (int i = kOzMaxSlices - 1; i >= 0; --i) {
-            if (i >= s) continue;
-            uint32_t lr = 0u, hr = 0u, li = 0u, hi = 0u;
+        write_planes(xr, xi, s, tab.digits + r * pitch + kp0, plane);
+        if (kDual) {
+            // the chunk again (an L1 hit) for the weighted operand
 #pragma unroll
             for (int u = 0; u < kSliceVec; ++u) {
-                int da, db;
-                if (i == 0) {
-                    da = (int)xr[u]; db = (int)xi[u];
-                } else {
-                    da = (int)(((xr[u] + 16) & 31) - 16);
-                    db = (int)(((xi[u] + 16) & 31) - 16);
-                    xr[u] = (xr[u] - da) >> 5;
-                    xi[u] = (xi[u] - db) >> 5;
-                }
-                const uint32_t ea = e4m3_of_digit(da) << (8 * (u & 3));
-                const uint32_t eb = e4m3_of_digit(db) << (8 * (u & 3));
-                if (u < 4) { lr |= ea; li |= eb; } else { hr |= ea; hi |= eb; }
+                const double2 z = u < nv ? zc[u] : make_double2(0.0, 0.0);
+                const double sc = u < nv ? base2 * v2[b * rpb + rr0 + u] : base2;
+                xr[u] = B + __double2ll_rn(z.x * sc);
+                xi[u] = B + __double2ll_rn(z.y * sc);
             }
-            *reinterpret_cast<uint2 *>(row + (int64_t)(2 * i) * plane) = make_uint2(lr, hr);
-            *reinterpret_cast<uint2 *>(row + (int64_t)(2 * i + 1) * plane) = make_uint2(li, hi);
+            write_planes(xr, xi, s, tab.digits2 + r * pitch + kp0, plane);
         }
     }
 }
@@ -983,7 +1015,8 @@ SliceTab slice_table(const double2 *Z, int64_t ldz, const double *v, int64_t Kin
 }
 
 cudaError_t slice_launch(const SliceTab &t, cudaStream_t st) {
-    oz_slice_kernel<<<(unsigned)t.plane_rows, kSliceThreads, 0, st>>>(t);
+    if (t.digits2) oz_slice_kernel<true><<<(unsigned)t.plane_rows, kSliceThreads, 0, st>>>(t);
+    else oz_slice_kernel<false><<<(unsigned)t.plane_rows, kSliceThreads, 0, st>>>(t);
     return cudaGetLastError();
 }
 
@@ -1196,7 +1229,7 @@ struct OzGroup {
     std::vector<OzKBufs> kb;
     std::vector<int64_t> row0;
     DigitOperand dC, dW, dX, dM, dT;
-    SliceTab tC, tW, tM, tX;
+    SliceTab tC, tM, tX;     // tC is dual: C and W
     CUtensorMap maps_t[4], maps_sh[4];
     OzJob *d_jobs_t = nullptr, *d_jobs_sh = nullptr, *h_jobs_sh = nullptr;
     int n_jobs_t = 0, n_jobs_sh = 0;
@@ -1411,7 +1444,9 @@ int ozaki_group_prepare(OzakiPlan &oz, const OzGroupDesc &d, const std::vector<O
         return t;
     };
     g->tC = table(g->dC, g->K, nullptr, g->K, 0);
-    g->tW = table(g->dW, g->K, d.w, g->K, 0);
+    g->tC.v2 = d.w;
+    g->tC.digits2 = g->dW.digits;
+    g->tC.expo2 = g->dW.expo;
     g->tX = table(g->dX, g->K, nullptr, g->K, 0);
     if (d.hoist) g->tM = table(g->dM, d.twoL * d.nt, nullptr, d.twoL * d.nt, 1);
     // T digits once: they do not change between runs
@@ -1509,9 +1544,9 @@ static cudaError_t record(cudaEvent_t ev, cudaStream_t st) {
 int ozaki_group_run(OzGroup *g, const DevSystem &sys, const KTable &ktab, cudaStream_t st, cudaEvent_t ev0,
                     cudaEvent_t ev1, int *launches) {
     int nl = 0;
+    // C and W = C diag(w) in one pass over C
     cudaError_t e = slice_launch(g->tC, st);
-    if (e == cudaSuccess) e = slice_launch(g->tW, st);
-    nl += 2;
+    nl += 1;
     if (e == cudaSuccess && g->hoist) { e = slice_launch(g->tM, st); nl += 1; }
     if (e == cudaSuccess)
         e = launch_prepared(g->maps_t, g->s, g->d_err, g->d_jobs_t, g->n_jobs_t, g->tiles_t, g->d_list_t, nullptr, st);
