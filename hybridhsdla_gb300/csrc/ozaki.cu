@@ -491,7 +491,28 @@ __global__ void __launch_bounds__(kThreads, 1)
 // Every wait is bounded as in oz_gemm_kernel; both CTAs meet at a cluster barrier before TMEM
 // is freed, so no CTA exits while its shared memory or TMEM can still be addressed by the other.
 constexpr int kPairTile = 256;
-constexpr int kPairSmemSlack = 32768;      // keeps every descriptor-addressed byte inside the allocation
+// No "memory" clobber: nothing in the kernel reads the output, and a clobber would pin every
+// later load (column exponents, job fields) behind each reduction.  Volatile asm statements keep
+// their order among themselves, so successive reductions of an element stay in program order.
+__device__ __forceinline__ void red_add_f64(double *p, double v) {
+    asm volatile("red.relaxed.gpu.global.add.f64 [%0], %1;\n" ::"l"(p), "d"(v));
+}
+// x * 2^k as a double for an FP32 accumulator x (an exact integer, |x| <= 2^24), built with
+// integer operations: GB300's FP64 pipe is a small fraction of its integer pipes, and a drain
+// converts 2^16 values per CTA.  (f & 0x7fffffff) >> 3 puts the FP32 exponent and the top 20
+// mantissa bits exactly where the FP64 high word keeps them, so rebasing the exponent is one
+// add of (1023 - 127 + k) << 20; the low word takes the last 3 mantissa bits.  Valid for
+// k in [kPow2Lo, kPow2Hi] (the result stays normal); pow2_ok() checks that once per column.
+constexpr int kPow2Lo = -1022, kPow2Hi = 999;
+__device__ __forceinline__ bool pow2_ok(int k) { return k >= kPow2Lo && k <= kPow2Hi; }
+__device__ __forceinline__ double f32_pow2_to_f64_fast(uint32_t f, uint32_t ebias) {
+    const uint32_t a = f & 0x7fffffffu;
+    const uint32_t hi = (f & 0x80000000u) | ((a >> 3) + ebias);
+    const uint32_t lo = f << 29;
+    return a ? __hiloint2double((int)hi, (int)lo) : 0.0;
+}
+__device__ __noinline__ double f32_pow2_to_f64_slow(uint32_t f, int k) { return ldexp((double)__uint_as_float(f), k); }
+__device__ __forceinline__ uint32_t pow2_ebias(int k) { return (uint32_t)(1023 - 127 + k) << 20; }
 
 __device__ __forceinline__ uint32_t cluster_rank() {
     uint32_t r;
@@ -715,24 +736,31 @@ __global__ void __launch_bounds__(kThreads, 1)
         }
     } else {
         // ------------------------------------------------------------ epilogue (warps 2..9, both CTAs)
+        // A unit's drain: TMEM -> registers -> FP64 with the full scale 2^(2-5t+e_row+e_col) (built
+        // with integer operations) -> the output: a plain store for the tile's first unit,
+        // fire-and-forget f64 reductions in L2 for the others.  Each lane owns one output row, so
+        // successive updates of an element come from one thread and stay in program order; the
+        // SM never waits on the output.  Only stored elements (row < m, col < n, lower: row >=
+        // col) are written.
         const int q = warp & 3;                      // TMEM lane quadrant of this warp
         const int cbeg = ((warp - 2) >> 2) * (kPairTile / 2);   // its half of the columns
-        const int r_in_tile = (int)half + q * 32 + lane;
         int64_t unit = 0;
         bool ok = true;
         for (int64_t tile = pair; ok && tile < total_tiles; tile += npairs) {
             int64_t tm, tn;
             const OzJob &j = resolve_tile(jobs, num_jobs, tile_list, tile, tm, tn);
-            const int64_t row = tm * kPairTile + r_in_tile;
+            const int64_t row = tm * kPairTile + half + q * 32 + lane;
             const bool row_ok = row < j.m;
             const int erow = row_ok ? j.el[row] : 0;
+            const int64_t n = j.n, ldo = j.ldo;
+            const bool lower = j.lower != 0;
+            const int32_t *er = j.er;
+            double2 *orow = j.out + row;
             for (int t = 2; ok && t <= s + 1; ++t) {
                 const int ilo = max(1, t - s), ihi = min(s, t - 1);
                 const int64_t ck = chunk_kblocks(ihi - ilo + 1);
-                const double wt = ldexp(1.0, 2 - 5 * t);
                 for (int64_t cb = 0; ok && cb < j.nkb; cb += ck) {
                     const bool first = (t == 2 && cb == 0);
-                    const bool last = (t == s + 1 && cb + ck >= j.nkb);
                     if (!pwait(&bars.tfull, (uint32_t)(unit & 1), 4, warp, (int)unit)) { ok = false; break; }
                     tc_fence_after();
                     const uint32_t tbase = tmem_base + ((uint32_t)(q * 32) << 16);
@@ -747,7 +775,49 @@ __global__ void __launch_bounds__(kThreads, 1)
                             __syncwarp();
                             if (lane == 0) mbar_arrive_remote(tempty_leader);
                         }
-                        if (row_ok) drain32(j, row, tn * kPairTile + c0, vre, vim, wt, first, last, erow);
+                        const int64_t colb = tn * kPairTile + c0;
+                        // the 32 column exponents: one coalesced load, then broadcasts
+                        const int ecl = colb + lane < n ? __ldg(er + colb + lane) : 0;
+                        const int kb = 2 - 5 * t + erow;
+                        // columns [0, cend) of this batch are stored by this lane's row
+                        int64_t ce = row_ok ? min(n - colb, (int64_t)32) : 0;
+                        if (lower) ce = min(ce, row - colb + 1);
+                        const int cend = (int)max(ce, (int64_t)0);
+                        double2 *p = orow + ldo * colb;
+                        const bool fast = __all_sync(0xffffffffu, pow2_ok(kb + __reduce_min_sync(0xffffffffu, ecl)) &&
+                                                                      pow2_ok(kb + __reduce_max_sync(0xffffffffu, ecl)));
+                        if (fast) {
+                            // straight-line: every column's work is issued back to back, the
+                            // store / reductions predicated on cc < cend
+#pragma unroll
+                            for (int cc = 0; cc < 32; ++cc, p += ldo) {
+                                const uint32_t eb = pow2_ebias(kb + __shfl_sync(0xffffffffu, ecl, cc));
+                                const double re = f32_pow2_to_f64_fast(vre[cc], eb);
+                                const double im = f32_pow2_to_f64_fast(vim[cc], eb);
+                                if (cc < cend) {
+                                    if (first) {
+                                        *p = make_double2(re, im);
+                                    } else {
+                                        red_add_f64(&p->x, re);
+                                        red_add_f64(&p->y, im);
+                                    }
+                                }
+                            }
+                        } else {
+#pragma unroll
+                            for (int cc = 0; cc < 32; ++cc, p += ldo) {
+                                const int k = kb + __shfl_sync(0xffffffffu, ecl, cc);
+                                if (cc >= cend) continue;
+                                const double re = f32_pow2_to_f64_slow(vre[cc], k);
+                                const double im = f32_pow2_to_f64_slow(vim[cc], k);
+                                if (first) {
+                                    *p = make_double2(re, im);
+                                } else {
+                                    red_add_f64(&p->x, re);
+                                    red_add_f64(&p->y, im);
+                                }
+                            }
+                        }
                     }
                     ++unit;
                 }
@@ -1271,7 +1341,7 @@ int upload_schedule(std::vector<OzJob> &jobs, OzJob *d_jobs, int4 *d_list, int64
 cudaError_t launch_pair(const CUtensorMap *maps, int s, int *d_err, const OzJob *d_jobs, int n_jobs, int64_t total,
                         const int4 *d_list, int *d_progress, cudaStream_t st) {
     if (total <= 0) return cudaSuccess;
-    const size_t smem = (size_t)kStages * kStageBytes + kPairSmemSlack + 1024;
+    const size_t smem = (size_t)kStages * kStageBytes + 1024;
     cudaError_t e = cudaFuncSetAttribute(oz_pair_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     cudaLaunchConfig_t cfg = {};
