@@ -491,6 +491,22 @@ __global__ void __launch_bounds__(kThreads, 1)
 // Every wait is bounded as in oz_gemm_kernel; both CTAs meet at a cluster barrier before TMEM
 // is freed, so no CTA exits while its shared memory or TMEM can still be addressed by the other.
 constexpr int kPairTile = 256;
+constexpr int kStageCols = 4;                               // columns per drain staging buffer
+constexpr int kStageWarpBytes = 2 * kStageCols * 32 * 16;  // two buffers x 4 columns x 32 rows x 16 B
+constexpr int kPairStageBytes = kEpiWarps * kStageWarpBytes;
+__device__ __forceinline__ void bulk_store_g(void *gdst, uint32_t ssrc, uint32_t bytes) {
+    asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;\n" ::"l"(gdst), "r"(ssrc), "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ void bulk_add_g(void *gdst, uint32_t ssrc, uint32_t bytes) {
+    asm volatile("cp.reduce.async.bulk.global.shared::cta.bulk_group.add.f64 [%0], [%1], %2;\n" ::"l"(gdst),
+                 "r"(ssrc), "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;\n" ::: "memory"); }
+__device__ __forceinline__ void bulk_wait_read_1() { asm volatile("cp.async.bulk.wait_group.read 1;\n" ::: "memory"); }
+__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory"); }
 // No "memory" clobber: nothing in the kernel reads the output, and a clobber would pin every
 // later load (column exponents, job fields) behind each reduction.  Volatile asm statements keep
 // their order among themselves, so successive reductions of an element stay in program order.
@@ -744,18 +760,20 @@ __global__ void __launch_bounds__(kThreads, 1)
         // col) are written.
         const int q = warp & 3;                      // TMEM lane quadrant of this warp
         const int cbeg = ((warp - 2) >> 2) * (kPairTile / 2);   // its half of the columns
+        unsigned char *stg = smem + kStages * kStageBytes + (warp - 2) * kStageWarpBytes;
+        const uint32_t stg_s = smem_u32(stg);
         int64_t unit = 0;
         bool ok = true;
         for (int64_t tile = pair; ok && tile < total_tiles; tile += npairs) {
             int64_t tm, tn;
             const OzJob &j = resolve_tile(jobs, num_jobs, tile_list, tile, tm, tn);
-            const int64_t row = tm * kPairTile + half + q * 32 + lane;
-            const bool row_ok = row < j.m;
+            const int64_t r0 = tm * kPairTile + half + q * 32, row = r0 + lane;
+            const int64_t m = j.m, n = j.n, ldo = j.ldo;
+            const bool row_ok = row < m;
             const int erow = row_ok ? j.el[row] : 0;
-            const int64_t n = j.n, ldo = j.ldo;
             const bool lower = j.lower != 0;
             const int32_t *er = j.er;
-            double2 *orow = j.out + row;
+            double2 *out = j.out;
             for (int t = 2; ok && t <= s + 1; ++t) {
                 const int ilo = max(1, t - s), ihi = min(s, t - 1);
                 const int64_t ck = chunk_kblocks(ihi - ilo + 1);
@@ -763,7 +781,10 @@ __global__ void __launch_bounds__(kThreads, 1)
                     const bool first = (t == 2 && cb == 0);
                     if (!pwait(&bars.tfull, (uint32_t)(unit & 1), 4, warp, (int)unit)) { ok = false; break; }
                     tc_fence_after();
+                    // the previous unit's copies are complete: successive updates stay in order
+                    if (lane < kStageCols) bulk_wait_all();
                     const uint32_t tbase = tmem_base + ((uint32_t)(q * 32) << 16);
+                    int rd = 0;
 #pragma unroll 1
                     for (int c0 = cbeg; c0 < cbeg + kPairTile / 2; c0 += 32) {
                         uint32_t vre[32], vim[32];
@@ -779,43 +800,40 @@ __global__ void __launch_bounds__(kThreads, 1)
                         // the 32 column exponents: one coalesced load, then broadcasts
                         const int ecl = colb + lane < n ? __ldg(er + colb + lane) : 0;
                         const int kb = 2 - 5 * t + erow;
-                        // columns [0, cend) of this batch are stored by this lane's row
-                        int64_t ce = row_ok ? min(n - colb, (int64_t)32) : 0;
-                        if (lower) ce = min(ce, row - colb + 1);
-                        const int cend = (int)max(ce, (int64_t)0);
-                        double2 *p = orow + ldo * colb;
                         const bool fast = __all_sync(0xffffffffu, pow2_ok(kb + __reduce_min_sync(0xffffffffu, ecl)) &&
                                                                       pow2_ok(kb + __reduce_max_sync(0xffffffffu, ecl)));
-                        if (fast) {
-                            // straight-line: every column's work is issued back to back, the
-                            // store / reductions predicated on cc < cend
 #pragma unroll
-                            for (int cc = 0; cc < 32; ++cc, p += ldo) {
-                                const uint32_t eb = pow2_ebias(kb + __shfl_sync(0xffffffffu, ecl, cc));
-                                const double re = f32_pow2_to_f64_fast(vre[cc], eb);
-                                const double im = f32_pow2_to_f64_fast(vim[cc], eb);
-                                if (cc < cend) {
-                                    if (first) {
-                                        *p = make_double2(re, im);
-                                    } else {
-                                        red_add_f64(&p->x, re);
-                                        red_add_f64(&p->y, im);
-                                    }
-                                }
-                            }
-                        } else {
+                        for (int g4 = 0; g4 < 32; g4 += kStageCols, ++rd) {
+                            const uint32_t buf = (uint32_t)(rd & 1) * (kStageCols * 512);
+                            if (lane < kStageCols) bulk_wait_read_1();
+                            __syncwarp();
 #pragma unroll
-                            for (int cc = 0; cc < 32; ++cc, p += ldo) {
-                                const int k = kb + __shfl_sync(0xffffffffu, ecl, cc);
-                                if (cc >= cend) continue;
-                                const double re = f32_pow2_to_f64_slow(vre[cc], k);
-                                const double im = f32_pow2_to_f64_slow(vim[cc], k);
-                                if (first) {
-                                    *p = make_double2(re, im);
+                            for (int cc = 0; cc < kStageCols; ++cc) {
+                                const int c = g4 + cc;
+                                const int k = kb + __shfl_sync(0xffffffffu, ecl, c);
+                                double re, im;
+                                if (fast) {
+                                    const uint32_t eb = pow2_ebias(k);
+                                    re = f32_pow2_to_f64_fast(vre[c], eb);
+                                    im = f32_pow2_to_f64_fast(vim[c], eb);
                                 } else {
-                                    red_add_f64(&p->x, re);
-                                    red_add_f64(&p->y, im);
+                                    re = f32_pow2_to_f64_slow(vre[c], k);
+                                    im = f32_pow2_to_f64_slow(vim[c], k);
                                 }
+                                *reinterpret_cast<double2 *>(stg + buf + cc * 512 + lane * 16) = make_double2(re, im);
+                            }
+                            fence_async_smem();
+                            __syncwarp();
+                            if (lane < kStageCols) {
+                                const int64_t col = colb + g4 + lane;
+                                const int64_t lo = lower ? max(r0, col) : r0, hi = min(r0 + 32, m);
+                                if (col < n && lo < hi) {
+                                    const uint32_t src = stg_s + buf + lane * 512 + (uint32_t)(lo - r0) * 16;
+                                    double2 *dst = out + lo + ldo * col;
+                                    if (first) bulk_store_g(dst, src, (uint32_t)(hi - lo) * 16);
+                                    else bulk_add_g(dst, src, (uint32_t)(hi - lo) * 16);
+                                }
+                                bulk_commit();
                             }
                         }
                     }
@@ -823,6 +841,8 @@ __global__ void __launch_bounds__(kThreads, 1)
                 }
             }
         }
+        // every copy complete before the CTA may exit
+        if (lane < kStageCols) bulk_wait_all();
     }
     tc_fence_before();
     __syncwarp();
@@ -1341,7 +1361,7 @@ int upload_schedule(std::vector<OzJob> &jobs, OzJob *d_jobs, int4 *d_list, int64
 cudaError_t launch_pair(const CUtensorMap *maps, int s, int *d_err, const OzJob *d_jobs, int n_jobs, int64_t total,
                         const int4 *d_list, int *d_progress, cudaStream_t st) {
     if (total <= 0) return cudaSuccess;
-    const size_t smem = (size_t)kStages * kStageBytes + 1024;
+    const size_t smem = (size_t)kStages * kStageBytes + kPairStageBytes + 1024;
     cudaError_t e = cudaFuncSetAttribute(oz_pair_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     cudaLaunchConfig_t cfg = {};
