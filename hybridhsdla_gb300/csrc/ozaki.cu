@@ -223,7 +223,8 @@ __host__ __device__ __forceinline__ int64_t chunk_kblocks(int pairs) {
 // identical stage sequences, so staying within an epoch keeps the operand panels they share
 // resident in L2 (left to themselves, CTAs drift apart by far more than L2 can hold).
 // Bounded: on expiry the CTA raises the abort flag and records the error word.
-__device__ bool grid_lockstep(int *progress, int n, int epoch, volatile int *abort_flag, int *err, int slot) {
+__device__ bool grid_lockstep(int *progress, int n, int epoch, volatile int *abort_flag, int *err, int slot,
+                              int slack = 1) {
     atomicExch(progress + slot, epoch);
     const long long t0 = clock64();
     while (true) {
@@ -232,7 +233,7 @@ __device__ bool grid_lockstep(int *progress, int n, int epoch, volatile int *abo
             const int4 v = __ldcg(reinterpret_cast<const int4 *>(progress + i));
             mn = min(mn, min(min(v.x, v.y), min(v.z, v.w)));
         }
-        if (mn >= epoch - 1) return true;
+        if (mn >= epoch - slack) return true;
         if (*abort_flag) return false;
         if (clock64() - t0 > kWaitCycles) {
             *abort_flag = 1;
@@ -591,7 +592,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     oz_pair_kernel(const __grid_constant__ CUtensorMap map0, const __grid_constant__ CUtensorMap map1,
                    const __grid_constant__ CUtensorMap map2, const __grid_constant__ CUtensorMap map3,
                    const OzJob *__restrict__ jobs, int num_jobs, int64_t total_tiles, int s, int *err,
-                   const int4 *__restrict__ tile_list, int *progress) {
+                   const int4 *__restrict__ tile_list, int *progress, int sync_every, int slack) {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     unsigned char *smem = reinterpret_cast<unsigned char *>(
         (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
@@ -663,9 +664,9 @@ __global__ void __launch_bounds__(kThreads, 1)
                         for (int64_t kb = cb; ok && kb < ce; ++kb) {
                             for (int i = ilo; i <= ihi; ++i) {
                                 const int jj = t - i;
-                                if (leader && progress && issued > 0 && issued % kSyncEvery == 0 &&
-                                    !grid_lockstep(progress, (int)npairs, (int)(issued / kSyncEvery), &abort_flag,
-                                                   err, (int)pair)) { ok = false; break; }
+                                if (leader && progress && issued > 0 && issued % sync_every == 0 &&
+                                    !grid_lockstep(progress, (int)npairs, (int)(issued / sync_every), &abort_flag,
+                                                   err, (int)pair, slack)) { ok = false; break; }
                                 if (!pwait(&bars.empty[stage], phase ^ 1, 1, stage, (int)issued)) { ok = false; break; }
                                 unsigned char *st = smem + stage * kStageBytes;
                                 if (leader) mbar_expect_tx(&bars.full[stage], 2 * kStageBytes);
@@ -1402,8 +1403,11 @@ cudaError_t launch_pair(const CUtensorMap *maps, int s, int *d_err, const OzJob 
             cfg.numAttrs = 2;
         }
     }
+    // lockstep epoch (stages) and how many epochs a pair may lead the slowest one
+    static const int sync_every = (int)std::max<int64_t>(8, env_int("HSDLA_SYNC_EVERY", kSyncEvery));
+    static const int slack = (int)std::max<int64_t>(1, env_int("HSDLA_SYNC_SLACK", 1));
     return cudaLaunchKernelEx(&cfg, oz_pair_kernel, maps[0], maps[1], maps[2], maps[3], d_jobs, n_jobs, total, s,
-                              d_err, d_list, lockstep ? d_progress : (int *)nullptr);
+                              d_err, d_list, lockstep ? d_progress : (int *)nullptr, sync_every, slack);
 }
 
 // Launch of a prepared job table (no host synchronisation; capturable).
