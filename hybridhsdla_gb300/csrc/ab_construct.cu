@@ -297,7 +297,7 @@ __global__ void __launch_bounds__(kThreads) construct_ab_kernel(DevSystem sys, c
 }  // namespace
 
 // X[2L a + r, g] = e^{i 2pi (k+g).tau_a} Z[2L t(a) + r, g]: the per-atom T application rebuilt
-// from the per-type product Z_t = T_t M_t.
+// from the per-type product Z_t = T_t M_t, for the atoms [a0, a1) of the table.
 __global__ void __launch_bounds__(kThreads) apply_phase_kernel(DevSystem sys, const __grid_constant__ KTable tab) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     double2 *ph = reinterpret_cast<double2 *>(smem_raw);       // [na]
@@ -321,8 +321,10 @@ __global__ void __launch_bounds__(kThreads) apply_phase_kernel(DevSystem sys, co
         __syncthreads();
         const double2 *zc = Z + ldz * gi;
         double2 *xc = X + ldx * gi;
-        const int64_t nrow = (int64_t)twoL * na;
-        for (int64_t idx = threadIdx.x; idx < nrow; idx += blockDim.x) {
+        const int a0 = tab.a0, a1 = tab.a1 < 0 ? na : tab.a1;
+        const int64_t r0 = (int64_t)twoL * a0, nrow = (int64_t)twoL * (a1 - a0);
+        for (int64_t i = threadIdx.x; i < nrow; i += blockDim.x) {
+            const int64_t idx = r0 + i;
             const int j = (int)(idx / twoL);
             const int r = (int)(idx - (int64_t)j * twoL);
             xc[idx] = cmul(ph[j], zc[(int64_t)twoL * sys.atom_type[j] + r]);

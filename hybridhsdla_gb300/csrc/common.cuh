@@ -55,6 +55,7 @@ struct KEntry {
 };
 struct KTable {
     int nk = 0;
+    int a0 = 0, a1 = -1;        // atom range of the phase expansion (a1 < 0: every atom)
     int64_t ldc = 0, ldm = 0;
     int64_t total_cols = 0;
     KEntry e[kMaxGroup];

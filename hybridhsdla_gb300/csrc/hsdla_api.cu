@@ -93,6 +93,7 @@ struct hsdla_plan {
     bool autotune = false;           // Ozaki slice count still to be chosen from the data
     bool hoist = false;              // T application per type (no atom carries its own rotation)
     bool external = false;           // C is supplied by the caller (contraction-only entry)
+    int panels = 1;                  // atom panels of the Ozaki contraction (memory-bounded streaming)
     double est_err = 0.0;            // autotuner's predicted relative error
     int launches = 0;
 };
@@ -638,7 +639,7 @@ int64_t group_bytes(const hsdla_plan *pl, const std::vector<int> &kidx) {
     std::vector<int64_t> G;
     for (int i : kidx) { b += kpoint_fp64_bytes(pl, pl->kps[i].n_g); G.push_back(pl->kps[i].n_g); }
     if (pl->opts.precision == HSDLA_PREC_OZAKI_FP8)
-        b += 1024 + ozaki_group_bytes(pl->oz.num_slices, 2 * (int64_t)pl->L, pl->na, pl->nt, G);
+        b += 1024 + ozaki_group_bytes(pl->oz.num_slices, 2 * (int64_t)pl->L, pl->na, pl->nt, G, pl->panels, pl->hoist);
     return b;
 }
 
@@ -646,7 +647,7 @@ int64_t group_persist_bytes(const hsdla_plan *pl, const std::vector<int> &kidx) 
     std::vector<int64_t> G;
     for (int i : kidx) G.push_back(pl->kps[i].n_g);
     if (pl->opts.precision == HSDLA_PREC_OZAKI_FP8)
-        return ozaki_group_persist_bytes(pl->oz.num_slices, 2 * (int64_t)pl->L, pl->na, pl->nt, G);
+        return ozaki_group_persist_bytes(pl->oz.num_slices, 2 * (int64_t)pl->L, pl->na, pl->nt, G, pl->panels);
     return 4096 + (int64_t)sizeof(Fp64Job) * (int64_t)kidx.size() * (std::max(pl->na, pl->nt) + 4);
 }
 
@@ -666,8 +667,26 @@ int64_t workspace_budget(hsdla_context *ctx) {
     return budget;
 }
 
+// Atom panels of the Ozaki contraction: the fewest whose one-k-point workspace (the largest
+// k-point) fits the budget; HSDLA_PANELS forces a count.  The digit planes of a panel are the
+// bulk of the workspace, so P panels need about 1/P of them.
+void choose_panels(hsdla_plan *pl, int64_t budget) {
+    pl->panels = 1;
+    if (pl->opts.precision != HSDLA_PREC_OZAKI_FP8) return;
+    const char *ev = getenv("HSDLA_PANELS");
+    const int64_t forced = ev ? strtoll(ev, nullptr, 10) : 0;
+    if (forced > 0) { pl->panels = (int)std::min<int64_t>(forced, pl->na); return; }
+    int big = -1;
+    for (int i = 0; i < (int)pl->kps.size(); ++i)
+        if (pl->kps[i].n_g > 0 && (big < 0 || pl->kps[i].n_g > pl->kps[big].n_g)) big = i;
+    if (big < 0) return;
+    const std::vector<int> one{big};
+    while (pl->panels < pl->na && group_bytes(pl, one) > budget) ++pl->panels;
+}
+
 // Greedy k-point groups whose workspace fits the budget (at least one k-point per group).
 void form_groups(hsdla_plan *pl, int64_t budget) {
+    choose_panels(pl, budget);
     pl->groups.clear();
     std::vector<int> cur;
     for (int i = 0; i < (int)pl->kps.size(); ++i) {
@@ -750,6 +769,7 @@ int prepare_groups(hsdla_plan *pl, void *ws, cudaStream_t st) {
             OzGroupDesc d;
             d.twoL = twoL; d.na = pl->na; d.nt = pl->nt; d.hoist = pl->hoist;
             d.w = pl->w; d.Tfull = pl->Tfull; d.atom_type = pl->atom_type.data();
+            d.panels = pl->panels;
             char *oz_ws = reinterpret_cast<char *>((reinterpret_cast<uintptr_t>(p) + 1023) & ~uintptr_t(1023));
             int rc = ozaki_group_prepare(pl->oz, d, kb, oz_ws, g.persist, st, &g.oz);
             if (rc) return set_err(ctx, rc, "group set-up failed: %s", ozaki_last_error());
@@ -1046,6 +1066,7 @@ int hsdla_plan_execute(hsdla_plan *pl, hsdla_cx *const *dH, hsdla_cx *const *dS,
         rep->num_slices = pl->opts.precision == HSDLA_PREC_OZAKI_FP8 ? pl->oz.num_slices : 0;
         rep->est_rel_err = pl->est_err;
         rep->kernel_launches = pl->launches;
+        rep->num_panels = pl->opts.precision == HSDLA_PREC_OZAKI_FP8 ? pl->panels : 0;
     }
     return HSDLA_OK;
 }
@@ -1201,6 +1222,7 @@ int hsdla_contract_ab(hsdla_context *ctx, int32_t L, int32_t a, int64_t G, const
         rep->dominant_flop = dom_flop;
         rep->num_slices = pl->opts.precision == HSDLA_PREC_OZAKI_FP8 ? pl->oz.num_slices : 0;
         rep->kernel_launches = pl->launches;
+        rep->num_panels = pl->opts.precision == HSDLA_PREC_OZAKI_FP8 ? pl->panels : 0;
     }
     return done(HSDLA_OK);
 }

@@ -65,7 +65,8 @@ constexpr int kErrWords = 8;                        // error word + diagnostics 
 
 struct OzJob {
     int32_t lmap, rmap;        // tensor-map index (0..3) of the left / right digit operand
-    int32_t lower, pad0;       // 1: only tiles and elements with row >= col
+    int32_t lower;             // 1: only tiles and elements with row >= col
+    int32_t accum;             // 1: the first unit of a tile adds to the output instead of storing
     int64_t lplane, rplane;    // rows per digit plane in each map
     int64_t lrow0, rrow0;      // first operand row (output row / col 0) inside a plane
     int64_t lk0, rk0;          // first contraction byte (multiple of 128)
@@ -243,13 +244,14 @@ __device__ bool grid_lockstep(int *progress, int n, int epoch, volatile int *abo
     }
 }
 
-// Drain 32 accumulator columns of one output row: out += w (re, im) (plain store on the first unit
-// of a tile), times 2^(e_row + e_col) on the last.  Loads are grouped 16 at a time ahead of the
-// stores (the compiler cannot reorder a load past a store to a possibly aliasing column), so a
-// drain costs a few L2 round trips per 32 columns instead of one per column.
+// Drain 32 accumulator columns of one output row: out = (out +) x 2^(kb + e_col) with kb =
+// 2 - 5t + e_row (a plain store on the first unit of a tile).  Every unit carries its full scale,
+// so an output that already holds an earlier panel's sum is accumulated correctly.  Loads are
+// grouped kDrainBatch at a time ahead of the stores (the compiler cannot reorder a load past a
+// store to a possibly aliasing column), so a drain costs a few L2 round trips per 32 columns.
 constexpr int kDrainBatch = 8;
 __device__ __forceinline__ void drain32(const OzJob &j, int64_t row, int64_t col0, const uint32_t (&vre)[32],
-                                        const uint32_t (&vim)[32], double wt, bool first, bool last, int erow) {
+                                        const uint32_t (&vim)[32], int kb, bool first) {
 #pragma unroll
     for (int h = 0; h < 32; h += kDrainBatch) {
         double2 o[kDrainBatch];
@@ -263,13 +265,9 @@ __device__ __forceinline__ void drain32(const OzJob &j, int64_t row, int64_t col
         for (int cc = 0; cc < kDrainBatch; ++cc) {
             const int64_t col = col0 + h + cc;
             if (col >= j.n || (j.lower && row < col)) continue;
-            double re = (double)__uint_as_float(vre[h + cc]) * wt + o[cc].x;
-            double im = (double)__uint_as_float(vim[h + cc]) * wt + o[cc].y;
-            if (last) {
-                const double sc = ldexp(1.0, erow + j.er[col]);
-                re *= sc;
-                im *= sc;
-            }
+            const double sc = ldexp(1.0, kb + j.er[col]);
+            const double re = (double)__uint_as_float(vre[h + cc]) * sc + o[cc].x;
+            const double im = (double)__uint_as_float(vim[h + cc]) * sc + o[cc].y;
             j.out[row + j.ldo * col] = make_double2(re, im);
         }
     }
@@ -443,10 +441,8 @@ __global__ void __launch_bounds__(kThreads, 1)
             for (int t = 2; ok && t <= s + 1; ++t) {
                 const int ilo = max(1, t - s), ihi = min(s, t - 1);
                 const int64_t ck = chunk_kblocks(ihi - ilo + 1);
-                const double wt = ldexp(1.0, 2 - 5 * t);
                 for (int64_t cb = 0; ok && cb < j.nkb; cb += ck) {
-                    const bool first = (t == 2 && cb == 0);
-                    const bool last = (t == s + 1 && cb + ck >= j.nkb);
+                    const bool first = (t == 2 && cb == 0) && !j.accum;
                     const int buf = (int)(unit & 1);
                     const uint32_t uphase = (uint32_t)((unit >> 1) & 1);
                     if (!mbar_wait(&bars.tfull[buf], uphase, &abort_flag, err, 4)) { ok = false; break; }
@@ -462,7 +458,7 @@ __global__ void __launch_bounds__(kThreads, 1)
                             tc_fence_before();
                             mbar_arrive(&bars.tempty[buf]);
                         }
-                        if (row_ok) drain32(j, row, tn * kTileN + c0, vre, vim, wt, first, last, erow);
+                        if (row_ok) drain32(j, row, tn * kTileN + c0, vre, vim, 2 - 5 * t + erow, first);
                     }
                     ++unit;
                 }
@@ -779,7 +775,7 @@ __global__ void __launch_bounds__(kThreads, 1)
                 const int ilo = max(1, t - s), ihi = min(s, t - 1);
                 const int64_t ck = chunk_kblocks(ihi - ilo + 1);
                 for (int64_t cb = 0; ok && cb < j.nkb; cb += ck) {
-                    const bool first = (t == 2 && cb == 0);
+                    const bool first = (t == 2 && cb == 0) && !j.accum;
                     if (!pwait(&bars.tfull, (uint32_t)(unit & 1), 4, warp, (int)unit)) { ok = false; break; }
                     tc_fence_after();
                     // the previous unit's copies are complete: successive updates stay in order
@@ -1313,17 +1309,28 @@ int ozaki_herkx(OzakiPlan &oz, const double2 *P, int64_t ldp, const double2 *Q, 
 // k-point, one slicing launch per operand covers the group, and one oz_gemm launch runs the T
 // application and one the S/H products of all k-points.  Everything but the output pointers
 // is prepared once; a run only enqueues launches (it can be captured in a CUDA graph).
+// One atom panel of a group: the contraction index split by atoms, each panel sliced with its own
+// exponents and its S/H products accumulated into the outputs.
+struct OzPanel {
+    int64_t a0 = 0, a1 = 0;            // atoms [a0, a1)
+    SliceTab tC, tX;                   // tC is dual: C and W
+    int64_t jt_off = 0, lt_off = 0;    // this panel's T-application jobs / tiles (non-hoisted)
+    int n_jobs_t = 0;
+    int64_t tiles_t = 0;
+};
+
 struct OzGroup {
-    int s = 0, nk = 0;
+    int s = 0, nk = 0, panels = 1;
     bool hoist = false;
-    int64_t twoL = 0, na = 0, nt = 0, K = 0, bpad = 0, Kpad = 0, rows = 0;
+    int64_t twoL = 0, na = 0, nt = 0, K = 0, bpad = 0, rows = 0;
     std::vector<OzKBufs> kb;
     std::vector<int64_t> row0;
+    std::vector<OzPanel> pan;
     DigitOperand dC, dW, dX, dM, dT;
-    SliceTab tC, tM, tX;     // tC is dual: C and W
+    SliceTab tM;
     CUtensorMap maps_t[4], maps_sh[4];
     OzJob *d_jobs_t = nullptr, *d_jobs_sh = nullptr, *h_jobs_sh = nullptr;
-    int n_jobs_t = 0, n_jobs_sh = 0;
+    int n_jobs_t = 0, n_jobs_sh = 0;   // hoisted T jobs; S/H jobs per panel (2 per k-point)
     int4 *d_list_t = nullptr, *d_list_sh = nullptr;
     int64_t tiles_t = 0, tiles_sh = 0;
     int *d_progress = nullptr;
@@ -1448,13 +1455,18 @@ cudaError_t launch_prepared(const CUtensorMap *maps, int s, int *d_err, const Oz
 
 // Run-time scratch of a group (digit planes and exponents, rewritten by every run; groups of a
 // plan share it) and its persistent part (T digits, job tables, tile schedules, lockstep slots).
-int64_t ozaki_group_bytes(int s, int64_t twoL, int64_t na, int64_t nt, const std::vector<int64_t> &G) {
-    const int64_t bpad = round_up(twoL, kKBlock), Kpad = bpad * na, rows = group_rows(G);
-    const int64_t dig = round_up(2 * s * rows * (Kpad + pitch_pad()), 1024) + round_up(4 * rows, 1024);
-    return 3 * dig + 4096;
+static int64_t panel_atoms(int64_t na, int panels) { return (na + panels - 1) / panels; }
+
+int64_t ozaki_group_bytes(int s, int64_t twoL, int64_t na, int64_t nt, const std::vector<int64_t> &G, int panels,
+                          bool hoist) {
+    const int64_t bpad = round_up(twoL, kKBlock), rows = group_rows(G);
+    const int64_t Kp = bpad * panel_atoms(na, panels), Kx = hoist ? std::max(Kp, bpad * nt) : Kp;
+    auto dig = [&](int64_t K) { return round_up(2 * s * rows * (K + pitch_pad()), 1024) + round_up(4 * rows, 1024); };
+    return 2 * dig(Kp) + dig(Kx) + 4096;
 }
 
-int64_t ozaki_group_persist_bytes(int s, int64_t twoL, int64_t na, int64_t nt, const std::vector<int64_t> &G) {
+int64_t ozaki_group_persist_bytes(int s, int64_t twoL, int64_t na, int64_t nt, const std::vector<int64_t> &G,
+                                  int panels) {
     const int64_t bpad = round_up(twoL, kKBlock);
     const int64_t nk = (int64_t)G.size();
     int64_t tiles_t = 0, tiles_sh = 0;
@@ -1464,7 +1476,7 @@ int64_t ozaki_group_persist_bytes(int s, int64_t twoL, int64_t na, int64_t nt, c
         tiles_sh += T * (T + 1);
     }
     return operand_bytes(s, nt * twoL, bpad) + round_up(sizeof(OzJob) * nk * (std::max(na, nt) + 2), 1024) +
-           round_up(sizeof(OzJob) * 2 * nk, 1024) + round_up(sizeof(int4) * (tiles_t + 1), 1024) +
+           round_up(sizeof(OzJob) * 2 * nk * panels, 1024) + round_up(sizeof(int4) * (tiles_t + panels), 1024) +
            round_up(sizeof(int4) * (tiles_sh + 1), 1024) + round_up(sizeof(int) * kProgressCap, 1024) + 8192;
 }
 
@@ -1472,6 +1484,7 @@ int ozaki_group_prepare(OzakiPlan &oz, const OzGroupDesc &d, const std::vector<O
                         void *persist, cudaStream_t st, OzGroup **out) {
     *out = nullptr;
     if (kb.empty() || (int)kb.size() > kMaxGroup) { g_oz_err = "group size out of range"; return HSDLA_ERR_ARG; }
+    if (d.panels < 1 || d.panels > d.na) { g_oz_err = "panel count out of range"; return HSDLA_ERR_ARG; }
     auto *g = new OzGroup();
     g->s = oz.num_slices;
     g->nk = (int)kb.size();
@@ -1479,9 +1492,17 @@ int ozaki_group_prepare(OzakiPlan &oz, const OzGroupDesc &d, const std::vector<O
     g->twoL = d.twoL; g->na = d.na; g->nt = d.nt;
     g->K = d.twoL * d.na;
     g->bpad = round_up(d.twoL, kKBlock);
-    g->Kpad = g->bpad * d.na;
     g->kb = kb;
     g->d_err = oz.d_error;
+    // atom panels: equal sizes but the last
+    const int64_t pa = panel_atoms(d.na, d.panels);
+    for (int64_t a0 = 0; a0 < d.na; a0 += pa) {
+        OzPanel p;
+        p.a0 = a0;
+        p.a1 = std::min(d.na, a0 + pa);
+        g->pan.push_back(p);
+    }
+    g->panels = (int)g->pan.size();
     std::vector<int64_t> G;
     for (auto &k : kb) G.push_back(k.G);
     g->rows = group_rows(G);
@@ -1497,11 +1518,13 @@ int ozaki_group_prepare(OzakiPlan &oz, const OzGroupDesc &d, const std::vector<O
         o.digits = ar.take<uint8_t>(2 * s * o.plane_rows * o.pitch);
         o.expo = ar.take<int32_t>(o.plane_rows);
     };
-    carve_rows(g->dC, g->Kpad);
-    carve_rows(g->dW, g->Kpad);
-    carve_rows(g->dX, g->Kpad);
+    const int64_t Kp = g->bpad * pa;
+    carve_rows(g->dC, Kp);
+    carve_rows(g->dW, Kp);
+    carve_rows(g->dX, d.hoist ? std::max(Kp, g->bpad * d.nt) : Kp);
     carve_operand(keep, g->dT, s, d.nt * d.twoL, g->bpad);
-    // the M digits (per-type rows, K = bpad nt) borrow the X digit region, free until X is sliced
+    // the M digits (per-type rows, K = bpad nt) borrow the X digit region: they are consumed by the
+    // T application, which runs before any panel's X is sliced
     g->dM.plane_rows = g->rows;
     g->dM.Kpad = g->bpad * d.nt;
     g->dM.pitch = g->dM.Kpad + pitch_pad();
@@ -1515,34 +1538,39 @@ int ozaki_group_prepare(OzakiPlan &oz, const OzGroupDesc &d, const std::vector<O
         tiles_sh += T * (T + 1);
     }
     g->d_jobs_t = keep.take<OzJob>(nk * (std::max(d.na, d.nt) + 2));
-    g->d_jobs_sh = keep.take<OzJob>(2 * nk);
-    g->d_list_t = keep.take<int4>(tiles_t + 1);
+    g->d_jobs_sh = keep.take<OzJob>(2 * nk * g->panels);
+    g->d_list_t = keep.take<int4>(tiles_t + g->panels);
     g->d_list_sh = keep.take<int4>(tiles_sh + 1);
     g->d_progress = keep.take<int>(kProgressCap);
     int rc = HSDLA_OK;
     auto fail = [&](int code) { ozaki_group_destroy(g); return code; };
-    if (cudaHostAlloc((void **)&g->h_jobs_sh, sizeof(OzJob) * 2 * nk, cudaHostAllocDefault) != cudaSuccess) {
+    if (cudaHostAlloc((void **)&g->h_jobs_sh, sizeof(OzJob) * 2 * nk * g->panels, cudaHostAllocDefault) !=
+        cudaSuccess) {
         g->h_jobs_sh = nullptr;
         g_oz_err = "pinned job table allocation failed";
         return fail(HSDLA_ERR_NOMEM);
     }
-    // slicing tables of the group's operands
-    auto table = [&](const DigitOperand &o, int64_t ldz, const double *v, int64_t Kin, int which) {
+    // slicing tables: source rows [a0 2L, a1 2L) of every k-point's column
+    auto table = [&](const DigitOperand &o, int64_t ldz, const double *v, int64_t row_off, int64_t Kin, int64_t kpad,
+                     int which) {
         SliceTab t;
         t.nk = g->nk; t.s = s; t.ldz = ldz; t.Kin = Kin; t.rpb = d.twoL; t.bpad = g->bpad; t.v = v;
-        t.digits = o.digits; t.Kpad = o.Kpad; t.plane_rows = o.plane_rows; t.pitch = o.pitch; t.expo = o.expo;
+        t.digits = o.digits; t.Kpad = kpad; t.plane_rows = o.plane_rows; t.pitch = o.pitch; t.expo = o.expo;
         for (int k = 0; k < g->nk; ++k) {
-            const double2 *src = which == 1 ? kb[k].M : kb[k].CX;
+            const double2 *src = which == 1 ? kb[k].M : kb[k].CX + row_off;
             t.e[k] = SliceEntry{src, kb[k].G, g->row0[k]};
         }
         return t;
     };
-    g->tC = table(g->dC, g->K, nullptr, g->K, 0);
-    g->tC.v2 = d.w;
-    g->tC.digits2 = g->dW.digits;
-    g->tC.expo2 = g->dW.expo;
-    g->tX = table(g->dX, g->K, nullptr, g->K, 0);
-    if (d.hoist) g->tM = table(g->dM, d.twoL * d.nt, nullptr, d.twoL * d.nt, 1);
+    for (OzPanel &p : g->pan) {
+        const int64_t off = p.a0 * d.twoL, Kin = (p.a1 - p.a0) * d.twoL, kpad = (p.a1 - p.a0) * g->bpad;
+        p.tC = table(g->dC, g->K, nullptr, off, Kin, kpad, 0);
+        p.tC.v2 = d.w + off;
+        p.tC.digits2 = g->dW.digits;
+        p.tC.expo2 = g->dW.expo;
+        p.tX = table(g->dX, g->K, nullptr, off, Kin, kpad, 0);
+    }
+    if (d.hoist) g->tM = table(g->dM, d.twoL * d.nt, nullptr, 0, d.twoL * d.nt, g->bpad * d.nt, 1);
     // T digits once: they do not change between runs
     cudaError_t e = slice(d.Tfull, d.twoL, nullptr, d.twoL, d.nt * d.twoL, d.twoL, g->bpad, s, g->dT, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
@@ -1553,10 +1581,10 @@ int ozaki_group_prepare(OzakiPlan &oz, const OzGroupDesc &d, const std::vector<O
     if (!rc) rc = make_map(g->dT, s);
     if (!rc && d.hoist) rc = make_map(g->dM, s);
     if (rc) return fail(rc);
-    // (b) T application jobs
-    std::vector<OzJob> jt;
-    for (int k = 0; k < g->nk; ++k) {
-        if (d.hoist) {
+    // (b) T application: per type once (hoisted), or per atom of each panel
+    if (d.hoist) {
+        std::vector<OzJob> jt;
+        for (int k = 0; k < g->nk; ++k)
             for (int64_t t = 0; t < d.nt; ++t) {
                 OzJob j;
                 memset(&j, 0, sizeof(j));
@@ -1570,59 +1598,88 @@ int ozaki_group_prepare(OzakiPlan &oz, const OzGroupDesc &d, const std::vector<O
                 j.el = g->dT.expo + t * d.twoL; j.er = g->dM.expo + g->row0[k];
                 jt.push_back(j);
             }
-        } else {
-            for (int64_t a = 0; a < d.na; ++a) {
-                const int64_t t = d.atom_type[a];
-                OzJob j;
-                memset(&j, 0, sizeof(j));
-                j.lmap = 3; j.rmap = 0;
-                j.lplane = g->dT.plane_rows; j.rplane = g->dC.plane_rows;
-                j.lrow0 = t * d.twoL; j.rrow0 = g->row0[k];
-                j.rk0 = a * g->bpad;
-                j.nkb = g->bpad / kKBlock;
-                j.m = d.twoL; j.n = kb[k].G;
-                j.out = kb[k].CX + d.twoL * a; j.ldo = g->K;
-                j.el = g->dT.expo + t * d.twoL; j.er = g->dC.expo + g->row0[k];
-                jt.push_back(j);
-            }
+        g->n_jobs_t = (int)jt.size();
+        rc = upload_schedule(jt, g->d_jobs_t, g->d_list_t, g->tiles_t);
+        if (rc) return fail(rc);
+    } else {
+        int64_t joff = 0, loff = 0;
+        for (OzPanel &p : g->pan) {
+            std::vector<OzJob> jt;
+            for (int k = 0; k < g->nk; ++k)
+                for (int64_t a = p.a0; a < p.a1; ++a) {
+                    const int64_t t = d.atom_type[a];
+                    OzJob j;
+                    memset(&j, 0, sizeof(j));
+                    j.lmap = 3; j.rmap = 0;
+                    j.lplane = g->dT.plane_rows; j.rplane = g->dC.plane_rows;
+                    j.lrow0 = t * d.twoL; j.rrow0 = g->row0[k];
+                    j.rk0 = (a - p.a0) * g->bpad;
+                    j.nkb = g->bpad / kKBlock;
+                    j.m = d.twoL; j.n = kb[k].G;
+                    j.out = kb[k].CX + d.twoL * a; j.ldo = g->K;
+                    j.el = g->dT.expo + t * d.twoL; j.er = g->dC.expo + g->row0[k];
+                    jt.push_back(j);
+                }
+            p.jt_off = joff;
+            p.lt_off = loff;
+            p.n_jobs_t = (int)jt.size();
+            rc = upload_schedule(jt, g->d_jobs_t + joff, g->d_list_t + loff, p.tiles_t);
+            if (rc) return fail(rc);
+            joff += p.n_jobs_t;
+            loff += p.tiles_t;
         }
     }
-    g->n_jobs_t = (int)jt.size();
-    rc = upload_schedule(jt, g->d_jobs_t, g->d_list_t, g->tiles_t);
-    if (rc) return fail(rc);
     g->maps_t[0] = d.hoist ? g->dM.map : g->dC.map;
     g->maps_t[1] = g->maps_t[0]; g->maps_t[2] = g->maps_t[0]; g->maps_t[3] = g->dT.map;
-    // (c) S and H jobs; outputs are patched per run
-    std::vector<OzJob> jsh;
-    for (int k = 0; k < g->nk; ++k)
-        for (int which = 0; which < 2; ++which) {
-            OzJob j;
-            memset(&j, 0, sizeof(j));
-            j.lmap = 0; j.rmap = which == 0 ? 1 : 2; j.lower = 1;
-            j.lplane = g->dC.plane_rows; j.rplane = which == 0 ? g->dW.plane_rows : g->dX.plane_rows;
-            j.lrow0 = g->row0[k]; j.rrow0 = g->row0[k];
-            j.nkb = g->Kpad / kKBlock;
-            j.m = kb[k].G; j.n = kb[k].G;
-            j.el = g->dC.expo + g->row0[k];
-            j.er = (which == 0 ? g->dW.expo : g->dX.expo) + g->row0[k];
-            jsh.push_back(j);
-        }
-    g->n_jobs_sh = (int)jsh.size();
+    // (c) S and H jobs of every panel; outputs are patched per run, later panels accumulate
     g->pair = use_pair();
-    rc = upload_schedule(jsh, g->d_jobs_sh, g->d_list_sh, g->tiles_sh, g->pair ? kPairTile : kTileN);
-    if (rc) return fail(rc);
-    memcpy(g->h_jobs_sh, jsh.data(), sizeof(OzJob) * jsh.size());
+    const int64_t tile = g->pair ? kPairTile : kTileN;
+    g->n_jobs_sh = 2 * g->nk;
+    for (int pi = 0; pi < g->panels; ++pi) {
+        const OzPanel &p = g->pan[pi];
+        std::vector<OzJob> jsh;
+        for (int k = 0; k < g->nk; ++k)
+            for (int which = 0; which < 2; ++which) {
+                OzJob j;
+                memset(&j, 0, sizeof(j));
+                j.lmap = 0; j.rmap = which == 0 ? 1 : 2; j.lower = 1;
+                j.accum = pi > 0;
+                j.lplane = g->dC.plane_rows; j.rplane = which == 0 ? g->dW.plane_rows : g->dX.plane_rows;
+                j.lrow0 = g->row0[k]; j.rrow0 = g->row0[k];
+                j.nkb = (p.a1 - p.a0) * g->bpad / kKBlock;
+                j.m = kb[k].G; j.n = kb[k].G;
+                j.el = g->dC.expo + g->row0[k];
+                j.er = (which == 0 ? g->dW.expo : g->dX.expo) + g->row0[k];
+                jsh.push_back(j);
+            }
+        // the tile list is the same for every panel: upload it once
+        if (pi == 0) {
+            rc = upload_schedule(jsh, g->d_jobs_sh, g->d_list_sh, g->tiles_sh, tile);
+            if (rc) return fail(rc);
+        } else {
+            int64_t total = 0;
+            for (auto &j : jsh) {
+                j.tiles_n = (j.n + tile - 1) / tile;
+                j.tile_begin = total;
+                total += job_tiles(j, tile);
+            }
+        }
+        memcpy(g->h_jobs_sh + 2 * g->nk * pi, jsh.data(), sizeof(OzJob) * jsh.size());
+    }
     g->maps_sh[0] = g->dC.map; g->maps_sh[1] = g->dW.map; g->maps_sh[2] = g->dX.map; g->maps_sh[3] = g->dC.map;
     *out = g;
     return HSDLA_OK;
 }
 
 void ozaki_group_set_outputs(OzGroup *g, double2 *const *S, double2 *const *H, const int64_t *ld) {
-    for (int k = 0; k < g->nk; ++k) {
-        g->h_jobs_sh[2 * k].out = S[k];
-        g->h_jobs_sh[2 * k].ldo = ld[k];
-        g->h_jobs_sh[2 * k + 1].out = H[k];
-        g->h_jobs_sh[2 * k + 1].ldo = ld[k];
+    for (int pi = 0; pi < g->panels; ++pi) {
+        OzJob *j = g->h_jobs_sh + 2 * g->nk * pi;
+        for (int k = 0; k < g->nk; ++k) {
+            j[2 * k].out = S[k];
+            j[2 * k].ldo = ld[k];
+            j[2 * k + 1].out = H[k];
+            j[2 * k + 1].ldo = ld[k];
+        }
     }
 }
 
@@ -1635,29 +1692,51 @@ static cudaError_t record(cudaEvent_t ev, cudaStream_t st) {
                                                : cudaEventRecord(ev, st);
 }
 
+// One run: [hoisted: M digits, Z_t = T_t M_t], then per atom panel: C and W digits, the panel's
+// T application (or phase expansion), X digits, the S/H products (accumulating after the first
+// panel).  With several panels the events span the panels' S/H launches and the slicing between
+// them.
 int ozaki_group_run(OzGroup *g, const DevSystem &sys, const KTable &ktab, cudaStream_t st, cudaEvent_t ev0,
                     cudaEvent_t ev1, int *launches) {
     int nl = 0;
-    // C and W = C diag(w) in one pass over C
-    cudaError_t e = slice_launch(g->tC, st);
-    nl += 1;
-    if (e == cudaSuccess && g->hoist) { e = slice_launch(g->tM, st); nl += 1; }
+    cudaError_t e = cudaSuccess;
+    if (g->hoist) {
+        e = slice_launch(g->tM, st);
+        if (e == cudaSuccess)
+            e = launch_prepared(g->maps_t, g->s, g->d_err, g->d_jobs_t, g->n_jobs_t, g->tiles_t, g->d_list_t, nullptr,
+                                st);
+        nl += 2;
+    }
+    // the S/H job tables travel from pinned memory in stream order (a graph replays the copy)
     if (e == cudaSuccess)
-        e = launch_prepared(g->maps_t, g->s, g->d_err, g->d_jobs_t, g->n_jobs_t, g->tiles_t, g->d_list_t, nullptr, st);
-    nl += 1;
-    if (e == cudaSuccess && g->hoist) { e = launch_apply_phase_multi(sys, ktab, st); nl += 1; }
-    if (e == cudaSuccess) e = slice_launch(g->tX, st);
-    nl += 1;
-    // the S/H job table travels from pinned memory in stream order (a graph replays the copy)
-    if (e == cudaSuccess)
-        e = cudaMemcpyAsync(g->d_jobs_sh, g->h_jobs_sh, sizeof(OzJob) * g->n_jobs_sh, cudaMemcpyHostToDevice, st);
-    if (e == cudaSuccess && ev0) e = record(ev0, st);
-    if (e == cudaSuccess)
-        e = g->pair ? launch_pair(g->maps_sh, g->s, g->d_err, g->d_jobs_sh, g->n_jobs_sh, g->tiles_sh, g->d_list_sh,
-                                  g->d_progress, st)
-                    : launch_prepared(g->maps_sh, g->s, g->d_err, g->d_jobs_sh, g->n_jobs_sh, g->tiles_sh,
-                                      g->d_list_sh, g->d_progress, st);
-    nl += 1;
+        e = cudaMemcpyAsync(g->d_jobs_sh, g->h_jobs_sh, sizeof(OzJob) * g->n_jobs_sh * g->panels,
+                            cudaMemcpyHostToDevice, st);
+    for (int pi = 0; pi < g->panels && e == cudaSuccess; ++pi) {
+        const OzPanel &p = g->pan[pi];
+        e = slice_launch(p.tC, st);           // C and W = C diag(w) in one pass over C
+        nl += 1;
+        if (e == cudaSuccess) {
+            if (g->hoist) {
+                KTable kt = ktab;
+                kt.a0 = (int)p.a0;
+                kt.a1 = (int)p.a1;
+                e = launch_apply_phase_multi(sys, kt, st);
+            } else {
+                e = launch_prepared(g->maps_t, g->s, g->d_err, g->d_jobs_t + p.jt_off, p.n_jobs_t, p.tiles_t,
+                                    g->d_list_t + p.lt_off, nullptr, st);
+            }
+            nl += 1;
+        }
+        if (e == cudaSuccess) { e = slice_launch(p.tX, st); nl += 1; }
+        if (e == cudaSuccess && pi == 0 && ev0) e = record(ev0, st);
+        const OzJob *jobs = g->d_jobs_sh + (int64_t)g->n_jobs_sh * pi;
+        if (e == cudaSuccess)
+            e = g->pair ? launch_pair(g->maps_sh, g->s, g->d_err, jobs, g->n_jobs_sh, g->tiles_sh, g->d_list_sh,
+                                      g->d_progress, st)
+                        : launch_prepared(g->maps_sh, g->s, g->d_err, jobs, g->n_jobs_sh, g->tiles_sh, g->d_list_sh,
+                                          g->d_progress, st);
+        nl += 1;
+    }
     if (e == cudaSuccess && ev1) e = record(ev1, st);
     if (launches) *launches = nl;
     if (e != cudaSuccess) { g_oz_err = cudaGetErrorString(e); return HSDLA_ERR_CUDA; }
@@ -1673,7 +1752,7 @@ void ozaki_group_destroy(OzGroup *g) {
 // One k-point through a temporary group (the slice autotuner's probe).
 int64_t ozaki_pipeline_workspace(int s, int64_t twoL, int64_t na, int64_t nt, int64_t G) {
     const std::vector<int64_t> g{G};
-    return ozaki_group_bytes(s, twoL, na, nt, g) + ozaki_group_persist_bytes(s, twoL, na, nt, g) + 2048;
+    return ozaki_group_bytes(s, twoL, na, nt, g, 1, true) + ozaki_group_persist_bytes(s, twoL, na, nt, g, 1) + 2048;
 }
 
 int ozaki_pipeline(OzakiPlan &oz, const OzakiInputs &in, double2 *S, double2 *H, int64_t ldo, void *ws,
@@ -1688,7 +1767,8 @@ int ozaki_pipeline(OzakiPlan &oz, const OzakiInputs &in, double2 *S, double2 *H,
     kb[0].Z = in.Z;
     kb[0].G = in.G;
     OzGroup *g = nullptr;
-    const int64_t scratch = ozaki_group_bytes(oz.num_slices, in.twoL, in.na, in.nt, std::vector<int64_t>{in.G});
+    const int64_t scratch = ozaki_group_bytes(oz.num_slices, in.twoL, in.na, in.nt, std::vector<int64_t>{in.G}, 1,
+                                              d.hoist);
     char *persist = reinterpret_cast<char *>(ws) + (scratch + 1023) / 1024 * 1024;
     int rc = ozaki_group_prepare(oz, d, kb, ws, persist, st, &g);
     if (rc) return rc;

@@ -50,12 +50,17 @@ struct OzGroupDesc {
     const double *w = nullptr;             // S row weights (K)
     const double2 *Tfull = nullptr;        // per-type 2L x 2L blocks
     const int32_t *atom_type = nullptr;    // host [na]
+    int panels = 1;                        // atom panels the contraction index is streamed in
 };
 struct OzGroup;
 // scratch: rewritten by every run (may be shared by the groups of a plan); persist: owned by
 // the group for its lifetime (T digits, job tables, schedules)
-int64_t ozaki_group_bytes(int s, int64_t twoL, int64_t na, int64_t nt, const std::vector<int64_t> &G);
-int64_t ozaki_group_persist_bytes(int s, int64_t twoL, int64_t na, int64_t nt, const std::vector<int64_t> &G);
+// Panels: the atoms split into `panels` contiguous ranges; only one panel's digit planes are
+// resident at a time (the scratch shrinks accordingly), the S/H products accumulate over panels.
+int64_t ozaki_group_bytes(int s, int64_t twoL, int64_t na, int64_t nt, const std::vector<int64_t> &G, int panels,
+                          bool hoist);
+int64_t ozaki_group_persist_bytes(int s, int64_t twoL, int64_t na, int64_t nt, const std::vector<int64_t> &G,
+                                  int panels);
 int ozaki_group_prepare(OzakiPlan &oz, const OzGroupDesc &d, const std::vector<OzKBufs> &kb, void *ws,
                         void *persist, cudaStream_t st, OzGroup **out);
 void ozaki_group_set_outputs(OzGroup *g, double2 *const *S, double2 *const *H, const int64_t *ld);

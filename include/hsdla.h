@@ -114,7 +114,8 @@ typedef struct hsdla_report {
     int32_t num_slices;          /* slices used (Ozaki) */
     int32_t num_kpoints;
     int32_t kernel_launches;     /* kernels launched per execution */
-    int32_t reserved[5];
+    int32_t num_panels;          /* Ozaki: atom panels the contraction was streamed in (1 = resident) */
+    int32_t reserved[4];
 } hsdla_report;
 
 typedef struct hsdla_context hsdla_context;

@@ -49,6 +49,7 @@ def test_groups_of_one_kpoint_match_one_group(ctx, prec, monkeypatch):
     one.execute(o1)
     torch.cuda.synchronize()
     monkeypatch.setenv("HSDLA_WORKSPACE_BUDGET", "1")   # every k-point its own group
+    monkeypatch.setenv("HSDLA_PANELS", "1")             # grouping only: no atom panels
     split = ctx.plan(s, precision=prec, num_slices=11 if prec == "ozaki" else 0)
     o2 = split.alloc_outputs()
     split.execute(o2)
