@@ -44,6 +44,7 @@ WORKLOAD_TEXT = {
     "c1": "c1: 14x14x20 bohr, 32 atoms / 4 types, lmax 8, n_G 3000, 1 k-point",
     "c2": "c2: cubic a=24 bohr, 128 atoms / 8 types, lmax 10, n_G 8000, 1 k-point",
     "c3": "c3: 17.6x17.6x25.2 bohr, 64 atoms / 4 types, lmax 8, 64 k-points (4x4x4), n_G 6000-6600, CUDA graph",
+    "c4": "c4: cubic a=40 bohr, 512 atoms / 16 types, lmax 10, 4 k-points, n_G 19800-20700, CUDA graph",
 }
 PROFILE_SUMMARY = os.path.join(ROOT, "profiles", "oz_pair_c2.md")
 
@@ -276,6 +277,21 @@ def run_ours(args):
         pl64.close()
         del o64
 
+    # ---- oracle check of the first k-point's top-left N x N block: A and B columns depend on their
+    # own G-vector only, so the oracle on the first N G-vectors gives exactly that block of H and S
+    block = None
+    if args.oracle_block > 0 and rank == 0:
+        import oracle
+        nb = min(args.oracle_block, G)
+        sub = synth.KPoint(k=kp.k, g=kp.g[:nb])
+        Hr, Sr = oracle.reference_hs(sys_, sub)
+        Hb = np.tril(H_oz[:nb, :nb].cpu().numpy().T)
+        Sb = np.tril(S_oz[:nb, :nb].cpu().numpy().T)
+        block = {"n": nb}
+        for nm, X, R in (("H", Hb, Hr), ("S", Sb, Sr)):
+            fro, mx = oracle.lower_errors(X, R)
+            block[nm + "_fro"], block[nm + "_max"] = fro, mx
+
     peaks, src = _peaks()
     fp8_peak = 2.0 * peaks["bf16_tflops"]
     dom = float(np.median(dom_ms))
@@ -313,6 +329,10 @@ def run_ours(args):
                 "stage_ms": {"construct_ab": rep["ms_construct_ab"], "tapply": rep["ms_tapply"],
                              "contract": rep["ms_contract"], "dominant": dom},
                 "fp64": fp64, "roofline": roof, "cpu_baseline": cpu, "clocks": clk.summary()}
+        if block is not None:
+            line["oracle_block"] = block
+        if rep.get("num_panels", 1) > 1:
+            line["config"]["atom_panels"] = rep["num_panels"]
         print(json.dumps(line), flush=True)
     ctx.close()
     if ws > 1:
@@ -328,6 +348,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--slices", type=int, default=0, help="Ozaki digit slices (0 = default)")
     ap.add_argument("--ref-sample-ng", type=int, default=1500)
+    ap.add_argument("--oracle-block", type=int, default=0,
+                    help="compare the first k-point's top-left N x N block of H and S with the oracle")
     ap.add_argument("--skip-fp64", action="store_true")
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--workload", default=WORKLOAD, choices=sorted(WORKLOAD_TEXT),
