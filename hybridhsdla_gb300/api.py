@@ -81,7 +81,7 @@ class ReportStruct(ctypes.Structure):
 EXPORTS = ["hsdla_context_create", "hsdla_context_destroy", "hsdla_last_error", "hsdla_set_mem_cap",
            "hsdla_prepare_tmat", "hsdla_create_hs", "hsdla_plan_create", "hsdla_plan_execute",
            "hsdla_plan_workspace_bytes", "hsdla_plan_destroy", "hsdla_plan_construct_ab",
-           "hsdla_zherkx_lower", "hsdla_zherkx_lower_noalloc", "hsdla_contract_ab"]
+           "hsdla_zherkx_lower", "hsdla_zherkx_lower_noalloc", "hsdla_contract_ab", "hsdla_pack_lower"]
 
 _lib = None
 
@@ -129,6 +129,7 @@ def load(build_if_missing: bool = True):
                                     ctypes.POINTER(_cxp), ctypes.POINTER(_cxp), ctypes.POINTER(_cxp), _ip,
                                     ctypes.c_int32, _dp, _cxp, _cxp, ctypes.c_int64, ctypes.POINTER(OptsStruct),
                                     ctypes.POINTER(ReportStruct)]
+    L.hsdla_pack_lower.argtypes = [vp, ctypes.c_int64, vp, ctypes.c_int64, vp, vp]
     L.hsdla_zherkx_lower_noalloc.argtypes = [ctypes.c_int32, ctypes.c_int64, ctypes.c_int64, vp, ctypes.c_int64, vp,
                                              ctypes.c_int64, vp, vp, ctypes.c_int64, vp]
     _lib = L
@@ -318,6 +319,20 @@ class Context:
                                                ctypes.c_void_p(P.data_ptr()), K, ctypes.c_void_p(Q.data_ptr()), K,
                                                ctypes.c_void_p(w.data_ptr()) if w is not None else None,
                                                ctypes.c_void_p(out.data_ptr()), n, st))
+        return out
+
+    def pack_lower(self, M, out=None, stream=None):
+        """Fleur's packed form (``hsdla_pack_lower``) of a device H or S: the lower triangle
+        row by row, element (r, c), c <= r, at r (r + 1) / 2 + c.  ``M`` is the column-major
+        n x n matrix as the library returns it (a torch tensor of shape (n, n) holding
+        ``M[col, row]``).  Returns a complex128 device tensor of n (n + 1) / 2 elements."""
+        import torch
+        n = M.shape[0]
+        if out is None:
+            out = torch.empty(n * (n + 1) // 2, dtype=torch.complex128, device=M.device)
+        st = ctypes.c_void_p(stream.cuda_stream if stream is not None else torch.cuda.current_stream().cuda_stream)
+        self.check(self.lib.hsdla_pack_lower(self.h, n, ctypes.c_void_p(M.data_ptr()), M.stride(0),
+                                             ctypes.c_void_p(out.data_ptr()), st))
         return out
 
 

@@ -90,4 +90,7 @@ constexpr int kFp64Tile = 64;
 int64_t fp64_job_tiles(const Fp64Job &j);
 cudaError_t launch_fp64_jobs(const Fp64Job *d_jobs, int num_jobs, int64_t total_tiles, cudaStream_t st);
 
+// Fleur's packed lower triangle (row by row) of a column-major n x n matrix (device buffers).
+cudaError_t launch_pack_lower(const double2 *M, int64_t ld, int64_t n, double2 *P, cudaStream_t st);
+
 }  // namespace hsdla

@@ -1291,6 +1291,18 @@ int hsdla_create_hs(hsdla_context *ctx, const hsdla_system *s, const hsdla_kpoin
     return rc;
 }
 
+int hsdla_pack_lower(hsdla_context *ctx, int64_t n, const hsdla_cx *M, int64_t ld, hsdla_cx *packed, void *stream) {
+    if (!ctx) return HSDLA_ERR_ARG;
+    if (n < 0 || ld < std::max<int64_t>(n, 1) || (n > 0 && (!M || !packed)))
+        return set_err(ctx, HSDLA_ERR_ARG, "pack_lower: n < 0, ld < n or a NULL buffer");
+    if (n == 0) return HSDLA_OK;
+    CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+    const cudaError_t e = launch_pack_lower(reinterpret_cast<const double2 *>(M), ld, n,
+                                            reinterpret_cast<double2 *>(packed), (cudaStream_t)stream);
+    if (e != cudaSuccess) return set_err(ctx, HSDLA_ERR_CUDA, "pack_lower: %s", cudaGetErrorString(e));
+    return HSDLA_OK;
+}
+
 int hsdla_zherkx_lower(hsdla_context *ctx, int32_t precision, int32_t num_slices, int64_t n, int64_t k,
                        const hsdla_cx *dP, int64_t ldp, const hsdla_cx *dQ, int64_t ldq, const double *dw,
                        hsdla_cx *dOut, int64_t ldo, void *stream) {

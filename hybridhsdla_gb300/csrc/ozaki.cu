@@ -504,12 +504,6 @@ __device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.comm
 __device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;\n" ::: "memory"); }
 __device__ __forceinline__ void bulk_wait_read_1() { asm volatile("cp.async.bulk.wait_group.read 1;\n" ::: "memory"); }
 __device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory"); }
-// No "memory" clobber: nothing in the kernel reads the output, and a clobber would pin every
-// later load (column exponents, job fields) behind each reduction.  Volatile asm statements keep
-// their order among themselves, so successive reductions of an element stay in program order.
-__device__ __forceinline__ void red_add_f64(double *p, double v) {
-    asm volatile("red.relaxed.gpu.global.add.f64 [%0], %1;\n" ::"l"(p), "d"(v));
-}
 // x * 2^k as a double for an FP32 accumulator x (an exact integer, |x| <= 2^24), built with
 // integer operations: GB300's FP64 pipe is a small fraction of its integer pipes, and a drain
 // converts 2^16 values per CTA.  (f & 0x7fffffff) >> 3 puts the FP32 exponent and the top 20

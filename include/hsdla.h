@@ -186,6 +186,15 @@ int hsdla_zherkx_lower(hsdla_context *ctx, int32_t precision, int32_t num_slices
                        const hsdla_cx *dP, int64_t ldp, const hsdla_cx *dQ, int64_t ldq,
                        const double *dw, hsdla_cx *dOut, int64_t ldo, void *stream);
 
+/* Hand-off to an eigensolver in Fleur's packed form: the lower triangle of the column-major
+ * n x n DEVICE matrix M (leading dimension ld >= n, e.g. H or S from hsdla_plan_execute) written
+ * row by row into the DEVICE array packed of n (n + 1) / 2 elements, element (r, c), c <= r, at
+ * r (r + 1) / 2 + c.  That is the layout of the H and S Fleur writes per k-point
+ * (fleur/src/binmat.f90:194-219) and the one the reference's checker unpacks
+ * (flapw_opt/tests/flapw_verify.py:68-82).  Asynchronous on `stream` (NULL: the legacy default
+ * stream); M and packed must not overlap. */
+int hsdla_pack_lower(hsdla_context *ctx, int64_t n, const hsdla_cx *M, int64_t ld, hsdla_cx *packed, void *stream);
+
 /* Allocation-free Ozaki form of hsdla_zherkx_lower (HSDLA_PREC_OZAKI_FP8), for callers that
  * cannot allocate device memory: code inside another framework's memory pool or under a
  * fixed memory budget, plug-ins that may only touch the buffers they are handed, processes
