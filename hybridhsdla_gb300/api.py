@@ -81,7 +81,8 @@ class ReportStruct(ctypes.Structure):
 EXPORTS = ["hsdla_context_create", "hsdla_context_destroy", "hsdla_last_error", "hsdla_set_mem_cap",
            "hsdla_prepare_tmat", "hsdla_create_hs", "hsdla_plan_create", "hsdla_plan_execute",
            "hsdla_plan_workspace_bytes", "hsdla_plan_destroy", "hsdla_plan_construct_ab",
-           "hsdla_zherkx_lower", "hsdla_zherkx_lower_noalloc", "hsdla_contract_ab", "hsdla_pack_lower"]
+           "hsdla_zherkx_lower", "hsdla_zherkx_lower_noalloc", "hsdla_contract_ab", "hsdla_pack_lower",
+           "hsdla_selftest_wait_timeout"]
 
 _lib = None
 
@@ -130,6 +131,7 @@ def load(build_if_missing: bool = True):
                                     ctypes.c_int32, _dp, _cxp, _cxp, ctypes.c_int64, ctypes.POINTER(OptsStruct),
                                     ctypes.POINTER(ReportStruct)]
     L.hsdla_pack_lower.argtypes = [vp, ctypes.c_int64, vp, ctypes.c_int64, vp, vp]
+    L.hsdla_selftest_wait_timeout.argtypes = [vp, ctypes.c_int32, ctypes.c_int64]
     L.hsdla_zherkx_lower_noalloc.argtypes = [ctypes.c_int32, ctypes.c_int64, ctypes.c_int64, vp, ctypes.c_int64, vp,
                                              ctypes.c_int64, vp, vp, ctypes.c_int64, vp]
     _lib = L

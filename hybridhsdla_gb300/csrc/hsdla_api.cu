@@ -1291,6 +1291,18 @@ int hsdla_create_hs(hsdla_context *ctx, const hsdla_system *s, const hsdla_kpoin
     return rc;
 }
 
+int hsdla_selftest_wait_timeout(hsdla_context *ctx, int32_t which, int64_t budget_cycles) {
+    if (!ctx) return HSDLA_ERR_ARG;
+    CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+    OzakiPlan oz{};
+    int rc = ozaki_plan_init(oz, kOzDefaultSlices, 1e-13);
+    if (rc) return set_err(ctx, rc, "self-test set-up failed: %s", ozaki_last_error());
+    rc = ozaki_wait_selftest(oz, which, budget_cycles, ctx->stream);
+    ozaki_plan_release(oz);
+    if (rc) return set_err(ctx, rc, "%s", ozaki_last_error());
+    return HSDLA_OK;
+}
+
 int hsdla_pack_lower(hsdla_context *ctx, int64_t n, const hsdla_cx *M, int64_t ld, hsdla_cx *packed, void *stream) {
     if (!ctx) return HSDLA_ERR_ARG;
     if (n < 0 || ld < std::max<int64_t>(n, 1) || (n > 0 && (!M || !packed)))

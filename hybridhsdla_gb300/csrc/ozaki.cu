@@ -62,6 +62,7 @@ constexpr int kExactTerms = 1 << 24;                // FP32 exact-integer bound
 constexpr int kSyncEvery = 64;                      // stages per lockstep epoch (cooperative launches)
 constexpr int kRetired = 0x7F7F7F7F;                // progress value of a CTA that has no work left
 constexpr int kErrWords = 8;                        // error word + diagnostics of the first expired wait
+constexpr int kErrAlloc = 16;                       // error words + the wait self-test's progress slots
 
 struct OzJob {
     int32_t lmap, rmap;        // tensor-map index (0..3) of the left / right digit operand
@@ -105,12 +106,12 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
 // Bounded wait.  Returns false (and raises the CTA abort flag) when the budget expires
 // or another role already aborted.
 __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, volatile int *abort_flag, int *err,
-                                          int where) {
+                                          int where, long long budget = kWaitCycles) {
     if (mbar_try_wait(bar, parity)) return true;
     const long long t0 = clock64();
     while (!mbar_try_wait(bar, parity)) {
         if (*abort_flag) return false;
-        if (clock64() - t0 > kWaitCycles) {
+        if (clock64() - t0 > budget) {
             *abort_flag = 1;
             atomicCAS(err, 0, kDevTimeout * 16 + where);
             return false;
@@ -225,7 +226,7 @@ __host__ __device__ __forceinline__ int64_t chunk_kblocks(int pairs) {
 // resident in L2 (left to themselves, CTAs drift apart by far more than L2 can hold).
 // Bounded: on expiry the CTA raises the abort flag and records the error word.
 __device__ bool grid_lockstep(int *progress, int n, int epoch, volatile int *abort_flag, int *err, int slot,
-                              int slack = 1) {
+                              int slack = 1, long long budget = kWaitCycles) {
     atomicExch(progress + slot, epoch);
     const long long t0 = clock64();
     while (true) {
@@ -236,7 +237,7 @@ __device__ bool grid_lockstep(int *progress, int n, int epoch, volatile int *abo
         }
         if (mn >= epoch - slack) return true;
         if (*abort_flag) return false;
-        if (clock64() - t0 > kWaitCycles) {
+        if (clock64() - t0 > budget) {
             *abort_flag = 1;
             atomicCAS(err, 0, kDevTimeout * 16 + 5);
             return false;
@@ -1221,6 +1222,64 @@ int launch_gemm(std::vector<OzJob> &jobs, const CUtensorMap *maps, int s, int *d
     return HSDLA_OK;
 }
 
+// ------------------------------------------------------------ wait self-test
+// Exercises the bounded-wait and abort path of the product kernels on a condition that never
+// comes true, with a short budget: the CTA holds TMEM as the product kernels do, one thread
+// waits on an mbarrier nothing arrives on (which = 0) or on a lockstep slot that never advances
+// (which = 1), the wait records the error word and raises the abort flag, and the CTA frees TMEM
+// and returns.  Nothing faults, traps or hangs.
+__global__ void __launch_bounds__(64, 1) oz_wait_probe_kernel(int *err, int *progress, long long budget, int which) {
+    __shared__ uint64_t bar;
+    __shared__ uint32_t tmem_sh;
+    __shared__ volatile int abort_flag;
+    const int warp = threadIdx.x >> 5;
+    if (threadIdx.x == 0) {
+        mbar_init(&bar, 1);
+        abort_flag = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    if (warp == 1) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 32;\n" ::"r"(smem_u32(&tmem_sh))
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (threadIdx.x == 0) {
+        if (which == 0) mbar_wait(&bar, 0, &abort_flag, err, 7, budget);
+        else grid_lockstep(progress, 4, 3, &abort_flag, err, 0, 1, budget);
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 1) {
+        tc_fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 32;\n" ::"r"(tmem_sh) : "memory");
+    }
+}
+
+}  // namespace
+
+int ozaki_wait_selftest(OzakiPlan &oz, int which, long long budget_cycles, cudaStream_t st) {
+    if (!oz.d_error) { g_oz_err = "Ozaki plan not initialised"; return HSDLA_ERR_ARG; }
+    if (which < 0 || which > 1 || budget_cycles <= 0 || budget_cycles > kWaitCycles) {
+        g_oz_err = "wait self-test: which must be 0 or 1, budget in (0, 2e9] cycles";
+        return HSDLA_ERR_ARG;
+    }
+    // progress slots for which = 1: slot 0 is this CTA, slots 1..3 stay at epoch 0
+    int *progress = oz.d_error + 8;
+    cudaError_t e = cudaMemsetAsync(progress, 0, 4 * sizeof(int), st);
+    if (e == cudaSuccess) {
+        oz_wait_probe_kernel<<<1, 64, 0, st>>>(oz.d_error, progress, budget_cycles, which);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) { g_oz_err = cudaGetErrorString(e); return HSDLA_ERR_CUDA; }
+    return ozaki_check_device_error(oz);
+}
+
+namespace {
+
 }  // namespace
 
 // ==================================================================== API
@@ -1230,8 +1289,8 @@ int ozaki_plan_init(OzakiPlan &oz, int num_slices, double target) {
     oz.num_slices = num_slices;
     oz.target = target;
     if (!oz.d_error) {
-        if (cudaMalloc(&oz.d_error, kErrWords * sizeof(int)) != cudaSuccess) { g_oz_err = "cudaMalloc"; return HSDLA_ERR_NOMEM; }
-        cudaMemset(oz.d_error, 0, kErrWords * sizeof(int));
+        if (cudaMalloc(&oz.d_error, kErrAlloc * sizeof(int)) != cudaSuccess) { g_oz_err = "cudaMalloc"; return HSDLA_ERR_NOMEM; }
+        cudaMemset(oz.d_error, 0, kErrAlloc * sizeof(int));
     }
     return HSDLA_OK;
 }

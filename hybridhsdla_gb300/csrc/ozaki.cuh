@@ -80,6 +80,9 @@ int ozaki_pipeline(OzakiPlan &oz, const OzakiInputs &in, double2 *S, double2 *H,
 int ozaki_herkx(OzakiPlan &oz, const double2 *P, int64_t ldp, const double2 *Q, int64_t ldq, const double *w,
                 int64_t K, int64_t n, double2 *out, int64_t ldo, void *ws, cudaStream_t st, int *launches);
 int ozaki_check_device_error(OzakiPlan &oz);
+// Lets one bounded wait expire on purpose (0: an mbarrier nothing arrives on, 1: a lockstep slot
+// that never advances) after budget_cycles; returns the status the host reads (HSDLA_ERR_TIMEOUT).
+int ozaki_wait_selftest(OzakiPlan &oz, int which, long long budget_cycles, cudaStream_t st);
 const char *ozaki_last_error();
 
 }  // namespace hsdla

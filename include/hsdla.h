@@ -195,6 +195,14 @@ int hsdla_zherkx_lower(hsdla_context *ctx, int32_t precision, int32_t num_slices
  * stream); M and packed must not overlap. */
 int hsdla_pack_lower(hsdla_context *ctx, int64_t n, const hsdla_cx *M, int64_t ld, hsdla_cx *packed, void *stream);
 
+/* Failure-detection self-test (no counterpart in the reference): runs a small kernel that holds
+ * TMEM like the contraction kernels and lets one of their bounded waits expire on a condition
+ * that never comes true -- which = 0: an mbarrier nothing arrives on; which = 1: a grid-lockstep
+ * slot that never advances -- after budget_cycles (1 .. 2e9 SM cycles).  The kernel records the
+ * error word, frees TMEM and returns; the call returns HSDLA_ERR_TIMEOUT with the expired wait in
+ * hsdla_last_error, and the context stays usable.  Nothing faults, traps or hangs. */
+int hsdla_selftest_wait_timeout(hsdla_context *ctx, int32_t which, int64_t budget_cycles);
+
 /* Allocation-free Ozaki form of hsdla_zherkx_lower (HSDLA_PREC_OZAKI_FP8), for callers that
  * cannot allocate device memory: code inside another framework's memory pool or under a
  * fixed memory budget, plug-ins that may only touch the buffers they are handed, processes
