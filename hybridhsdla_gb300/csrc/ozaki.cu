@@ -1509,18 +1509,24 @@ cudaError_t launch_prepared(const CUtensorMap *maps, int s, int *d_err, const Oz
 // Run-time scratch of a group (digit planes and exponents, rewritten by every run; groups of a
 // plan share it) and its persistent part (T digits, job tables, tile schedules, lockstep slots).
 static int64_t panel_atoms(int64_t na, int panels) { return (na + panels - 1) / panels; }
+// Stride of one atom's 2L rows along the contraction index of the digit planes: 16 bytes keeps
+// every atom's block on a TMA boundary (the T application starts its loads there).  A T job reads
+// ceil(2L / 128) k-blocks from that start; the rows past 2L it covers (padding and the next atoms)
+// meet T digits that are exactly zero, and reads past the operand's extent are zero-filled.
+static int64_t atom_stride(int64_t twoL) { return round_up(twoL, 16); }
 
 int64_t ozaki_group_bytes(int s, int64_t twoL, int64_t na, int64_t nt, const std::vector<int64_t> &G, int panels,
                           bool hoist) {
-    const int64_t bpad = round_up(twoL, kKBlock), rows = group_rows(G);
-    const int64_t Kp = bpad * panel_atoms(na, panels), Kx = hoist ? std::max(Kp, bpad * nt) : Kp;
+    const int64_t bpad = atom_stride(twoL), rows = group_rows(G);
+    const int64_t Kp = round_up(bpad * panel_atoms(na, panels), kKBlock);
+    const int64_t Kx = hoist ? std::max(Kp, round_up(bpad * nt, kKBlock)) : Kp;
     auto dig = [&](int64_t K) { return round_up(2 * s * rows * (K + pitch_pad()), 1024) + round_up(4 * rows, 1024); };
     return 2 * dig(Kp) + dig(Kx) + 4096;
 }
 
 int64_t ozaki_group_persist_bytes(int s, int64_t twoL, int64_t na, int64_t nt, const std::vector<int64_t> &G,
                                   int panels) {
-    const int64_t bpad = round_up(twoL, kKBlock);
+    const int64_t bpad = round_up(atom_stride(twoL), kKBlock);    // T operand: one atom's rows per plane row
     const int64_t nk = (int64_t)G.size();
     int64_t tiles_t = 0, tiles_sh = 0;
     for (int64_t g : G) {
@@ -1544,7 +1550,8 @@ int ozaki_group_prepare(OzakiPlan &oz, const OzGroupDesc &d, const std::vector<O
     g->hoist = d.hoist;
     g->twoL = d.twoL; g->na = d.na; g->nt = d.nt;
     g->K = d.twoL * d.na;
-    g->bpad = round_up(d.twoL, kKBlock);
+    g->bpad = atom_stride(d.twoL);
+    const int64_t tkb = (d.twoL + kKBlock - 1) / kKBlock;      // k-blocks of one T application
     g->kb = kb;
     g->d_err = oz.d_error;
     // atom panels: equal sizes but the last
@@ -1571,15 +1578,15 @@ int ozaki_group_prepare(OzakiPlan &oz, const OzGroupDesc &d, const std::vector<O
         o.digits = ar.take<uint8_t>(2 * s * o.plane_rows * o.pitch);
         o.expo = ar.take<int32_t>(o.plane_rows);
     };
-    const int64_t Kp = g->bpad * pa;
+    const int64_t Kp = round_up(g->bpad * pa, kKBlock), Km = round_up(g->bpad * d.nt, kKBlock);
     carve_rows(g->dC, Kp);
     carve_rows(g->dW, Kp);
-    carve_rows(g->dX, d.hoist ? std::max(Kp, g->bpad * d.nt) : Kp);
-    carve_operand(keep, g->dT, s, d.nt * d.twoL, g->bpad);
+    carve_rows(g->dX, d.hoist ? std::max(Kp, Km) : Kp);
+    carve_operand(keep, g->dT, s, d.nt * d.twoL, tkb * kKBlock);
     // the M digits (per-type rows, K = bpad nt) borrow the X digit region: they are consumed by the
     // T application, which runs before any panel's X is sliced
     g->dM.plane_rows = g->rows;
-    g->dM.Kpad = g->bpad * d.nt;
+    g->dM.Kpad = Km;
     g->dM.pitch = g->dM.Kpad + pitch_pad();
     g->dM.digits = g->dX.digits;
     g->dM.expo = g->dX.expo;
@@ -1616,14 +1623,15 @@ int ozaki_group_prepare(OzakiPlan &oz, const OzGroupDesc &d, const std::vector<O
         return t;
     };
     for (OzPanel &p : g->pan) {
-        const int64_t off = p.a0 * d.twoL, Kin = (p.a1 - p.a0) * d.twoL, kpad = (p.a1 - p.a0) * g->bpad;
+        const int64_t off = p.a0 * d.twoL, Kin = (p.a1 - p.a0) * d.twoL;
+        const int64_t kpad = round_up((p.a1 - p.a0) * g->bpad, kKBlock);
         p.tC = table(g->dC, g->K, nullptr, off, Kin, kpad, 0);
         p.tC.v2 = d.w + off;
         p.tC.digits2 = g->dW.digits;
         p.tC.expo2 = g->dW.expo;
         p.tX = table(g->dX, g->K, nullptr, off, Kin, kpad, 0);
     }
-    if (d.hoist) g->tM = table(g->dM, d.twoL * d.nt, nullptr, 0, d.twoL * d.nt, g->bpad * d.nt, 1);
+    if (d.hoist) g->tM = table(g->dM, d.twoL * d.nt, nullptr, 0, d.twoL * d.nt, Km, 1);
     // T digits once: they do not change between runs
     cudaError_t e = slice(d.Tfull, d.twoL, nullptr, d.twoL, d.nt * d.twoL, d.twoL, g->bpad, s, g->dT, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
@@ -1645,7 +1653,7 @@ int ozaki_group_prepare(OzakiPlan &oz, const OzGroupDesc &d, const std::vector<O
                 j.lplane = g->dT.plane_rows; j.rplane = g->dM.plane_rows;
                 j.lrow0 = t * d.twoL; j.rrow0 = g->row0[k];
                 j.rk0 = t * g->bpad;
-                j.nkb = g->bpad / kKBlock;
+                j.nkb = tkb;
                 j.m = d.twoL; j.n = kb[k].G;
                 j.out = kb[k].Z + d.twoL * t; j.ldo = d.twoL * d.nt;
                 j.el = g->dT.expo + t * d.twoL; j.er = g->dM.expo + g->row0[k];
@@ -1667,7 +1675,7 @@ int ozaki_group_prepare(OzakiPlan &oz, const OzGroupDesc &d, const std::vector<O
                     j.lplane = g->dT.plane_rows; j.rplane = g->dC.plane_rows;
                     j.lrow0 = t * d.twoL; j.rrow0 = g->row0[k];
                     j.rk0 = (a - p.a0) * g->bpad;
-                    j.nkb = g->bpad / kKBlock;
+                    j.nkb = tkb;
                     j.m = d.twoL; j.n = kb[k].G;
                     j.out = kb[k].CX + d.twoL * a; j.ldo = g->K;
                     j.el = g->dT.expo + t * d.twoL; j.er = g->dC.expo + g->row0[k];
@@ -1699,7 +1707,7 @@ int ozaki_group_prepare(OzakiPlan &oz, const OzGroupDesc &d, const std::vector<O
                 j.accum = pi > 0;
                 j.lplane = g->dC.plane_rows; j.rplane = which == 0 ? g->dW.plane_rows : g->dX.plane_rows;
                 j.lrow0 = g->row0[k]; j.rrow0 = g->row0[k];
-                j.nkb = (p.a1 - p.a0) * g->bpad / kKBlock;
+                j.nkb = round_up((p.a1 - p.a0) * g->bpad, kKBlock) / kKBlock;
                 j.m = kb[k].G; j.n = kb[k].G;
                 j.el = g->dC.expo + g->row0[k];
                 j.er = (which == 0 ? g->dW.expo : g->dX.expo) + g->row0[k];
