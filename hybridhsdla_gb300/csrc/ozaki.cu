@@ -245,6 +245,23 @@ __device__ bool grid_lockstep(int *progress, int n, int epoch, volatile int *abo
     }
 }
 
+// x * 2^k as a double for an FP32 accumulator x (an exact integer, |x| <= 2^24), built with
+// integer operations: GB300's FP64 pipe is a small fraction of its integer pipes, and a drain
+// converts 2^16 values per CTA.  (f & 0x7fffffff) >> 3 puts the FP32 exponent and the top 20
+// mantissa bits exactly where the FP64 high word keeps them, so rebasing the exponent is one
+// add of (1023 - 127 + k) << 20; the low word takes the last 3 mantissa bits.  Valid for
+// k in [kPow2Lo, kPow2Hi] (the result stays normal); pow2_ok() checks that once per column.
+constexpr int kPow2Lo = -1022, kPow2Hi = 999;
+__device__ __forceinline__ bool pow2_ok(int k) { return k >= kPow2Lo && k <= kPow2Hi; }
+__device__ __forceinline__ double f32_pow2_to_f64_fast(uint32_t f, uint32_t ebias) {
+    const uint32_t a = f & 0x7fffffffu;
+    const uint32_t hi = (f & 0x80000000u) | ((a >> 3) + ebias);
+    const uint32_t lo = f << 29;
+    return a ? __hiloint2double((int)hi, (int)lo) : 0.0;
+}
+__device__ __noinline__ double f32_pow2_to_f64_slow(uint32_t f, int k) { return ldexp((double)__uint_as_float(f), k); }
+__device__ __forceinline__ uint32_t pow2_ebias(int k) { return (uint32_t)(1023 - 127 + k) << 20; }
+
 // Drain 32 accumulator columns of one output row: out = (out +) x 2^(kb + e_col) with kb =
 // 2 - 5t + e_row (a plain store on the first unit of a tile).  Every unit carries its full scale,
 // so an output that already holds an earlier panel's sum is accumulated correctly.  Loads are
@@ -266,10 +283,17 @@ __device__ __forceinline__ void drain32(const OzJob &j, int64_t row, int64_t col
         for (int cc = 0; cc < kDrainBatch; ++cc) {
             const int64_t col = col0 + h + cc;
             if (col >= j.n || (j.lower && row < col)) continue;
-            const double sc = ldexp(1.0, kb + j.er[col]);
-            const double re = (double)__uint_as_float(vre[h + cc]) * sc + o[cc].x;
-            const double im = (double)__uint_as_float(vim[h + cc]) * sc + o[cc].y;
-            j.out[row + j.ldo * col] = make_double2(re, im);
+            const int k = kb + j.er[col];
+            double re, im;
+            if (pow2_ok(k)) {
+                const uint32_t eb = pow2_ebias(k);
+                re = f32_pow2_to_f64_fast(vre[h + cc], eb);
+                im = f32_pow2_to_f64_fast(vim[h + cc], eb);
+            } else {
+                re = f32_pow2_to_f64_slow(vre[h + cc], k);
+                im = f32_pow2_to_f64_slow(vim[h + cc], k);
+            }
+            j.out[row + j.ldo * col] = make_double2(re + o[cc].x, im + o[cc].y);
         }
     }
 }
@@ -505,22 +529,6 @@ __device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.comm
 __device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;\n" ::: "memory"); }
 __device__ __forceinline__ void bulk_wait_read_1() { asm volatile("cp.async.bulk.wait_group.read 1;\n" ::: "memory"); }
 __device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory"); }
-// x * 2^k as a double for an FP32 accumulator x (an exact integer, |x| <= 2^24), built with
-// integer operations: GB300's FP64 pipe is a small fraction of its integer pipes, and a drain
-// converts 2^16 values per CTA.  (f & 0x7fffffff) >> 3 puts the FP32 exponent and the top 20
-// mantissa bits exactly where the FP64 high word keeps them, so rebasing the exponent is one
-// add of (1023 - 127 + k) << 20; the low word takes the last 3 mantissa bits.  Valid for
-// k in [kPow2Lo, kPow2Hi] (the result stays normal); pow2_ok() checks that once per column.
-constexpr int kPow2Lo = -1022, kPow2Hi = 999;
-__device__ __forceinline__ bool pow2_ok(int k) { return k >= kPow2Lo && k <= kPow2Hi; }
-__device__ __forceinline__ double f32_pow2_to_f64_fast(uint32_t f, uint32_t ebias) {
-    const uint32_t a = f & 0x7fffffffu;
-    const uint32_t hi = (f & 0x80000000u) | ((a >> 3) + ebias);
-    const uint32_t lo = f << 29;
-    return a ? __hiloint2double((int)hi, (int)lo) : 0.0;
-}
-__device__ __noinline__ double f32_pow2_to_f64_slow(uint32_t f, int k) { return ldexp((double)__uint_as_float(f), k); }
-__device__ __forceinline__ uint32_t pow2_ebias(int k) { return (uint32_t)(1023 - 127 + k) << 20; }
 
 __device__ __forceinline__ uint32_t cluster_rank() {
     uint32_t r;
@@ -889,30 +897,39 @@ __device__ __forceinline__ uint32_t pack4_e4m3(int d0, int d1, int d2, int d3) {
     return lo | (hi << 16);
 }
 
-// plane i (0 = most significant) of U = X + B
-__device__ __forceinline__ int digit_of(long long U, int i, int s) {
-    if (i == 0) return (int)(U >> (5 * (s - 1)));
-    return (int)(((unsigned long long)U >> (5 * (s - 1 - i))) & 31ull) - 16;
-}
-
-// digit planes 2i + part (part 0 = real, 1 = imaginary) of 8 consecutive contraction bytes
-__device__ __forceinline__ void write_part(const long long (&x)[kSliceVec], int part, int s, uint8_t *row,
-                                          int64_t plane) {
+// The planes of U = X + B from the least significant: plane i (0 = most significant) holds
+// ((U >> 5 (s-1-i)) & 31) - 16 for i >= 1, and the top plane the rest, U >> 5 (s-1) in
+// [-16, 16].  A running arithmetic shift by 5 leaves each field in the low bits in turn (the low
+// bits are the same for arithmetic and logical shifts).
+template <int kVec>
+__device__ __forceinline__ void write_part(const long long (&x)[kVec], int part, int s, uint8_t *row, int64_t plane) {
+    long long u[kVec];
 #pragma unroll
-    for (int i = 0; i < kOzMaxSlices; ++i) {
-        if (i >= s) break;
-        int d[kSliceVec];
+    for (int v = 0; v < kVec; ++v) u[v] = x[v];
 #pragma unroll
-        for (int u = 0; u < kSliceVec; ++u) d[u] = digit_of(x[u], i, s);
-        *reinterpret_cast<uint2 *>(row + (int64_t)(2 * i + part) * plane) =
-            make_uint2(pack4_e4m3(d[0], d[1], d[2], d[3]), pack4_e4m3(d[4], d[5], d[6], d[7]));
+    for (int step = 0; step < kOzMaxSlices; ++step) {
+        if (step >= s) break;
+        const int i = s - 1 - step;
+        int d[kVec];
+#pragma unroll
+        for (int v = 0; v < kVec; ++v) {
+            d[v] = i == 0 ? (int)u[v] : (int)(u[v] & 31) - 16;
+            u[v] >>= 5;
+        }
+        uint8_t *dst = row + (int64_t)(2 * i + part) * plane;
+        if (kVec == 8)
+            *reinterpret_cast<uint2 *>(dst) =
+                make_uint2(pack4_e4m3(d[0], d[1], d[2], d[3]), pack4_e4m3(d[4 % kVec], d[5 % kVec], d[6 % kVec], d[7 % kVec]));
+        else
+            *reinterpret_cast<uint32_t *>(dst) = pack4_e4m3(d[0], d[1], d[2], d[3]);
     }
 }
 
-__device__ __forceinline__ void write_planes(const long long (&ur)[kSliceVec], const long long (&ui)[kSliceVec], int s,
+template <int kVec>
+__device__ __forceinline__ void write_planes(const long long (&ur)[kVec], const long long (&ui)[kVec], int s,
                                              uint8_t *row, int64_t plane) {
-    write_part(ur, 0, s, row, plane);
-    write_part(ui, 1, s, row, plane);
+    write_part<kVec>(ur, 0, s, row, plane);
+    write_part<kVec>(ui, 1, s, row, plane);
 }
 
 __device__ __forceinline__ double block_max(double m, double *red) {
@@ -924,8 +941,59 @@ __device__ __forceinline__ double block_max(double m, double *red) {
     return r;
 }
 
+// Integer-pipe helpers of the slicing (GB300's FP64 pipe runs ~1/64 of its integer rate).
+// |x| as an ordered integer: for finite doubles the bit pattern of |x| orders like |x|.
+__device__ __forceinline__ unsigned long long abs_bits(double x) {
+    return (unsigned long long)__double_as_longlong(x) & 0x7fffffffffffffffull;
+}
+// rint(x 2^k), round half to even, exactly as __double2ll_rn(x * 2^k) for |x 2^k| < 2^62: the
+// mantissa shifted by the exponent, with the round bit and the sticky remainder.
+__device__ __forceinline__ long long rint_pow2(double x, int k) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const int E = (int)((b >> 52) & 0x7ff);
+    const unsigned long long mant = b & 0xfffffffffffffull;
+    const unsigned long long m = E ? (mant | (1ull << 52)) : mant;
+    const int sh = 1075 - (E ? E : 1) - k;          // |x 2^k| = m 2^-sh
+    unsigned long long q;
+    if (sh <= 0) {
+        q = m << (-sh);
+    } else if (sh >= 54) {
+        q = 0;                                      // m 2^-sh < 1/2
+    } else {
+        q = m >> sh;
+        const unsigned long long rem = m & ((1ull << sh) - 1), half = 1ull << (sh - 1);
+        q += (rem > half) | ((rem == half) & (q & 1ull));
+    }
+    return (b >> 63) ? -(long long)q : (long long)q;
+}
+// v 2^k by an exponent add (v normal and the result normal), else ldexp
+__device__ __forceinline__ double scale_pow2(double v, int k) {
+    const long long b = __double_as_longlong(v);
+    const int E = (int)((b >> 52) & 0x7ff);
+    if (E > 0 && E + k > 0 && E + k < 2047) return __longlong_as_double(b + ((long long)k << 52));
+    return ldexp(v, k);
+}
+
+// the weighted operand's digits of one chunk (kept out of line: inlined next to the first
+// operand's, the compiler interleaves the two and spills)
+template <int kV>
+__device__ __noinline__ void weighted_chunk(const double2 *zc, const double *vv, int nv, int kw, long long B, int s,
+                                            uint8_t *row, int64_t plane) {
+    long long xr[kV], xi[kV];
+#pragma unroll
+    for (int u = 0; u < kV; ++u) {
+        const double2 z = u < nv ? zc[u] : make_double2(0.0, 0.0);
+        const double sc = u < nv ? scale_pow2(vv[u], kw) : 0.0;
+        xr[u] = B + rint_pow2(z.x * sc, 0);
+        xi[u] = B + rint_pow2(z.y * sc, 0);
+    }
+    write_planes<kV>(xr, xi, s, row, plane);
+}
+
 template <bool kDual>
 __global__ void __launch_bounds__(kSliceThreads, 1) oz_slice_kernel(const __grid_constant__ SliceTab tab) {
+    // values per thread and step of the digit pass (the dual pass keeps two operands' state)
+    constexpr int kV = kDual ? 4 : kSliceVec;
     const int64_t r = blockIdx.x;           // plane row
     int k = 0;
     while (k + 1 < tab.nk && tab.e[k + 1].row0 <= r) ++k;
@@ -937,21 +1005,30 @@ __global__ void __launch_bounds__(kSliceThreads, 1) oz_slice_kernel(const __grid
     const int64_t pitch = tab.pitch, plane_rows = tab.plane_rows;
     const int s = tab.s;
     __shared__ double red[2][kSliceThreads / 32];
-    // pass 1: column max of max(|re|, |im|) (times the row weight)
-    double mx = 0.0, mx2 = 0.0;
+    // pass 1: column max of max(|re|, |im|) (times the row weight; the only FP64 multiply here)
+    // Each thread reads 8 consecutive values per step (all loads of a step in flight together):
+    // one value per thread and step kept too few bytes in flight to cover the memory latency.
+    unsigned long long mx = 0, mx2 = 0;
     if (live) {
-        for (int kk = threadIdx.x; kk < Kin; kk += kSliceThreads) {
-            const double2 z = Zc[kk];
-            const double a = fmax(fabs(z.x), fabs(z.y));
-            mx = fmax(mx, v ? a * v[kk] : a);
-            if (kDual) mx2 = fmax(mx2, a * v2[kk]);
+        for (int k0 = threadIdx.x * kSliceVec; k0 < Kin; k0 += kSliceThreads * kSliceVec) {
+            double2 z[kSliceVec];
+#pragma unroll
+            for (int u = 0; u < kSliceVec; ++u) z[u] = k0 + u < Kin ? Zc[k0 + u] : make_double2(0.0, 0.0);
+#pragma unroll
+            for (int u = 0; u < kSliceVec; ++u) {
+                const unsigned long long a = max(abs_bits(z[u].x), abs_bits(z[u].y));
+                if (k0 + u < Kin) {
+                    mx = max(mx, v ? abs_bits(__longlong_as_double((long long)a) * v[k0 + u]) : a);
+                    if (kDual) mx2 = max(mx2, abs_bits(__longlong_as_double((long long)a) * v2[k0 + u]));
+                }
+            }
         }
     }
     int e = 0, e2 = 0;
-    const double m = block_max(mx, red[0]);
+    const double m = block_max(__longlong_as_double((long long)mx), red[0]);
     if (m > 0.0) frexp(m, &e);              // m < 2^e
     if (kDual) {
-        const double m2 = block_max(mx2, red[1]);
+        const double m2 = block_max(__longlong_as_double((long long)mx2), red[1]);
         if (m2 > 0.0) frexp(m2, &e2);
     }
     if (threadIdx.x == 0) {
@@ -959,37 +1036,33 @@ __global__ void __launch_bounds__(kSliceThreads, 1) oz_slice_kernel(const __grid
         if (kDual) tab.expo2[r] = e2;
     }
     const int top = 5 * s - 1;              // X = rint(z 2^(5s-1)), |z| < 1
-    const double base = ldexp(1.0, top - e), base2 = ldexp(1.0, top - e2);
+    const int kx = top - e, kw = top - e2;
     long long B = 0;
     for (int p = 0; p < s - 1; ++p) B |= 16ll << (5 * p);
     const int nb = Kpad / bpad;
     const int64_t plane = plane_rows * pitch;
-    for (int kp0 = threadIdx.x * kSliceVec; kp0 < Kpad; kp0 += kSliceThreads * kSliceVec) {
-        // a chunk never straddles a contraction block (bpad is a multiple of kSliceVec)
+    for (int kp0 = threadIdx.x * kV; kp0 < Kpad; kp0 += kSliceThreads * kV) {
+        // a chunk never straddles a contraction block (bpad is a multiple of kV)
         const int b = kp0 / bpad, rr0 = kp0 - b * bpad;
         // number of live values of this chunk (a prefix: the block tail and Kin cut it from above)
-        const int nv = live && b < nb ? max(0, min(min(kSliceVec, rpb - rr0), Kin - (b * rpb + rr0))) : 0;
+        const int nv = live && b < nb ? max(0, min(min(kV, rpb - rr0), Kin - (b * rpb + rr0))) : 0;
         const double2 *zc = Zc + b * rpb + rr0;
-        long long xr[kSliceVec], xi[kSliceVec];
+        long long xr[kV], xi[kV];
 #pragma unroll
-        for (int u = 0; u < kSliceVec; ++u) {
+        for (int u = 0; u < kV; ++u) {
             const double2 z = u < nv ? zc[u] : make_double2(0.0, 0.0);
-            const double sc = (v && u < nv) ? base * v[b * rpb + rr0 + u] : base;
-            xr[u] = B + __double2ll_rn(z.x * sc);
-            xi[u] = B + __double2ll_rn(z.y * sc);
-        }
-        write_planes(xr, xi, s, tab.digits + r * pitch + kp0, plane);
-        if (kDual) {
-            // the chunk again (an L1 hit) for the weighted operand
-#pragma unroll
-            for (int u = 0; u < kSliceVec; ++u) {
-                const double2 z = u < nv ? zc[u] : make_double2(0.0, 0.0);
-                const double sc = u < nv ? base2 * v2[b * rpb + rr0 + u] : base2;
-                xr[u] = B + __double2ll_rn(z.x * sc);
-                xi[u] = B + __double2ll_rn(z.y * sc);
+            if (v && u < nv) {
+                const double sc = scale_pow2(v[b * rpb + rr0 + u], kx);
+                xr[u] = B + rint_pow2(z.x * sc, 0);
+                xi[u] = B + rint_pow2(z.y * sc, 0);
+            } else {
+                xr[u] = B + rint_pow2(z.x, kx);
+                xi[u] = B + rint_pow2(z.y, kx);
             }
-            write_planes(xr, xi, s, tab.digits2 + r * pitch + kp0, plane);
         }
+        write_planes<kV>(xr, xi, s, tab.digits + r * pitch + kp0, plane);
+        if (kDual)      // the chunk again (an L1 hit) for the weighted operand
+            weighted_chunk<kV>(zc, v2 + b * rpb + rr0, nv, kw, B, s, tab.digits2 + r * pitch + kp0, plane);
     }
 }
 
