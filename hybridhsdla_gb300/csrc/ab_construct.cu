@@ -211,7 +211,8 @@ __global__ void __launch_bounds__(kThreads) construct_ab_kernel(DevSystem sys, c
             }
             __syncthreads();
             double2 *col = C + ldc * gi;
-            const int64_t nrow = (int64_t)twoL * na;
+            // C may be absent: the structure-factor form needs only the per-type rows M
+            const int64_t nrow = C ? (int64_t)twoL * na : 0;
             for (int64_t idx = threadIdx.x; idx < nrow; idx += blockDim.x) {
                 const int j = (int)(idx / twoL);
                 const int r = (int)(idx - (int64_t)j * twoL);

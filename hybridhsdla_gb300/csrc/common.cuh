@@ -90,6 +90,29 @@ constexpr int kFp64Tile = 64;
 int64_t fp64_job_tiles(const Fp64Job &j);
 cudaError_t launch_fp64_jobs(const Fp64Job *d_jobs, int num_jobs, int64_t total_tiles, cudaStream_t st);
 
+// ---- structure-factor form (atoms sharing their type's rotation)
+// One k-point of a combine: per-type products PS, PH (lower triangles, ld ldp) into the outputs
+// S, H (ld ldo); g the k-point's G-vectors [n][3] on the device.
+struct SfEntry {
+    const double2 *PS = nullptr, *PH = nullptr;
+    double2 *S = nullptr, *H = nullptr;
+    int64_t ldp = 0, ldo = 0, n = 0;
+    const int32_t *g = nullptr;
+    int64_t tile_begin = 0;
+};
+struct SfTab {
+    int nk = 0, type = 0;
+    int dx = 0, dy = 0, dz = 0, ny = 0, nz = 0;   // box offsets (half widths) and extents
+    int64_t box = 0;                              // entries per type
+    SfEntry e[kMaxGroup];
+};
+// SF_t(dG) = sum_{a of type t} e^{i 2pi dG.tau_a} over the box of G-vector differences, from
+// per-atom factors ex[a][dGx + dx] = e^{i 2pi dGx tau_a,x} (and y, z); atoms listed by type.
+cudaError_t launch_sf_table(const double2 *ex, const double2 *ey, const double2 *ez, const int32_t *order,
+                            const int32_t *type_begin, int nt, int nx, int ny, int nz, double2 *sf, cudaStream_t st);
+// S (+)= SF_t (.) PS and H (+)= SF_t (.) PH over the lower triangles of every entry (t = tab.type).
+cudaError_t launch_sf_combine(const SfTab &tab, const double2 *sf, bool first, cudaStream_t st);
+
 // Fleur's packed lower triangle (row by row) of a column-major n x n matrix (device buffers).
 cudaError_t launch_pack_lower(const double2 *M, int64_t ld, int64_t n, double2 *P, cudaStream_t st);
 

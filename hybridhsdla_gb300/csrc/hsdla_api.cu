@@ -82,6 +82,7 @@ struct hsdla_plan {
         void *persist = nullptr;         // prepared tables (not shared with other groups)
         int64_t persist_bytes = 0;
         cudaEvent_t ev_dom[2] = {nullptr, nullptr};   // around the S/H launch (graph runs too)
+        SfTab sft{};                     // structure-factor combine of this group (outputs per run)
     };
     std::vector<Group> groups;
     void *prepared_ws = nullptr;
@@ -94,6 +95,12 @@ struct hsdla_plan {
     bool hoist = false;              // T application per type (no atom carries its own rotation)
     bool external = false;           // C is supplied by the caller (contraction-only entry)
     int panels = 1;                  // atom panels of the Ozaki contraction (memory-bounded streaming)
+    // structure-factor form (atoms share their type's rotation): per-type S weights [nt][2L] and
+    // the structure factors SF_t over the box of G-vector differences
+    bool sf = false;
+    double *wt = nullptr;
+    double2 *sf_tab = nullptr;
+    SfTab sf_dims{};                 // box extents and offsets (entries filled per group)
     double est_err = 0.0;            // autotuner's predicted relative error
     int launches = 0;
 };
@@ -563,6 +570,21 @@ int hsdla_plan_create(hsdla_context *ctx, const hsdla_system *s, const hsdla_kpo
     add(sizeof(double2) * tf_all.size());
     add(sizeof(double) * pl->twoLa); add(sizeof(double) * pl->twoLa);
     for (int i = 0; i < nk; ++i) add(sizeof(int32_t) * 3 * kpts[i].n_g);
+    // structure-factor form: per-type weights, per-atom phase factors along each axis, the atoms
+    // grouped by type and the table itself over the box of G-vector differences g_col - g_row
+    const char *sf_env = getenv("HSDLA_SF");
+    pl->sf = pl->hoist && !(sf_env && strtol(sf_env, nullptr, 10) == 0) && pl->opts.precision == HSDLA_PREC_FP64;
+    int half[3] = {0, 0, 0}, ext[3] = {1, 1, 1};
+    if (pl->sf) {
+        for (int i = 0; i < nk; ++i)
+            for (int64_t q = 0; q < kpts[i].n_g; ++q)
+                for (int c = 0; c < 3; ++c) half[c] = std::max(half[c], 2 * std::abs(kpts[i].g[3 * q + c]));
+        for (int c = 0; c < 3; ++c) ext[c] = 2 * half[c] + 1;
+        add(sizeof(double) * 2 * L * nt);
+        add(sizeof(double2) * (int64_t)na * (ext[0] + ext[1] + ext[2]));
+        add(sizeof(int32_t) * (na + nt + 1));
+        add(sizeof(double2) * (int64_t)nt * ext[0] * ext[1] * ext[2]);
+    }
     rc = ctx_malloc(ctx, &pl->tables, bytes);
     if (rc) { delete pl; return rc; }
     pl->tables_bytes = bytes;
@@ -604,7 +626,46 @@ int hsdla_plan_create(hsdla_context *ctx, const hsdla_system *s, const hsdla_kpo
         const double G = (double)kpts[i].n_g;
         pl->flop += 20.0 * G * G * L * na + 24.0 * (double)L * L * na * G;
     }
+    const double2 *d_ex = nullptr;
+    const int32_t *d_order = nullptr;
+    if (pl->sf) {
+        std::vector<double> wt((size_t)2 * L * nt);
+        for (int t = 0; t < nt; ++t)
+            for (int l = 0; l < nl; ++l)
+                for (int lm = l * l; lm < (l + 1) * (l + 1); ++lm) {
+                    wt[(size_t)2 * L * t + lm] = 1.0;
+                    wt[(size_t)2 * L * t + L + lm] = (l <= s->type_lmax[t]) ? s->type_dE_u_norm[t * nl + l] : 0.0;
+                }
+        pl->wt = (double *)put(wt.data(), sizeof(double) * wt.size());
+        std::vector<double2> ph((size_t)na * (ext[0] + ext[1] + ext[2]));
+        size_t o = 0;
+        for (int c = 0; c < 3; ++c)
+            for (int j = 0; j < na; ++j)
+                for (int i = 0; i < ext[c]; ++i) {
+                    const double ang = 2 * kPi * (double)(i - half[c]) * s->atom_pos[3 * j + c];
+                    ph[o++] = make_double2(std::cos(ang), std::sin(ang));
+                }
+        d_ex = (const double2 *)put(ph.data(), sizeof(double2) * ph.size());
+        std::vector<int32_t> ord;
+        std::vector<int32_t> tb(nt + 1, 0);
+        for (int t = 0; t < nt; ++t) {
+            tb[t] = (int32_t)ord.size();
+            for (int j = 0; j < na; ++j)
+                if (s->atom_type[j] == t) ord.push_back(j);
+        }
+        tb[nt] = (int32_t)ord.size();
+        ord.insert(ord.end(), tb.begin(), tb.end());
+        d_order = (const int32_t *)put(ord.data(), sizeof(int32_t) * ord.size());
+        pl->sf_tab = (double2 *)put(nullptr, sizeof(double2) * (int64_t)nt * ext[0] * ext[1] * ext[2]);
+        SfTab &dm = pl->sf_dims;
+        dm.dx = half[0]; dm.dy = half[1]; dm.dz = half[2];
+        dm.ny = ext[1]; dm.nz = ext[2];
+        dm.box = (int64_t)ext[0] * ext[1] * ext[2];
+    }
     cudaError_t e = cudaMemcpyAsync(pl->tables, host.data(), bytes, cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess && pl->sf)
+        e = launch_sf_table(d_ex, d_ex + (size_t)na * ext[0], d_ex + (size_t)na * (ext[0] + ext[1]), d_order,
+                            d_order + na, nt, ext[0], ext[1], ext[2], pl->sf_tab, ctx->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
     if (e != cudaSuccess) {
         hsdla_plan_destroy(pl);
@@ -627,8 +688,10 @@ namespace {
 // FP64 buffers of one k-point inside a group workspace.
 int64_t kpoint_fp64_bytes(const hsdla_plan *pl, int64_t G) {
     const int64_t K = pl->twoLa, ldm = 2 * (int64_t)pl->L * pl->nt;
-    const int64_t nCX = pl->opts.precision == HSDLA_PREC_FP64 ? 2 : 1;   // FP64 keeps C and X apart
     auto r = [](int64_t x) { return (x + 1023) / 1024 * 1024; };        // each buffer is 1 KB aligned
+    // structure-factor form: M, Z and the two per-type products (no C, no X)
+    if (pl->sf) return 2 * r(ldm * G * (int64_t)sizeof(double2)) + 2 * r(G * G * (int64_t)sizeof(double2));
+    const int64_t nCX = pl->opts.precision == HSDLA_PREC_FP64 ? 2 : 1;   // FP64 keeps C and X apart
     int64_t b = nCX * r(K * G * (int64_t)sizeof(double2));
     if (pl->hoist) b += 2 * r(ldm * G * (int64_t)sizeof(double2));
     return b;
@@ -754,17 +817,36 @@ int prepare_groups(hsdla_plan *pl, void *ws, cudaStream_t st) {
             e.kp = pk.dk;
             e.col_begin = col;
             col += G;
-            e.C = reinterpret_cast<double2 *>(take(K * G * (int64_t)sizeof(double2)));
-            e.X = pl->opts.precision == HSDLA_PREC_FP64 ? reinterpret_cast<double2 *>(take(K * G * (int64_t)sizeof(double2)))
-                                                        : e.C;   // Ozaki: X reuses C once C is sliced
+            if (pl->sf) {
+                e.C = nullptr;            // structure-factor form: only the per-type rows
+                e.X = nullptr;
+            } else {
+                e.C = reinterpret_cast<double2 *>(take(K * G * (int64_t)sizeof(double2)));
+                e.X = pl->opts.precision == HSDLA_PREC_FP64
+                          ? reinterpret_cast<double2 *>(take(K * G * (int64_t)sizeof(double2)))
+                          : e.C;   // Ozaki: X reuses C once C is sliced
+            }
             e.M = pl->hoist ? reinterpret_cast<double2 *>(take(ldm * G * (int64_t)sizeof(double2))) : nullptr;
             double2 *Z = pl->hoist ? reinterpret_cast<double2 *>(take(ldm * G * (int64_t)sizeof(double2))) : nullptr;
             e.Z = Z;
+            if (pl->sf) {
+                SfEntry &f = g.sft.e[q];
+                f = SfEntry();
+                f.PS = reinterpret_cast<double2 *>(take(G * G * (int64_t)sizeof(double2)));
+                f.PH = reinterpret_cast<double2 *>(take(G * G * (int64_t)sizeof(double2)));
+                f.ldp = G; f.n = G; f.g = pk.dk.g;
+            }
             OzKBufs b;
             b.CX = e.C; b.M = e.M; b.Z = Z; b.G = G;
             kb.push_back(b);
         }
         kt.total_cols = col;
+        if (pl->sf) {
+            SfTab &ft = g.sft;
+            const SfTab &dm = pl->sf_dims;
+            ft.nk = kt.nk;
+            ft.dx = dm.dx; ft.dy = dm.dy; ft.dz = dm.dz; ft.ny = dm.ny; ft.nz = dm.nz; ft.box = dm.box;
+        }
         if (pl->opts.precision == HSDLA_PREC_OZAKI_FP8) {
             OzGroupDesc d;
             d.twoL = twoL; d.na = pl->na; d.nt = pl->nt; d.hoist = pl->hoist;
@@ -797,6 +879,7 @@ int prepare_groups(hsdla_plan *pl, void *ws, cudaStream_t st) {
                         jt.push_back(jb);
                     }
                 }
+                if (pl->sf) continue;
                 Fp64Job js{};
                 js.P = e.C; js.ldp = K; js.Q = e.C; js.ldq = K; js.w = pl->w;
                 js.m = G; js.n = G; js.k = K; js.lower = 1;
@@ -806,7 +889,31 @@ int prepare_groups(hsdla_plan *pl, void *ws, cudaStream_t st) {
                 jsh.push_back(jh);
             }
             g.tiles_t = assign_tiles(jt, 0);
-            g.tiles_sh = assign_tiles(jsh, 0);
+            if (pl->sf) {
+                // per type: S_t = M_t^H diag(w_t) M_t and H_t = M_t^H Z_t of every k-point into the
+                // products; one launch per type (each type's jobs carry their own tile numbering)
+                for (int t = 0; t < pl->nt; ++t) {
+                    std::vector<Fp64Job> jt_sh;
+                    for (int q = 0; q < kt.nk; ++q) {
+                        const KEntry &e = kt.e[q];
+                        const int64_t G = pl->kps[g.kidx[q]].n_g;
+                        Fp64Job js{};
+                        js.P = e.M + twoL * t; js.ldp = ldm; js.Q = e.M + twoL * t; js.ldq = ldm;
+                        js.w = pl->wt + twoL * t;
+                        js.out = const_cast<double2 *>(g.sft.e[q].PS); js.ldo = G;
+                        js.m = G; js.n = G; js.k = twoL; js.lower = 1;
+                        Fp64Job jh = js;
+                        jh.Q = e.Z + twoL * t; jh.w = nullptr;
+                        jh.out = const_cast<double2 *>(g.sft.e[q].PH);
+                        jt_sh.push_back(js);
+                        jt_sh.push_back(jh);
+                    }
+                    g.tiles_sh = assign_tiles(jt_sh, 0);
+                    jsh.insert(jsh.end(), jt_sh.begin(), jt_sh.end());
+                }
+            } else {
+                g.tiles_sh = assign_tiles(jsh, 0);
+            }
             g.n_jobs_t = (int)jt.size();
             g.d_jobs_t = reinterpret_cast<Fp64Job *>(keep(sizeof(Fp64Job) * jt.size()));
             g.d_jobs_sh = reinterpret_cast<Fp64Job *>(keep(sizeof(Fp64Job) * jsh.size()));
@@ -816,6 +923,8 @@ int prepare_groups(hsdla_plan *pl, void *ws, cudaStream_t st) {
             }
             memcpy(g.h_jobs_sh, jsh.data(), sizeof(Fp64Job) * jsh.size());
             CUDA_TRY(ctx, cudaMemcpy(g.d_jobs_t, jt.data(), sizeof(Fp64Job) * jt.size(), cudaMemcpyHostToDevice));
+            if (pl->sf)     // the products' jobs do not change between runs
+                CUDA_TRY(ctx, cudaMemcpy(g.d_jobs_sh, jsh.data(), sizeof(Fp64Job) * jsh.size(), cudaMemcpyHostToDevice));
         }
     }
     pl->prepared_ws = ws;
@@ -833,7 +942,14 @@ void set_outputs(hsdla_plan *pl, hsdla_cx *const *dH, hsdla_cx *const *dS, const
             H[q] = reinterpret_cast<double2 *>(dH[g.kidx[q]]);
             l[q] = ld[g.kidx[q]];
         }
-        if (g.oz) {
+        if (pl->sf) {
+            for (int q = 0; q < nk; ++q) {
+                g.sft.e[q].S = S[q];
+                g.sft.e[q].H = H[q];
+                g.sft.e[q].ldo = l[q];
+            }
+            if (g.oz) ozaki_group_set_sf(g.oz, g.sft);
+        } else if (g.oz) {
             ozaki_group_set_outputs(g.oz, S.data(), H.data(), l.data());
         } else {
             for (int q = 0; q < nk; ++q) {
@@ -865,16 +981,21 @@ float dominant_ms(const hsdla_plan *pl) {
     return tot;
 }
 
-// Algorithmic flops of the S/H launches of one execution (FP8 digit products for Ozaki).
+// Algorithmic flops of one group's S/H launches (FP8 digit products for Ozaki): contraction
+// length 2La, or 2L per type in the structure-factor form.
+void run_groups_flop_one(const hsdla_plan *pl, const hsdla_plan::Group &g, double *dom_flop) {
+    const double sl = pl->oz.num_slices;
+    const double Klen = pl->sf ? 2.0 * pl->L * pl->nt : (double)pl->twoLa;
+    for (int q = 0; q < g.ktab.nk; ++q) {
+        const double G = (double)g.ktab.e[q].kp.n_g;
+        const double lower = 4.0 * G * (G + 1.0) * Klen;
+        *dom_flop += 2.0 * lower * (g.oz ? sl * (sl + 1) / 2 : 1.0);
+    }
+}
+
 void run_groups_flop(const hsdla_plan *pl, double *dom_flop) {
     *dom_flop = 0.0;
-    const double sl = pl->oz.num_slices;
-    for (const auto &g : pl->groups)
-        for (int q = 0; q < g.ktab.nk; ++q) {
-            const double G = (double)g.ktab.e[q].kp.n_g;
-            const double lower = 4.0 * G * (G + 1.0) * (double)pl->twoLa;
-            *dom_flop += 2.0 * lower * (g.oz ? sl * (sl + 1) / 2 : 1.0);
-        }
+    for (const auto &g : pl->groups) run_groups_flop_one(pl, g, dom_flop);
 }
 
 // Enqueue every group's launches (no host synchronisation: capturable in a CUDA graph).
@@ -889,17 +1010,28 @@ int run_groups(hsdla_plan *pl, cudaStream_t st, bool timed, float *ms_ab, float 
             pl->launches++;
         }
         if (timed) CUDA_TRY(ctx, cudaEventRecord(ctx->evs[1], st));
-        for (int q = 0; q < g.ktab.nk; ++q) {
-            const double G = (double)g.ktab.e[q].kp.n_g;
-            const double lower = 4.0 * G * (G + 1.0) * (double)pl->twoLa;
-            const double sl = pl->oz.num_slices;
-            if (dom_flop) *dom_flop += 2.0 * lower * (g.oz ? sl * (sl + 1) / 2 : 1.0);
+        if (dom_flop) {
+            double f = 0.0;
+            run_groups_flop_one(pl, g, &f);
+            *dom_flop += f;
         }
         if (g.oz) {
             int nl = 0;
             const int rc = ozaki_group_run(g.oz, pl->dsys, g.ktab, st, g.ev_dom[0], g.ev_dom[1], &nl);
             if (rc) return set_err(ctx, rc, "Ozaki group failed: %s", ozaki_last_error());
             pl->launches += nl;
+        } else if (pl->sf) {
+            CUDA_TRY(ctx, launch_fp64_jobs(g.d_jobs_t, g.n_jobs_t, g.tiles_t, st));
+            pl->launches++;
+            CUDA_TRY(ctx, record_event(g.ev_dom[0], st));
+            const int nj = 2 * g.ktab.nk;
+            for (int t = 0; t < pl->nt; ++t) {
+                CUDA_TRY(ctx, launch_fp64_jobs(g.d_jobs_sh + (int64_t)nj * t, nj, g.tiles_sh, st));
+                g.sft.type = t;
+                CUDA_TRY(ctx, launch_sf_combine(g.sft, pl->sf_tab, t == 0, st));
+                pl->launches += 2;
+            }
+            CUDA_TRY(ctx, record_event(g.ev_dom[1], st));
         } else {
             CUDA_TRY(ctx, launch_fp64_jobs(g.d_jobs_t, g.n_jobs_t, g.tiles_t, st));
             pl->launches++;

@@ -1462,6 +1462,9 @@ struct OzGroup {
     int *d_progress = nullptr;
     int *d_err = nullptr;
     bool pair = false;          // S/H on CTA-pair tiles
+    bool sf = false;            // structure-factor form
+    SfTab sft{};                // its combine table (outputs patched per run)
+    const double2 *sf_tab = nullptr;
 };
 
 namespace {
@@ -1804,6 +1807,8 @@ int ozaki_group_prepare(OzakiPlan &oz, const OzGroupDesc &d, const std::vector<O
     *out = g;
     return HSDLA_OK;
 }
+
+void ozaki_group_set_sf(OzGroup *g, const SfTab &t) { g->sft = t; }
 
 void ozaki_group_set_outputs(OzGroup *g, double2 *const *S, double2 *const *H, const int64_t *ld) {
     for (int pi = 0; pi < g->panels; ++pi) {

@@ -64,6 +64,8 @@ int64_t ozaki_group_persist_bytes(int s, int64_t twoL, int64_t na, int64_t nt, c
 int ozaki_group_prepare(OzakiPlan &oz, const OzGroupDesc &d, const std::vector<OzKBufs> &kb, void *ws,
                         void *persist, cudaStream_t st, OzGroup **out);
 void ozaki_group_set_outputs(OzGroup *g, double2 *const *S, double2 *const *H, const int64_t *ld);
+// Structure-factor form: the group's combine table (outputs of this run, per-type products).
+void ozaki_group_set_sf(OzGroup *g, const SfTab &t);
 // Enqueues the group's launches (slices, T application, phases, S/H products); no host sync.
 int ozaki_group_run(OzGroup *g, const DevSystem &sys, const KTable &ktab, cudaStream_t st, cudaEvent_t ev0,
                     cudaEvent_t ev1, int *launches);

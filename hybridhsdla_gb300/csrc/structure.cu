@@ -1,0 +1,116 @@
+// Structure-factor form of S and H for plans whose atoms share their type's rotation.
+//
+// With C_a = phi_a (.) M_t(a) and X_a = phi_a (.) Z_t(a), phi_a(g) = e^{i 2pi (k+g).tau_a} (the
+// per-type rows M_t and Z_t = T_t M_t of the hoisted T application), the per-atom sums of
+// create_HS2_stripped_v2 (flapw_opt/src/h_and_s_stripped_v2.cpp:155-368) regroup by type:
+//     S[g, g'] = sum_t SF_t(g' - g) (M_t^H diag(w_t) M_t)[g, g'],
+//     H[g, g'] = sum_t SF_t(g' - g) (M_t^H Z_t)[g, g'],
+//     SF_t(dG) = sum_{a of type t} e^{i 2pi dG.tau_a}          (k cancels),
+// so the contractions run over 2L rows per type instead of 2L rows per atom (a factor of atoms
+// per type fewer products), and the structure factors enter once per element and type.
+#include "common.cuh"
+
+namespace hsdla {
+
+namespace {
+
+__device__ __forceinline__ double2 cmul_d(double2 a, double2 b) {
+    return make_double2(fma(a.x, b.x, -a.y * b.y), fma(a.x, b.y, a.y * b.x));
+}
+
+// sf[t][(ix ny + iy) nz + iz] = sum over the atoms of type t of ex[a][ix] ey[a][iy] ez[a][iz],
+// the atoms listed type by type (order[type_begin[t] .. type_begin[t+1])).
+__global__ void sf_table_kernel(const double2 *__restrict__ ex, const double2 *__restrict__ ey,
+                                const double2 *__restrict__ ez, const int32_t *__restrict__ order,
+                                const int32_t *__restrict__ type_begin, int nt, int nx, int ny, int nz,
+                                double2 *__restrict__ sf) {
+    const int64_t box = (int64_t)nx * ny * nz;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < box * nt; i += (int64_t)gridDim.x * blockDim.x) {
+        const int t = (int)(i / box);
+        const int64_t e = i - (int64_t)t * box;
+        const int ix = (int)(e / ((int64_t)ny * nz));
+        const int iy = (int)((e / nz) % ny);
+        const int iz = (int)(e % nz);
+        double2 acc = make_double2(0.0, 0.0);
+        for (int q = type_begin[t]; q < type_begin[t + 1]; ++q) {
+            const int a = order[q];
+            const double2 v = cmul_d(cmul_d(ex[(int64_t)a * nx + ix], ey[(int64_t)a * ny + iy]), ez[(int64_t)a * nz + iz]);
+            acc.x += v.x;
+            acc.y += v.y;
+        }
+        sf[i] = acc;
+    }
+}
+
+constexpr int kSfTile = 32, kSfRows = 8;
+
+// out (+)= SF_t(g_col - g_row) * P over the lower triangle of every entry (S and H together),
+// one CTA per 32 x 32 tile; consecutive threads take consecutive rows of a column.
+__global__ void __launch_bounds__(kSfTile * kSfRows) sf_combine_kernel(const __grid_constant__ SfTab tab,
+                                                                       const double2 *__restrict__ sf, int first) {
+    const int64_t tile = blockIdx.x;
+    int k = 0;
+    while (k + 1 < tab.nk && tab.e[k + 1].tile_begin <= tile) ++k;
+    const SfEntry &E = tab.e[k];
+    const int64_t b = tile - E.tile_begin;
+    int64_t tr = (int64_t)((sqrt(8.0 * (double)b + 1.0) - 1.0) * 0.5);
+    while (tr * (tr + 1) / 2 > b) --tr;
+    while ((tr + 1) * (tr + 2) / 2 <= b) ++tr;
+    const int64_t tc = b - tr * (tr + 1) / 2;
+    const int64_t row = tr * kSfTile + threadIdx.x;
+    if (row >= E.n) return;
+    const int32_t *gr = E.g + 3 * row;
+    const int gr0 = gr[0], gr1 = gr[1], gr2 = gr[2];
+    const double2 *sft = sf + (int64_t)tab.type * tab.box;
+#pragma unroll
+    for (int q = 0; q < kSfTile; q += kSfRows) {
+        const int64_t col = tc * kSfTile + threadIdx.y + q;
+        if (col > row) continue;
+        const int32_t *gc = E.g + 3 * col;
+        const int64_t idx = ((int64_t)(gc[0] - gr0 + tab.dx) * tab.ny + (gc[1] - gr1 + tab.dy)) * tab.nz +
+                            (gc[2] - gr2 + tab.dz);
+        const double2 f = sft[idx];
+        const double2 ps = E.PS[row + E.ldp * col], ph = E.PH[row + E.ldp * col];
+        double2 *so = E.S + row + E.ldo * col, *ho = E.H + row + E.ldo * col;
+        double2 vs = cmul_d(f, ps), vh = cmul_d(f, ph);
+        if (!first) {
+            const double2 s0 = *so, h0 = *ho;
+            vs.x += s0.x; vs.y += s0.y;
+            vh.x += h0.x; vh.y += h0.y;
+        }
+        *so = vs;
+        *ho = vh;
+    }
+}
+
+}  // namespace
+
+cudaError_t launch_sf_table(const double2 *ex, const double2 *ey, const double2 *ez, const int32_t *order,
+                            const int32_t *type_begin, int nt, int nx, int ny, int nz, double2 *sf, cudaStream_t st) {
+    const int64_t n = (int64_t)nx * ny * nz * nt;
+    if (n <= 0) return cudaSuccess;
+    const int64_t blocks = std::min<int64_t>((n + 255) / 256, 65535);
+    sf_table_kernel<<<(unsigned)blocks, 256, 0, st>>>(ex, ey, ez, order, type_begin, nt, nx, ny, nz, sf);
+    return cudaGetLastError();
+}
+
+int64_t sf_tab_tiles(SfTab &tab) {
+    int64_t total = 0;
+    for (int k = 0; k < tab.nk; ++k) {
+        const int64_t T = (tab.e[k].n + kSfTile - 1) / kSfTile;
+        tab.e[k].tile_begin = total;
+        total += T * (T + 1) / 2;
+    }
+    return total;
+}
+
+cudaError_t launch_sf_combine(const SfTab &tab, const double2 *sf, bool first, cudaStream_t st) {
+    SfTab t = tab;
+    const int64_t tiles = sf_tab_tiles(t);
+    if (tiles <= 0) return cudaSuccess;
+    if (tiles > 0x7fffffffLL) return cudaErrorInvalidValue;
+    sf_combine_kernel<<<(unsigned)tiles, dim3(kSfTile, kSfRows), 0, st>>>(t, sf, first ? 1 : 0);
+    return cudaGetLastError();
+}
+
+}  // namespace hsdla
