@@ -573,7 +573,7 @@ int hsdla_plan_create(hsdla_context *ctx, const hsdla_system *s, const hsdla_kpo
     // structure-factor form: per-type weights, per-atom phase factors along each axis, the atoms
     // grouped by type and the table itself over the box of G-vector differences g_col - g_row
     const char *sf_env = getenv("HSDLA_SF");
-    pl->sf = pl->hoist && !(sf_env && strtol(sf_env, nullptr, 10) == 0) && pl->opts.precision == HSDLA_PREC_FP64;
+    pl->sf = pl->hoist && !(sf_env && strtol(sf_env, nullptr, 10) == 0);
     int half[3] = {0, 0, 0}, ext[3] = {1, 1, 1};
     if (pl->sf) {
         for (int i = 0; i < nk; ++i)
@@ -702,7 +702,8 @@ int64_t group_bytes(const hsdla_plan *pl, const std::vector<int> &kidx) {
     std::vector<int64_t> G;
     for (int i : kidx) { b += kpoint_fp64_bytes(pl, pl->kps[i].n_g); G.push_back(pl->kps[i].n_g); }
     if (pl->opts.precision == HSDLA_PREC_OZAKI_FP8)
-        b += 1024 + ozaki_group_bytes(pl->oz.num_slices, 2 * (int64_t)pl->L, pl->na, pl->nt, G, pl->panels, pl->hoist);
+        b += 1024 + ozaki_group_bytes(pl->oz.num_slices, 2 * (int64_t)pl->L, pl->na, pl->nt, G, pl->panels, pl->hoist,
+                                      pl->sf);
     return b;
 }
 
@@ -710,7 +711,8 @@ int64_t group_persist_bytes(const hsdla_plan *pl, const std::vector<int> &kidx) 
     std::vector<int64_t> G;
     for (int i : kidx) G.push_back(pl->kps[i].n_g);
     if (pl->opts.precision == HSDLA_PREC_OZAKI_FP8)
-        return ozaki_group_persist_bytes(pl->oz.num_slices, 2 * (int64_t)pl->L, pl->na, pl->nt, G, pl->panels);
+        return ozaki_group_persist_bytes(pl->oz.num_slices, 2 * (int64_t)pl->L, pl->na, pl->nt, G,
+                                         pl->sf ? std::max(pl->panels, pl->nt) : pl->panels);
     return 4096 + (int64_t)sizeof(Fp64Job) * (int64_t)kidx.size() * (std::max(pl->na, pl->nt) + 4);
 }
 
@@ -735,7 +737,7 @@ int64_t workspace_budget(hsdla_context *ctx) {
 // bulk of the workspace, so P panels need about 1/P of them.
 void choose_panels(hsdla_plan *pl, int64_t budget) {
     pl->panels = 1;
-    if (pl->opts.precision != HSDLA_PREC_OZAKI_FP8) return;
+    if (pl->opts.precision != HSDLA_PREC_OZAKI_FP8 || pl->sf) return;   // the per-type digits are small
     const char *ev = getenv("HSDLA_PANELS");
     const int64_t forced = ev ? strtoll(ev, nullptr, 10) : 0;
     if (forced > 0) { pl->panels = (int)std::min<int64_t>(forced, pl->na); return; }
@@ -838,6 +840,10 @@ int prepare_groups(hsdla_plan *pl, void *ws, cudaStream_t st) {
             }
             OzKBufs b;
             b.CX = e.C; b.M = e.M; b.Z = Z; b.G = G;
+            if (pl->sf) {
+                b.PS = const_cast<double2 *>(g.sft.e[q].PS);
+                b.PH = const_cast<double2 *>(g.sft.e[q].PH);
+            }
             kb.push_back(b);
         }
         kt.total_cols = col;
@@ -852,6 +858,7 @@ int prepare_groups(hsdla_plan *pl, void *ws, cudaStream_t st) {
             d.twoL = twoL; d.na = pl->na; d.nt = pl->nt; d.hoist = pl->hoist;
             d.w = pl->w; d.Tfull = pl->Tfull; d.atom_type = pl->atom_type.data();
             d.panels = pl->panels;
+            d.sf = pl->sf; d.wt = pl->wt; d.sf_tab = pl->sf_tab;
             char *oz_ws = reinterpret_cast<char *>((reinterpret_cast<uintptr_t>(p) + 1023) & ~uintptr_t(1023));
             int rc = ozaki_group_prepare(pl->oz, d, kb, oz_ws, g.persist, st, &g.oz);
             if (rc) return set_err(ctx, rc, "group set-up failed: %s", ozaki_last_error());

@@ -1592,8 +1592,12 @@ static int64_t panel_atoms(int64_t na, int panels) { return (na + panels - 1) / 
 static int64_t atom_stride(int64_t twoL) { return round_up(twoL, 16); }
 
 int64_t ozaki_group_bytes(int s, int64_t twoL, int64_t na, int64_t nt, const std::vector<int64_t> &G, int panels,
-                          bool hoist) {
+                          bool hoist, bool sf) {
     const int64_t bpad = atom_stride(twoL), rows = group_rows(G);
+    if (sf) {      // M, M diag(w_t) and Z digits: each type's rows on whole k-blocks
+        const int64_t KT = round_up(twoL, kKBlock) * nt;
+        return 3 * (round_up(2 * s * rows * (KT + pitch_pad()), 1024) + round_up(4 * rows, 1024)) + 4096;
+    }
     const int64_t Kp = round_up(bpad * panel_atoms(na, panels), kKBlock);
     const int64_t Kx = hoist ? std::max(Kp, round_up(bpad * nt, kKBlock)) : Kp;
     auto dig = [&](int64_t K) { return round_up(2 * s * rows * (K + pitch_pad()), 1024) + round_up(4 * rows, 1024); };
@@ -1615,11 +1619,148 @@ int64_t ozaki_group_persist_bytes(int s, int64_t twoL, int64_t na, int64_t nt, c
            round_up(sizeof(int4) * (tiles_sh + 1), 1024) + round_up(sizeof(int) * kProgressCap, 1024) + 8192;
 }
 
+// Structure-factor form of a group: digit planes of M, M diag(w_t) and Z (2L rows per type, each
+// type's rows starting on a k-block so that the per-type products never mix types), the T
+// application Z_t = T_t M_t, and per type one S/H launch into the products PS, PH followed by the
+// combine into S and H.
+static int group_prepare_sf(OzakiPlan &oz, const OzGroupDesc &d, const std::vector<OzKBufs> &kb, void *ws,
+                            void *persist, cudaStream_t st, OzGroup **out) {
+    auto *g = new OzGroup();
+    g->sf = true;
+    g->s = oz.num_slices;
+    g->nk = (int)kb.size();
+    g->hoist = true;
+    g->twoL = d.twoL; g->na = d.na; g->nt = d.nt;
+    g->bpad = round_up(d.twoL, kKBlock);                      // type stride along the contraction
+    const int64_t tkb = g->bpad / kKBlock, KT = g->bpad * d.nt;
+    g->kb = kb;
+    g->d_err = oz.d_error;
+    g->sf_tab = d.sf_tab;
+    std::vector<int64_t> G;
+    for (auto &k : kb) G.push_back(k.G);
+    g->rows = group_rows(G);
+    int64_t r0 = 0;
+    for (int64_t x : G) { g->row0.push_back(r0); r0 += round_up(std::max<int64_t>(x, 1), kTileM); }
+    const int s = g->s;
+    Arena ar{reinterpret_cast<char *>(ws)};
+    Arena keep{reinterpret_cast<char *>(persist)};
+    auto carve_rows = [&](DigitOperand &o) {
+        o.plane_rows = g->rows;
+        o.Kpad = KT;
+        o.pitch = KT + pitch_pad();
+        o.digits = ar.take<uint8_t>(2 * s * o.plane_rows * o.pitch);
+        o.expo = ar.take<int32_t>(o.plane_rows);
+    };
+    carve_rows(g->dM);        // M
+    carve_rows(g->dW);        // M diag(w_t)
+    carve_rows(g->dX);        // Z
+    carve_operand(keep, g->dT, s, d.nt * d.twoL, tkb * kKBlock);
+    const int64_t nk = g->nk;
+    int64_t tiles_t = 0, tiles_sh = 0;
+    for (int64_t x : G) {
+        const int64_t T = (x + kTileN - 1) / kTileN;
+        tiles_t += d.nt * ((d.twoL + kTileM - 1) / kTileM) * T;
+        tiles_sh += T * (T + 1);
+    }
+    g->d_jobs_t = keep.take<OzJob>(nk * (d.nt + 2));
+    g->d_jobs_sh = keep.take<OzJob>(2 * nk * d.nt);
+    g->d_list_t = keep.take<int4>(tiles_t + 1);
+    g->d_list_sh = keep.take<int4>(tiles_sh + 1);
+    g->d_progress = keep.take<int>(kProgressCap);
+    auto fail = [&](int code) { ozaki_group_destroy(g); return code; };
+    auto table = [&](const DigitOperand &o, int which) {
+        SliceTab t;
+        t.nk = g->nk; t.s = s; t.ldz = d.twoL * d.nt; t.Kin = d.twoL * d.nt; t.rpb = d.twoL; t.bpad = g->bpad;
+        t.digits = o.digits; t.Kpad = KT; t.plane_rows = o.plane_rows; t.pitch = o.pitch; t.expo = o.expo;
+        for (int k = 0; k < g->nk; ++k) t.e[k] = SliceEntry{which == 0 ? kb[k].M : kb[k].Z, kb[k].G, g->row0[k]};
+        return t;
+    };
+    g->tM = table(g->dM, 0);              // dual: M and M diag(w_t)
+    g->tM.v2 = d.wt;
+    g->tM.digits2 = g->dW.digits;
+    g->tM.expo2 = g->dW.expo;
+    OzPanel p;                            // one "panel" carries the Z slicing table
+    p.a0 = 0; p.a1 = d.na;
+    p.tX = table(g->dX, 1);
+    g->pan.push_back(p);
+    g->panels = 1;
+    cudaError_t e = slice(d.Tfull, d.twoL, nullptr, d.twoL, d.nt * d.twoL, d.twoL, g->bpad, s, g->dT, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) { g_oz_err = cudaGetErrorString(e); return fail(HSDLA_ERR_CUDA); }
+    int rc = make_map(g->dM, s);
+    if (!rc) rc = make_map(g->dW, s);
+    if (!rc) rc = make_map(g->dX, s);
+    if (!rc) rc = make_map(g->dT, s);
+    if (rc) return fail(rc);
+    // T application per type: Z_t = T_t M_t
+    std::vector<OzJob> jt;
+    for (int k = 0; k < g->nk; ++k)
+        for (int64_t t = 0; t < d.nt; ++t) {
+            OzJob j;
+            memset(&j, 0, sizeof(j));
+            j.lmap = 3; j.rmap = 0;
+            j.lplane = g->dT.plane_rows; j.rplane = g->dM.plane_rows;
+            j.lrow0 = t * d.twoL; j.rrow0 = g->row0[k];
+            j.rk0 = t * g->bpad;
+            j.nkb = tkb;
+            j.m = d.twoL; j.n = kb[k].G;
+            j.out = kb[k].Z + d.twoL * t; j.ldo = d.twoL * d.nt;
+            j.el = g->dT.expo + t * d.twoL; j.er = g->dM.expo + g->row0[k];
+            jt.push_back(j);
+        }
+    g->n_jobs_t = (int)jt.size();
+    rc = upload_schedule(jt, g->d_jobs_t, g->d_list_t, g->tiles_t);
+    if (rc) return fail(rc);
+    g->maps_t[0] = g->dM.map; g->maps_t[1] = g->dM.map; g->maps_t[2] = g->dM.map; g->maps_t[3] = g->dT.map;
+    // per type: S_t = M_t^H diag(w_t) M_t and H_t = M_t^H Z_t into the products
+    g->pair = use_pair();
+    const int64_t tile = g->pair ? kPairTile : kTileN;
+    g->n_jobs_sh = 2 * g->nk;
+    std::vector<OzJob> all;
+    for (int64_t t = 0; t < d.nt; ++t) {
+        std::vector<OzJob> jsh;
+        for (int k = 0; k < g->nk; ++k)
+            for (int which = 0; which < 2; ++which) {
+                OzJob j;
+                memset(&j, 0, sizeof(j));
+                j.lmap = 0; j.rmap = which == 0 ? 1 : 2; j.lower = 1;
+                j.lplane = g->rows; j.rplane = g->rows;
+                j.lrow0 = g->row0[k]; j.rrow0 = g->row0[k];
+                j.lk0 = t * g->bpad; j.rk0 = t * g->bpad;
+                j.nkb = tkb;
+                j.m = kb[k].G; j.n = kb[k].G;
+                j.out = which == 0 ? kb[k].PS : kb[k].PH;
+                j.ldo = kb[k].G;
+                j.el = g->dM.expo + g->row0[k];
+                j.er = (which == 0 ? g->dW.expo : g->dX.expo) + g->row0[k];
+                jsh.push_back(j);
+            }
+        if (t == 0) {
+            rc = upload_schedule(jsh, g->d_jobs_sh, g->d_list_sh, g->tiles_sh, tile);
+            if (rc) return fail(rc);
+        } else {
+            int64_t total = 0;
+            for (auto &j : jsh) {
+                j.tiles_n = (j.n + tile - 1) / tile;
+                j.tile_begin = total;
+                total += job_tiles(j, tile);
+            }
+        }
+        all.insert(all.end(), jsh.begin(), jsh.end());
+    }
+    e = cudaMemcpy(g->d_jobs_sh, all.data(), sizeof(OzJob) * all.size(), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) { g_oz_err = cudaGetErrorString(e); return fail(HSDLA_ERR_CUDA); }
+    g->maps_sh[0] = g->dM.map; g->maps_sh[1] = g->dW.map; g->maps_sh[2] = g->dX.map; g->maps_sh[3] = g->dM.map;
+    *out = g;
+    return HSDLA_OK;
+}
+
 int ozaki_group_prepare(OzakiPlan &oz, const OzGroupDesc &d, const std::vector<OzKBufs> &kb, void *ws,
                         void *persist, cudaStream_t st, OzGroup **out) {
     *out = nullptr;
     if (kb.empty() || (int)kb.size() > kMaxGroup) { g_oz_err = "group size out of range"; return HSDLA_ERR_ARG; }
     if (d.panels < 1 || d.panels > d.na) { g_oz_err = "panel count out of range"; return HSDLA_ERR_ARG; }
+    if (d.sf) return group_prepare_sf(oz, d, kb, ws, persist, st, out);
     auto *g = new OzGroup();
     g->s = oz.num_slices;
     g->nk = (int)kb.size();
@@ -1839,6 +1980,31 @@ int ozaki_group_run(OzGroup *g, const DevSystem &sys, const KTable &ktab, cudaSt
                     cudaEvent_t ev1, int *launches) {
     int nl = 0;
     cudaError_t e = cudaSuccess;
+    if (g->sf) {
+        e = slice_launch(g->tM, st);                      // M and M diag(w_t)
+        if (e == cudaSuccess)
+            e = launch_prepared(g->maps_t, g->s, g->d_err, g->d_jobs_t, g->n_jobs_t, g->tiles_t, g->d_list_t, nullptr,
+                                st);
+        if (e == cudaSuccess) e = slice_launch(g->pan[0].tX, st);    // Z
+        nl += 3;
+        if (e == cudaSuccess && ev0) e = record(ev0, st);
+        for (int t = 0; t < g->nt && e == cudaSuccess; ++t) {
+            const OzJob *jobs = g->d_jobs_sh + (int64_t)g->n_jobs_sh * t;
+            e = g->pair ? launch_pair(g->maps_sh, g->s, g->d_err, jobs, g->n_jobs_sh, g->tiles_sh, g->d_list_sh,
+                                      g->d_progress, st)
+                        : launch_prepared(g->maps_sh, g->s, g->d_err, jobs, g->n_jobs_sh, g->tiles_sh, g->d_list_sh,
+                                          g->d_progress, st);
+            if (e == cudaSuccess) {
+                g->sft.type = t;
+                e = launch_sf_combine(g->sft, g->sf_tab, t == 0, st);
+            }
+            nl += 2;
+        }
+        if (e == cudaSuccess && ev1) e = record(ev1, st);
+        if (launches) *launches = nl;
+        if (e != cudaSuccess) { g_oz_err = cudaGetErrorString(e); return HSDLA_ERR_CUDA; }
+        return HSDLA_OK;
+    }
     if (g->hoist) {
         e = slice_launch(g->tM, st);
         if (e == cudaSuccess)
@@ -1891,7 +2057,8 @@ void ozaki_group_destroy(OzGroup *g) {
 // One k-point through a temporary group (the slice autotuner's probe).
 int64_t ozaki_pipeline_workspace(int s, int64_t twoL, int64_t na, int64_t nt, int64_t G) {
     const std::vector<int64_t> g{G};
-    return ozaki_group_bytes(s, twoL, na, nt, g, 1, true) + ozaki_group_persist_bytes(s, twoL, na, nt, g, 1) + 2048;
+    return ozaki_group_bytes(s, twoL, na, nt, g, 1, true, false) + ozaki_group_persist_bytes(s, twoL, na, nt, g, 1) +
+           2048;
 }
 
 int ozaki_pipeline(OzakiPlan &oz, const OzakiInputs &in, double2 *S, double2 *H, int64_t ldo, void *ws,
@@ -1907,7 +2074,7 @@ int ozaki_pipeline(OzakiPlan &oz, const OzakiInputs &in, double2 *S, double2 *H,
     kb[0].G = in.G;
     OzGroup *g = nullptr;
     const int64_t scratch = ozaki_group_bytes(oz.num_slices, in.twoL, in.na, in.nt, std::vector<int64_t>{in.G}, 1,
-                                              d.hoist);
+                                              d.hoist, false);
     char *persist = reinterpret_cast<char *>(ws) + (scratch + 1023) / 1024 * 1024;
     int rc = ozaki_group_prepare(oz, d, kb, ws, persist, st, &g);
     if (rc) return rc;

@@ -43,6 +43,8 @@ struct OzKBufs {
     double2 *M = nullptr;    // per-type rows M (2L nt x G), hoisted T application only
     double2 *Z = nullptr;    // per-type products Z (2L nt x G), hoisted T application only
     int64_t G = 0;
+    double2 *PS = nullptr;   // structure-factor form: per-type products (G x G, ld G)
+    double2 *PH = nullptr;
 };
 struct OzGroupDesc {
     int64_t twoL = 0, na = 0, nt = 0;
@@ -51,6 +53,9 @@ struct OzGroupDesc {
     const double2 *Tfull = nullptr;        // per-type 2L x 2L blocks
     const int32_t *atom_type = nullptr;    // host [na]
     int panels = 1;                        // atom panels the contraction index is streamed in
+    bool sf = false;                       // structure-factor form (requires hoist)
+    const double *wt = nullptr;            // its per-type S weights [nt][2L]
+    const double2 *sf_tab = nullptr;       // its structure factors
 };
 struct OzGroup;
 // scratch: rewritten by every run (may be shared by the groups of a plan); persist: owned by
@@ -58,7 +63,7 @@ struct OzGroup;
 // Panels: the atoms split into `panels` contiguous ranges; only one panel's digit planes are
 // resident at a time (the scratch shrinks accordingly), the S/H products accumulate over panels.
 int64_t ozaki_group_bytes(int s, int64_t twoL, int64_t na, int64_t nt, const std::vector<int64_t> &G, int panels,
-                          bool hoist);
+                          bool hoist, bool sf);
 int64_t ozaki_group_persist_bytes(int s, int64_t twoL, int64_t na, int64_t nt, const std::vector<int64_t> &G,
                                   int panels);
 int ozaki_group_prepare(OzakiPlan &oz, const OzGroupDesc &d, const std::vector<OzKBufs> &kb, void *ws,

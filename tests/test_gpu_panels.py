@@ -27,7 +27,10 @@ def ctx():
 
 @pytest.fixture
 def env():
-    saved = {k: os.environ.get(k) for k in ("HSDLA_PANELS", "HSDLA_WORKSPACE_BUDGET")}
+    """Panels belong to the per-atom form of the contraction: the structure-factor form (taken when
+    no atom carries its own rotation) has small per-type digits and needs none, so it is off here."""
+    saved = {k: os.environ.get(k) for k in ("HSDLA_PANELS", "HSDLA_WORKSPACE_BUDGET", "HSDLA_SF")}
+    os.environ["HSDLA_SF"] = "0"
     yield os.environ
     for k, v in saved.items():
         if v is None:

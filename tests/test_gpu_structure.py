@@ -1,0 +1,61 @@
+"""The structure-factor form of S and H (atoms sharing their type's rotation): per-type
+contractions M_t^H diag(w_t) M_t and M_t^H Z_t combined with SF_t(g' - g) = sum_a e^{i 2pi (g'-g).tau_a}.
+It must agree with the per-atom form (HSDLA_SF=0) and with the oracle, in both precisions.
+Tolerance 1e-13 relative Frobenius and max-norm on the lower triangles."""
+import os
+
+import numpy as np
+import pytest
+
+import oracle
+from hybridhsdla_gb300 import api, synth
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-13
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no GPU")
+    c = api.Context()
+    yield c
+    c.close()
+
+
+def _run(ctx, s, precision, sf):
+    old = os.environ.get("HSDLA_SF")
+    os.environ["HSDLA_SF"] = "1" if sf else "0"
+    try:
+        return ctx.create_hs(s, precision=precision, num_slices=11 if precision == "ozaki" else 0)
+    finally:
+        if old is None:
+            os.environ.pop("HSDLA_SF")
+        else:
+            os.environ["HSDLA_SF"] = old
+
+
+@pytest.mark.parametrize("precision", ["fp64", "ozaki"])
+@pytest.mark.parametrize("cfg", ["t1", "c0", "c1"])
+def test_structure_factor_form_matches_per_atom_and_oracle(ctx, cfg, precision):
+    s = synth.make_system(cfg)
+    res_sf, rep_sf = _run(ctx, s, precision, True)
+    res_pa, _ = _run(ctx, s, precision, False)
+    for (H, S), (Hp, Sp), kp in zip(res_sf, res_pa, s.kpoints):
+        Hr, Sr = oracle.reference_hs(s, kp)
+        for X, P, R in ((H, Hp, Hr), (S, Sp, Sr)):
+            fro, mx = oracle.lower_errors(X, R)
+            assert fro < TOL and mx < TOL, (cfg, precision, fro, mx)
+            assert oracle.lower_errors(X, P)[0] < TOL
+        iu = np.triu_indices(kp.n_g, 1)
+        assert np.all(H[iu] == 0) and np.all(S[iu] == 0)
+
+
+def test_structure_factor_form_is_used(ctx):
+    """Without per-atom rotations the S/H work shrinks to one contraction of 2L rows per type."""
+    s = synth.make_system("c1")
+    _, r_sf = _run(ctx, s, "fp64", True)
+    _, r_pa = _run(ctx, s, "fp64", False)
+    ratio = r_pa["dominant_flop"] / r_sf["dominant_flop"]
+    assert abs(ratio - s.num_atoms / s.num_types) < 1e-9, ratio
