@@ -268,9 +268,9 @@ class Context:
         sh = _SysHolder(sys_, tmats)
         kh = _KptHolder(kpoints)
         nk = len(kpoints)
-        if out is None:
-            out = [(np.empty((kp.n_g, kp.n_g), np.complex128, order="F"),
-                    np.empty((kp.n_g, kp.n_g), np.complex128, order="F")) for kp in kpoints]
+        if out is None:      # zeroed: the library writes the lower triangles only
+            out = [(np.zeros((kp.n_g, kp.n_g), np.complex128, order="F"),
+                    np.zeros((kp.n_g, kp.n_g), np.complex128, order="F")) for kp in kpoints]
         Hp = (_cxp * max(nk, 1))(*[o[0].ctypes.data_as(_cxp) for o in out])
         Sp = (_cxp * max(nk, 1))(*[o[1].ctypes.data_as(_cxp) for o in out])
         ld = (ctypes.c_int64 * max(nk, 1))(*[max(1, o[0].shape[0]) for o in out])
@@ -294,8 +294,8 @@ class Context:
         pbb = (_cxp * a)(*[k[2].ctypes.data_as(_cxp) for k in keep])
         lmaxs = np.ascontiguousarray(d.lmaxs, np.int32)
         un = np.ascontiguousarray(d.sqrt_u_norms, np.float64)
-        H = np.empty((G, G), np.complex128, order="F")
-        S = np.empty((G, G), np.complex128, order="F")
+        H = np.zeros((G, G), np.complex128, order="F")     # the library writes the lower triangles
+        S = np.zeros((G, G), np.complex128, order="F")
         o = _opts(precision, num_slices)
         rep = ReportStruct()
         self.check(self.lib.hsdla_contract_ab(self.h, d.L, a, G, A.ctypes.data_as(_cxp), B.ctypes.data_as(_cxp),

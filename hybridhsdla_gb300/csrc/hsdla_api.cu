@@ -38,6 +38,9 @@ struct hsdla_context {
     // persistent workspace reused across calls (grows on demand)
     void *ws = nullptr;
     int64_t ws_bytes = 0;
+    // device H/S buffer of the host-buffer entry points, kept across calls (grows on demand)
+    void *hout = nullptr;
+    int64_t hout_bytes = 0;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr, evs[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
     std::set<hsdla_plan *> plans;   // live plans, destroyed with the context
     // slice autotuner results: (L, atoms, types, n_G bucket, target) -> (slices, predicted error)
@@ -81,7 +84,9 @@ struct hsdla_plan {
         int64_t tiles_sh = 0;
         void *persist = nullptr;         // prepared tables (not shared with other groups)
         int64_t persist_bytes = 0;
-        cudaEvent_t ev_dom[2] = {nullptr, nullptr};   // around the S/H launch (graph runs too)
+        // event pairs around the S/H product launches (one pair, or one per type in the
+        // structure-factor form; recorded under graph capture too)
+        std::vector<cudaEvent_t> ev_dom;
         SfTab sft{};                     // structure-factor combine of this group (outputs per run)
     };
     std::vector<Group> groups;
@@ -149,6 +154,36 @@ void ctx_free(hsdla_context *ctx, void *p, int64_t bytes) {
 }
 
 // Workspace of at least `bytes`, owned by the context (reused across calls).
+int ctx_host_out(hsdla_context *ctx, int64_t bytes, void **out) {
+    if (bytes <= ctx->hout_bytes && ctx->hout) { *out = ctx->hout; return HSDLA_OK; }
+    if (ctx->hout) {
+        cudaStreamSynchronize(ctx->stream);
+        ctx_free(ctx, ctx->hout, ctx->hout_bytes);
+        ctx->hout = nullptr;
+        ctx->hout_bytes = 0;
+    }
+    int rc = ctx_malloc(ctx, &ctx->hout, bytes);
+    if (rc) return rc;
+    ctx->hout_bytes = bytes;
+    *out = ctx->hout;
+    return HSDLA_OK;
+}
+
+// Download of the lower triangle of a column-major n x n device matrix into a host matrix of
+// leading dimension ld: column blocks of kDownBlock, each from its first row down (the strict
+// upper triangle outside the diagonal blocks is not copied; ~half the bytes of the full matrix).
+constexpr int64_t kDownBlock = 512;
+cudaError_t download_lower(hsdla_cx *host, int64_t ld, const hsdla_cx *dev, int64_t n, cudaStream_t st) {
+    for (int64_t c0 = 0; c0 < n; c0 += kDownBlock) {
+        const int64_t w = std::min(kDownBlock, n - c0);
+        const cudaError_t e = cudaMemcpy2DAsync(host + c0 + ld * c0, ld * sizeof(hsdla_cx), dev + c0 + n * c0,
+                                                n * sizeof(hsdla_cx), (n - c0) * sizeof(hsdla_cx), w,
+                                                cudaMemcpyDeviceToHost, st);
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
+
 int ctx_workspace(hsdla_context *ctx, int64_t bytes, void **out) {
     if (bytes <= ctx->ws_bytes && ctx->ws) { *out = ctx->ws; return HSDLA_OK; }
     if (ctx->ws) {
@@ -458,6 +493,7 @@ void hsdla_context_destroy(hsdla_context *ctx) {
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     while (!ctx->plans.empty()) hsdla_plan_destroy(*ctx->plans.begin());
     if (ctx->ws) ctx_free(ctx, ctx->ws, ctx->ws_bytes);
+    if (ctx->hout) ctx_free(ctx, ctx->hout, ctx->hout_bytes);
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
     if (ctx->ev1) cudaEventDestroy(ctx->ev1);
     for (auto &e : ctx->evs) if (e) cudaEventDestroy(e);
@@ -583,12 +619,14 @@ int hsdla_plan_create(hsdla_context *ctx, const hsdla_system *s, const hsdla_kpo
         add(sizeof(double) * 2 * L * nt);
         add(sizeof(double2) * (int64_t)na * (ext[0] + ext[1] + ext[2]));
         add(sizeof(int32_t) * (na + nt + 1));
-        add(sizeof(double2) * (int64_t)nt * ext[0] * ext[1] * ext[2]);
     }
+    // the structure-factor table comes last: it is filled on the device, not uploaded
+    const int64_t upload_bytes = bytes;
+    if (pl->sf) add(sizeof(double2) * (int64_t)nt * ext[0] * ext[1] * ext[2]);
     rc = ctx_malloc(ctx, &pl->tables, bytes);
     if (rc) { delete pl; return rc; }
     pl->tables_bytes = bytes;
-    std::vector<char> host(bytes, 0);
+    std::vector<char> host(upload_bytes, 0);
     char *hp = host.data();
     char *dp = reinterpret_cast<char *>(pl->tables);
     auto put = [&](const void *src, int64_t b) -> void * {
@@ -656,13 +694,13 @@ int hsdla_plan_create(hsdla_context *ctx, const hsdla_system *s, const hsdla_kpo
         tb[nt] = (int32_t)ord.size();
         ord.insert(ord.end(), tb.begin(), tb.end());
         d_order = (const int32_t *)put(ord.data(), sizeof(int32_t) * ord.size());
-        pl->sf_tab = (double2 *)put(nullptr, sizeof(double2) * (int64_t)nt * ext[0] * ext[1] * ext[2]);
+        pl->sf_tab = (double2 *)dp;   // past the uploaded part
         SfTab &dm = pl->sf_dims;
         dm.dx = half[0]; dm.dy = half[1]; dm.dz = half[2];
         dm.ny = ext[1]; dm.nz = ext[2];
         dm.box = (int64_t)ext[0] * ext[1] * ext[2];
     }
-    cudaError_t e = cudaMemcpyAsync(pl->tables, host.data(), bytes, cudaMemcpyHostToDevice, ctx->stream);
+    cudaError_t e = cudaMemcpyAsync(pl->tables, host.data(), upload_bytes, cudaMemcpyHostToDevice, ctx->stream);
     if (e == cudaSuccess && pl->sf)
         e = launch_sf_table(d_ex, d_ex + (size_t)na * ext[0], d_ex + (size_t)na * (ext[0] + ext[1]), d_order,
                             d_order + na, nt, ext[0], ext[1], ext[2], pl->sf_tab, ctx->stream);
@@ -782,7 +820,7 @@ void release_groups(hsdla_plan *pl) {
         if (g.h_jobs_sh) cudaFreeHost(g.h_jobs_sh);
         if (g.persist) ctx_free(pl->ctx, g.persist, g.persist_bytes);
         for (auto &e : g.ev_dom) if (e) cudaEventDestroy(e);
-        g.ev_dom[0] = g.ev_dom[1] = nullptr;
+        g.ev_dom.clear();
         g.oz = nullptr;
         g.h_jobs_sh = nullptr;
         g.persist = nullptr;
@@ -803,8 +841,8 @@ int prepare_groups(hsdla_plan *pl, void *ws, cudaStream_t st) {
         g.persist_bytes = group_persist_bytes(pl, g.kidx);
         int rcp = ctx_malloc(ctx, &g.persist, g.persist_bytes);
         if (rcp) return rcp;
-        CUDA_TRY(ctx, cudaEventCreate(&g.ev_dom[0]));
-        CUDA_TRY(ctx, cudaEventCreate(&g.ev_dom[1]));
+        g.ev_dom.assign(pl->sf ? 2 * pl->nt : 2, nullptr);
+        for (auto &e : g.ev_dom) CUDA_TRY(ctx, cudaEventCreate(&e));
         char *pp = reinterpret_cast<char *>(g.persist);
         auto keep = [&](int64_t bytes) { char *r = pp; pp += (bytes + 1023) / 1024 * 1024; return r; };
         KTable &kt = g.ktab;
@@ -982,7 +1020,8 @@ float dominant_ms(const hsdla_plan *pl) {
     float tot = 0.f;
     for (const auto &g : pl->groups) {
         float d = 0.f;
-        if (g.ev_dom[0] && cudaEventElapsedTime(&d, g.ev_dom[0], g.ev_dom[1]) == cudaSuccess) tot += d;
+        for (size_t i = 0; i + 1 < g.ev_dom.size(); i += 2)
+            if (g.ev_dom[i] && cudaEventElapsedTime(&d, g.ev_dom[i], g.ev_dom[i + 1]) == cudaSuccess) tot += d;
     }
     cudaGetLastError();
     return tot;
@@ -1024,21 +1063,21 @@ int run_groups(hsdla_plan *pl, cudaStream_t st, bool timed, float *ms_ab, float 
         }
         if (g.oz) {
             int nl = 0;
-            const int rc = ozaki_group_run(g.oz, pl->dsys, g.ktab, st, g.ev_dom[0], g.ev_dom[1], &nl);
+            const int rc = ozaki_group_run(g.oz, pl->dsys, g.ktab, st, g.ev_dom.data(), (int)g.ev_dom.size(), &nl);
             if (rc) return set_err(ctx, rc, "Ozaki group failed: %s", ozaki_last_error());
             pl->launches += nl;
         } else if (pl->sf) {
             CUDA_TRY(ctx, launch_fp64_jobs(g.d_jobs_t, g.n_jobs_t, g.tiles_t, st));
             pl->launches++;
-            CUDA_TRY(ctx, record_event(g.ev_dom[0], st));
             const int nj = 2 * g.ktab.nk;
             for (int t = 0; t < pl->nt; ++t) {
+                CUDA_TRY(ctx, record_event(g.ev_dom[2 * t], st));
                 CUDA_TRY(ctx, launch_fp64_jobs(g.d_jobs_sh + (int64_t)nj * t, nj, g.tiles_sh, st));
+                CUDA_TRY(ctx, record_event(g.ev_dom[2 * t + 1], st));
                 g.sft.type = t;
                 CUDA_TRY(ctx, launch_sf_combine(g.sft, pl->sf_tab, t == 0, st));
                 pl->launches += 2;
             }
-            CUDA_TRY(ctx, record_event(g.ev_dom[1], st));
         } else {
             CUDA_TRY(ctx, launch_fp64_jobs(g.d_jobs_t, g.n_jobs_t, g.tiles_t, st));
             pl->launches++;
@@ -1055,7 +1094,7 @@ int run_groups(hsdla_plan *pl, cudaStream_t st, bool timed, float *ms_ab, float 
         }
         if (timed) {
             // stage times need the events: wait for this group (un-graphed runs only)
-            CUDA_TRY(ctx, cudaEventSynchronize(g.ev_dom[1]));
+            CUDA_TRY(ctx, cudaEventSynchronize(g.ev_dom.back()));
             float a = 0;
             cudaEventElapsedTime(&a, ctx->evs[0], ctx->evs[1]);
             *ms_ab += a;
@@ -1299,7 +1338,6 @@ int hsdla_contract_ab(hsdla_context *ctx, int32_t L, int32_t a, int64_t G, const
     void *dout = nullptr, *ws = nullptr;
     auto done = [&](int code) {
         cudaStreamSynchronize(st);
-        if (dout) ctx_free(ctx, dout, 2 * G * G * (int64_t)sizeof(double2));
         hsdla_plan_destroy(pl);
         cudaEventDestroy(e0);
         cudaEventDestroy(e1);
@@ -1322,7 +1360,7 @@ int hsdla_contract_ab(hsdla_context *ctx, int32_t L, int32_t a, int64_t G, const
     if (rc) return done(rc);
     rc = prepare_groups(pl, ws, st);
     if (rc) return done(rc);
-    rc = ctx_malloc(ctx, &dout, 2 * G * G * (int64_t)sizeof(double2));
+    rc = ctx_host_out(ctx, 2 * G * G * (int64_t)sizeof(double2), &dout);
     if (rc) return done(rc);
     hsdla_cx *dH = reinterpret_cast<hsdla_cx *>(dout), *dS = dH + G * G;
     const int64_t ldd = G;
@@ -1339,10 +1377,7 @@ int hsdla_contract_ab(hsdla_context *ctx, int32_t L, int32_t a, int64_t G, const
     double dom_flop = 0.0;
     rc = run_groups(pl, st, true, &ms_ab, &ms_dom, &dom_flop);
     if (rc) return done(rc);
-    if (cudaMemcpy2DAsync(H, ld * sizeof(hsdla_cx), dH, G * sizeof(hsdla_cx), G * sizeof(hsdla_cx), G,
-                          cudaMemcpyDeviceToHost, st) != cudaSuccess ||
-        cudaMemcpy2DAsync(S, ld * sizeof(hsdla_cx), dS, G * sizeof(hsdla_cx), G * sizeof(hsdla_cx), G,
-                          cudaMemcpyDeviceToHost, st) != cudaSuccess)
+    if (download_lower(H, ld, dH, G, st) != cudaSuccess || download_lower(S, ld, dS, G, st) != cudaSuccess)
         return done(set_err(ctx, HSDLA_ERR_CUDA, "H/S download failed"));
     cudaEventRecord(e1, st);
     if (cudaStreamSynchronize(st) != cudaSuccess) return done(set_err(ctx, HSDLA_ERR_CUDA, "sync failed"));
@@ -1387,7 +1422,7 @@ int hsdla_create_hs(hsdla_context *ctx, const hsdla_system *s, const hsdla_kpoin
     int64_t out_elems = 0;
     for (int i = 0; i < nk; ++i) { ng[i] = kpts[i].n_g; out_elems += 2 * ng[i] * ng[i]; }
     void *dout = nullptr;
-    rc = ctx_malloc(ctx, &dout, out_elems * (int64_t)sizeof(double2));
+    rc = ctx_host_out(ctx, std::max<int64_t>(out_elems, 1) * (int64_t)sizeof(double2), &dout);
     if (rc) { hsdla_plan_destroy(pl); cudaEventDestroy(e0); cudaEventDestroy(e1); return rc; }
     std::vector<hsdla_cx *> dH(nk), dS(nk);
     std::vector<int64_t> dld(nk);
@@ -1397,7 +1432,7 @@ int hsdla_create_hs(hsdla_context *ctx, const hsdla_system *s, const hsdla_kpoin
         dS[i] = p; p += ng[i] * ng[i];
         dld[i] = std::max<int64_t>(ng[i], 1);
     }
-    // the upper triangles of the outputs are returned as zero
+    // zero device outputs: the diagonal blocks of the download carry their upper triangles
     cudaError_t e = cudaMemsetAsync(dout, 0, out_elems * sizeof(double2), ctx->stream);
     if (e == cudaSuccess) {
         rc = hsdla_plan_execute(pl, dH.data(), dS.data(), dld.data(), ctx->stream, rep);
@@ -1406,11 +1441,8 @@ int hsdla_create_hs(hsdla_context *ctx, const hsdla_system *s, const hsdla_kpoin
     }
     for (int i = 0; rc == HSDLA_OK && i < nk; ++i) {
         if (ng[i] == 0) continue;
-        e = cudaMemcpy2DAsync(H[i], ld[i] * sizeof(hsdla_cx), dH[i], ng[i] * sizeof(hsdla_cx),
-                              ng[i] * sizeof(hsdla_cx), ng[i], cudaMemcpyDeviceToHost, ctx->stream);
-        if (e == cudaSuccess)
-            e = cudaMemcpy2DAsync(S[i], ld[i] * sizeof(hsdla_cx), dS[i], ng[i] * sizeof(hsdla_cx),
-                                  ng[i] * sizeof(hsdla_cx), ng[i], cudaMemcpyDeviceToHost, ctx->stream);
+        e = download_lower(H[i], ld[i], dH[i], ng[i], ctx->stream);
+        if (e == cudaSuccess) e = download_lower(S[i], ld[i], dS[i], ng[i], ctx->stream);
         if (e != cudaSuccess) rc = set_err(ctx, HSDLA_ERR_CUDA, "D2H copy failed: %s", cudaGetErrorString(e));
     }
     cudaEventRecord(e1, ctx->stream);
@@ -1423,7 +1455,6 @@ int hsdla_create_hs(hsdla_context *ctx, const hsdla_system *s, const hsdla_kpoin
         rep->ms_per_kpoint = nk ? ms / nk : 0.0;
         rep->eff_tflops = ms > 0 ? pl->flop / (ms * 1e-3) / 1e12 : 0.0;
     }
-    ctx_free(ctx, dout, out_elems * (int64_t)sizeof(double2));
     hsdla_plan_destroy(pl);
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);

@@ -1976,8 +1976,9 @@ static cudaError_t record(cudaEvent_t ev, cudaStream_t st) {
 // T application (or phase expansion), X digits, the S/H products (accumulating after the first
 // panel).  With several panels the events span the panels' S/H launches and the slicing between
 // them.
-int ozaki_group_run(OzGroup *g, const DevSystem &sys, const KTable &ktab, cudaStream_t st, cudaEvent_t ev0,
-                    cudaEvent_t ev1, int *launches) {
+int ozaki_group_run(OzGroup *g, const DevSystem &sys, const KTable &ktab, cudaStream_t st, const cudaEvent_t *ev,
+                    int nev, int *launches) {
+    const cudaEvent_t ev0 = nev >= 2 ? ev[0] : nullptr, ev1 = nev >= 2 ? ev[nev - 1] : nullptr;
     int nl = 0;
     cudaError_t e = cudaSuccess;
     if (g->sf) {
@@ -1987,20 +1988,21 @@ int ozaki_group_run(OzGroup *g, const DevSystem &sys, const KTable &ktab, cudaSt
                                 st);
         if (e == cudaSuccess) e = slice_launch(g->pan[0].tX, st);    // Z
         nl += 3;
-        if (e == cudaSuccess && ev0) e = record(ev0, st);
         for (int t = 0; t < g->nt && e == cudaSuccess; ++t) {
             const OzJob *jobs = g->d_jobs_sh + (int64_t)g->n_jobs_sh * t;
-            e = g->pair ? launch_pair(g->maps_sh, g->s, g->d_err, jobs, g->n_jobs_sh, g->tiles_sh, g->d_list_sh,
-                                      g->d_progress, st)
-                        : launch_prepared(g->maps_sh, g->s, g->d_err, jobs, g->n_jobs_sh, g->tiles_sh, g->d_list_sh,
-                                          g->d_progress, st);
+            if (nev >= 2 * g->nt) e = record(ev[2 * t], st);
+            if (e == cudaSuccess)
+                e = g->pair ? launch_pair(g->maps_sh, g->s, g->d_err, jobs, g->n_jobs_sh, g->tiles_sh, g->d_list_sh,
+                                          g->d_progress, st)
+                            : launch_prepared(g->maps_sh, g->s, g->d_err, jobs, g->n_jobs_sh, g->tiles_sh,
+                                              g->d_list_sh, g->d_progress, st);
+            if (e == cudaSuccess && nev >= 2 * g->nt) e = record(ev[2 * t + 1], st);
             if (e == cudaSuccess) {
                 g->sft.type = t;
                 e = launch_sf_combine(g->sft, g->sf_tab, t == 0, st);
             }
             nl += 2;
         }
-        if (e == cudaSuccess && ev1) e = record(ev1, st);
         if (launches) *launches = nl;
         if (e != cudaSuccess) { g_oz_err = cudaGetErrorString(e); return HSDLA_ERR_CUDA; }
         return HSDLA_OK;
@@ -2084,7 +2086,8 @@ int ozaki_pipeline(OzakiPlan &oz, const OzakiInputs &in, double2 *S, double2 *H,
     KTable kt;
     kt.nk = 1; kt.ldc = in.twoL * in.na; kt.ldm = in.twoL * in.nt; kt.total_cols = in.G;
     if (in.kp) kt.e[0] = KEntry{*in.kp, nullptr, nullptr, in.Z, kb[0].CX, 0};
-    rc = ozaki_group_run(g, in.sys ? *in.sys : DevSystem{}, kt, st, in.ev_dom0, in.ev_dom1, launches);
+    const cudaEvent_t evs[2] = {in.ev_dom0, in.ev_dom1};
+    rc = ozaki_group_run(g, in.sys ? *in.sys : DevSystem{}, kt, st, evs, in.ev_dom0 ? 2 : 0, launches);
     if (rc == HSDLA_OK && cudaStreamSynchronize(st) != cudaSuccess) rc = HSDLA_ERR_CUDA;
     ozaki_group_destroy(g);
     return rc;

@@ -72,8 +72,10 @@ void ozaki_group_set_outputs(OzGroup *g, double2 *const *S, double2 *const *H, c
 // Structure-factor form: the group's combine table (outputs of this run, per-type products).
 void ozaki_group_set_sf(OzGroup *g, const SfTab &t);
 // Enqueues the group's launches (slices, T application, phases, S/H products); no host sync.
-int ozaki_group_run(OzGroup *g, const DevSystem &sys, const KTable &ktab, cudaStream_t st, cudaEvent_t ev0,
-                    cudaEvent_t ev1, int *launches);
+// ev: event pairs recorded around the S/H product launches (one pair, or one per type in the
+// structure-factor form; nev events, may be 0).
+int ozaki_group_run(OzGroup *g, const DevSystem &sys, const KTable &ktab, cudaStream_t st, const cudaEvent_t *ev,
+                    int nev, int *launches);
 void ozaki_group_destroy(OzGroup *g);
 
 int ozaki_plan_init(OzakiPlan &oz, int num_slices, double target);

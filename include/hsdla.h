@@ -29,7 +29,11 @@
  *     R = mrot bmat per atom (tensor_AB_match.cpp:97, FleurData.cpp:453-455);
  *   - lm index = l(l+1)+m, L = (max_lmax+1)^2;
  *   - H, S: n_G x n_G column-major with leading dimension ld; only the lower
- *     triangle (row >= column) is written, the upper triangle is left untouched.
+ *     triangle (row >= column) is defined.  Entry points with device outputs leave the
+ *     strict upper triangle untouched.  The host-buffer entry points (hsdla_create_hs,
+ *     hsdla_contract_ab) download 512-column blocks from their first row down, which sets
+ *     the strict upper triangle of the diagonal 512 x 512 blocks to zero and leaves the rest
+ *     of it untouched (the reference leaves it unset as well).
  */
 #ifndef HSDLA_H
 #define HSDLA_H
@@ -153,7 +157,7 @@ int hsdla_create_hs(hsdla_context *ctx, const hsdla_system *sys, const hsdla_kpo
  * column-major blocks t_aa[j], t_ab[j], t_bb[j] (the reference's myTMat; T_AA/T_BB through their
  * lower triangles, smaller blocks act zero-padded).  lmaxs[a], sqrt_u_norms[a][max_lmax+1] =
  * sqrt(||udot_l||^2) as the reference packs them (h_and_s.cpp:700-715).  H, S: HOST G x G,
- * leading dimension ld; lower triangles written, upper triangles set to zero.  With Ozaki
+ * leading dimension ld; lower triangles written (upper triangles: see the conventions above).  With Ozaki
  * precision, num_slices = 0 selects the default slice count (no sampling autotune here). */
 int hsdla_contract_ab(hsdla_context *ctx, int32_t L, int32_t num_atoms, int64_t n_g, const hsdla_cx *A,
                       const hsdla_cx *B, const int32_t *t_sizes, const hsdla_cx *const *t_aa,
