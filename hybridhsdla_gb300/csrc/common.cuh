@@ -94,14 +94,15 @@ cudaError_t launch_fp64_jobs(const Fp64Job *d_jobs, int num_jobs, int64_t total_
 // One k-point of a combine: per-type products PS, PH (lower triangles, ld ldp) into the outputs
 // S, H (ld ldo); g the k-point's G-vectors [n][3] on the device.
 struct SfEntry {
-    const double2 *PS = nullptr, *PH = nullptr;
+    const double2 *PS = nullptr, *PH = nullptr;   // per-type products, type slot b at + b pstride
     double2 *S = nullptr, *H = nullptr;
-    int64_t ldp = 0, ldo = 0, n = 0;
+    int64_t ldp = 0, ldo = 0, n = 0, pstride = 0;
     const int32_t *g = nullptr;
     int64_t tile_begin = 0;
 };
 struct SfTab {
-    int nk = 0, type = 0;
+    int nk = 0, type = 0, ntypes = 1;             // the batch: types [type, type + ntypes) in slots 0..
+
     int dx = 0, dy = 0, dz = 0, ny = 0, nz = 0;   // box offsets (half widths) and extents
     int64_t box = 0;                              // entries per type
     SfEntry e[kMaxGroup];
@@ -110,7 +111,8 @@ struct SfTab {
 // per-atom factors ex[a][dGx + dx] = e^{i 2pi dGx tau_a,x} (and y, z); atoms listed by type.
 cudaError_t launch_sf_table(const double2 *ex, const double2 *ey, const double2 *ez, const int32_t *order,
                             const int32_t *type_begin, int nt, int nx, int ny, int nz, double2 *sf, cudaStream_t st);
-// S (+)= SF_t (.) PS and H (+)= SF_t (.) PH over the lower triangles of every entry (t = tab.type).
+// S (+)= sum_b SF_{type+b} (.) PS_b and H (+)= sum_b SF_{type+b} (.) PH_b over the lower triangles
+// of every entry, b over the batch's type slots.
 cudaError_t launch_sf_combine(const SfTab &tab, const double2 *sf, bool first, cudaStream_t st);
 
 // Fleur's packed lower triangle (row by row) of a column-major n x n matrix (device buffers).

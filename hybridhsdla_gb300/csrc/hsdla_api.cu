@@ -106,6 +106,7 @@ struct hsdla_plan {
     double *wt = nullptr;
     double2 *sf_tab = nullptr;
     SfTab sf_dims{};                 // box extents and offsets (entries filled per group)
+    int tbatch = 1;                  // types whose products are combined into S and H in one pass
     double est_err = 0.0;            // autotuner's predicted relative error
     int launches = 0;
 };
@@ -727,8 +728,8 @@ namespace {
 int64_t kpoint_fp64_bytes(const hsdla_plan *pl, int64_t G) {
     const int64_t K = pl->twoLa, ldm = 2 * (int64_t)pl->L * pl->nt;
     auto r = [](int64_t x) { return (x + 1023) / 1024 * 1024; };        // each buffer is 1 KB aligned
-    // structure-factor form: M, Z and the two per-type products (no C, no X)
-    if (pl->sf) return 2 * r(ldm * G * (int64_t)sizeof(double2)) + 2 * r(G * G * (int64_t)sizeof(double2));
+    // structure-factor form: M, Z and the two products of each type of a combine batch (no C, no X)
+    if (pl->sf) return 2 * r(ldm * G * (int64_t)sizeof(double2)) + 2 * r(pl->tbatch * G * G * (int64_t)sizeof(double2));
     const int64_t nCX = pl->opts.precision == HSDLA_PREC_FP64 ? 2 : 1;   // FP64 keeps C and X apart
     int64_t b = nCX * r(K * G * (int64_t)sizeof(double2));
     if (pl->hoist) b += 2 * r(ldm * G * (int64_t)sizeof(double2));
@@ -787,9 +788,28 @@ void choose_panels(hsdla_plan *pl, int64_t budget) {
     while (pl->panels < pl->na && group_bytes(pl, one) > budget) ++pl->panels;
 }
 
+// Structure-factor form: the most types per combine batch (each type of a batch keeps its own
+// products, and the batch reads and writes S and H once) whose one-k-point workspace fits the
+// budget; HSDLA_TYPE_BATCH forces a count.
+void choose_type_batch(hsdla_plan *pl, int64_t budget) {
+    pl->tbatch = 1;
+    if (!pl->sf) return;
+    const char *ev = getenv("HSDLA_TYPE_BATCH");
+    const int64_t forced = ev ? strtoll(ev, nullptr, 10) : 0;
+    if (forced > 0) { pl->tbatch = (int)std::min<int64_t>(forced, pl->nt); return; }
+    int big = -1;
+    for (int i = 0; i < (int)pl->kps.size(); ++i)
+        if (pl->kps[i].n_g > 0 && (big < 0 || pl->kps[i].n_g > pl->kps[big].n_g)) big = i;
+    if (big < 0) return;
+    const std::vector<int> one{big};
+    pl->tbatch = pl->nt;
+    while (pl->tbatch > 1 && group_bytes(pl, one) > budget) --pl->tbatch;
+}
+
 // Greedy k-point groups whose workspace fits the budget (at least one k-point per group).
 void form_groups(hsdla_plan *pl, int64_t budget) {
     choose_panels(pl, budget);
+    choose_type_batch(pl, budget);
     pl->groups.clear();
     std::vector<int> cur;
     for (int i = 0; i < (int)pl->kps.size(); ++i) {
@@ -872,15 +892,16 @@ int prepare_groups(hsdla_plan *pl, void *ws, cudaStream_t st) {
             if (pl->sf) {
                 SfEntry &f = g.sft.e[q];
                 f = SfEntry();
-                f.PS = reinterpret_cast<double2 *>(take(G * G * (int64_t)sizeof(double2)));
-                f.PH = reinterpret_cast<double2 *>(take(G * G * (int64_t)sizeof(double2)));
-                f.ldp = G; f.n = G; f.g = pk.dk.g;
+                f.PS = reinterpret_cast<double2 *>(take(pl->tbatch * G * G * (int64_t)sizeof(double2)));
+                f.PH = reinterpret_cast<double2 *>(take(pl->tbatch * G * G * (int64_t)sizeof(double2)));
+                f.ldp = G; f.n = G; f.pstride = G * G; f.g = pk.dk.g;
             }
             OzKBufs b;
             b.CX = e.C; b.M = e.M; b.Z = Z; b.G = G;
             if (pl->sf) {
                 b.PS = const_cast<double2 *>(g.sft.e[q].PS);
                 b.PH = const_cast<double2 *>(g.sft.e[q].PH);
+                b.pstride = g.sft.e[q].pstride;
             }
             kb.push_back(b);
         }
@@ -896,7 +917,7 @@ int prepare_groups(hsdla_plan *pl, void *ws, cudaStream_t st) {
             d.twoL = twoL; d.na = pl->na; d.nt = pl->nt; d.hoist = pl->hoist;
             d.w = pl->w; d.Tfull = pl->Tfull; d.atom_type = pl->atom_type.data();
             d.panels = pl->panels;
-            d.sf = pl->sf; d.wt = pl->wt; d.sf_tab = pl->sf_tab;
+            d.sf = pl->sf; d.wt = pl->wt; d.sf_tab = pl->sf_tab; d.tbatch = pl->tbatch;
             char *oz_ws = reinterpret_cast<char *>((reinterpret_cast<uintptr_t>(p) + 1023) & ~uintptr_t(1023));
             int rc = ozaki_group_prepare(pl->oz, d, kb, oz_ws, g.persist, st, &g.oz);
             if (rc) return set_err(ctx, rc, "group set-up failed: %s", ozaki_last_error());
@@ -945,11 +966,12 @@ int prepare_groups(hsdla_plan *pl, void *ws, cudaStream_t st) {
                         Fp64Job js{};
                         js.P = e.M + twoL * t; js.ldp = ldm; js.Q = e.M + twoL * t; js.ldq = ldm;
                         js.w = pl->wt + twoL * t;
-                        js.out = const_cast<double2 *>(g.sft.e[q].PS); js.ldo = G;
+                        const int64_t slot = (int64_t)(t % pl->tbatch) * g.sft.e[q].pstride;
+                        js.out = const_cast<double2 *>(g.sft.e[q].PS) + slot; js.ldo = G;
                         js.m = G; js.n = G; js.k = twoL; js.lower = 1;
                         Fp64Job jh = js;
                         jh.Q = e.Z + twoL * t; jh.w = nullptr;
-                        jh.out = const_cast<double2 *>(g.sft.e[q].PH);
+                        jh.out = const_cast<double2 *>(g.sft.e[q].PH) + slot;
                         jt_sh.push_back(js);
                         jt_sh.push_back(jh);
                     }
@@ -1074,9 +1096,15 @@ int run_groups(hsdla_plan *pl, cudaStream_t st, bool timed, float *ms_ab, float 
                 CUDA_TRY(ctx, record_event(g.ev_dom[2 * t], st));
                 CUDA_TRY(ctx, launch_fp64_jobs(g.d_jobs_sh + (int64_t)nj * t, nj, g.tiles_sh, st));
                 CUDA_TRY(ctx, record_event(g.ev_dom[2 * t + 1], st));
-                g.sft.type = t;
-                CUDA_TRY(ctx, launch_sf_combine(g.sft, pl->sf_tab, t == 0, st));
-                pl->launches += 2;
+                pl->launches++;
+                // the batch's last type: its products into S and H
+                if ((t + 1) % pl->tbatch == 0 || t + 1 == pl->nt) {
+                    const int t0 = t / pl->tbatch * pl->tbatch;
+                    g.sft.type = t0;
+                    g.sft.ntypes = t + 1 - t0;
+                    CUDA_TRY(ctx, launch_sf_combine(g.sft, pl->sf_tab, t0 == 0, st));
+                    pl->launches++;
+                }
             }
         } else {
             CUDA_TRY(ctx, launch_fp64_jobs(g.d_jobs_t, g.n_jobs_t, g.tiles_t, st));

@@ -255,9 +255,10 @@ constexpr int kPow2Lo = -1022, kPow2Hi = 999;
 __device__ __forceinline__ bool pow2_ok(int k) { return k >= kPow2Lo && k <= kPow2Hi; }
 __device__ __forceinline__ double f32_pow2_to_f64_fast(uint32_t f, uint32_t ebias) {
     const uint32_t a = f & 0x7fffffffu;
-    const uint32_t hi = (f & 0x80000000u) | ((a >> 3) + ebias);
+    // a signed zero keeps its bits (high word = f, low word = 0)
+    const uint32_t hi = a ? ((f & 0x80000000u) | ((a >> 3) + ebias)) : f;
     const uint32_t lo = f << 29;
-    return a ? __hiloint2double((int)hi, (int)lo) : 0.0;
+    return __hiloint2double((int)hi, (int)lo);
 }
 __device__ __noinline__ double f32_pow2_to_f64_slow(uint32_t f, int k) { return ldexp((double)__uint_as_float(f), k); }
 __device__ __forceinline__ uint32_t pow2_ebias(int k) { return (uint32_t)(1023 - 127 + k) << 20; }
@@ -513,21 +514,46 @@ __global__ void __launch_bounds__(kThreads, 1)
 // Every wait is bounded as in oz_gemm_kernel; both CTAs meet at a cluster barrier before TMEM
 // is freed, so no CTA exits while its shared memory or TMEM can still be addressed by the other.
 constexpr int kPairTile = 256;
-constexpr int kStageCols = 4;                               // columns per drain staging buffer
-constexpr int kStageWarpBytes = 2 * kStageCols * 32 * 16;  // two buffers x 4 columns x 32 rows x 16 B
+#ifndef HSDLA_DRAIN_COLS
+#define HSDLA_DRAIN_COLS 4
+#endif
+#ifndef HSDLA_DRAIN_BUFS
+#define HSDLA_DRAIN_BUFS 2
+#endif
+constexpr int kStageCols = HSDLA_DRAIN_COLS;                 // columns per drain staging buffer
+constexpr int kDrainBufs = HSDLA_DRAIN_BUFS;                 // staging buffers per epilogue warp
+constexpr int kStageWarpBytes = kDrainBufs * kStageCols * 32 * 16;   // buffers x columns x 32 rows x 16 B
+static_assert(32 % kStageCols == 0 && kDrainBufs >= 2, "drain staging shape");
+static_assert(kPairTile / 2 == 4 * 32, "four 32-column chunks per epilogue warp (the exponent rotation)");
 constexpr int kPairStageBytes = kEpiWarps * kStageWarpBytes;
-__device__ __forceinline__ void bulk_store_g(void *gdst, uint32_t ssrc, uint32_t bytes) {
-    asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;\n" ::"l"(gdst), "r"(ssrc), "r"(bytes)
+// Bulk copies and f64 add-reductions shared memory -> global with an L2 eviction policy
+// (createpolicy): an output tile stays resident through its units (evict_last) and leaves first
+// after its last one (evict_first).
+__device__ __forceinline__ void bulk_store_g(void *gdst, uint32_t ssrc, uint32_t bytes, uint64_t pol) {
+    asm volatile("cp.async.bulk.global.shared::cta.bulk_group.L2::cache_hint [%0], [%1], %2, %3;\n" ::"l"(gdst),
+                 "r"(ssrc), "r"(bytes), "l"(pol)
                  : "memory");
 }
-__device__ __forceinline__ void bulk_add_g(void *gdst, uint32_t ssrc, uint32_t bytes) {
-    asm volatile("cp.reduce.async.bulk.global.shared::cta.bulk_group.add.f64 [%0], [%1], %2;\n" ::"l"(gdst),
-                 "r"(ssrc), "r"(bytes)
+__device__ __forceinline__ void bulk_add_g(void *gdst, uint32_t ssrc, uint32_t bytes, uint64_t pol) {
+    asm volatile("cp.reduce.async.bulk.global.shared::cta.bulk_group.L2::cache_hint.add.f64 [%0], [%1], %2, %3;\n" ::"l"(
+                     gdst),
+                 "r"(ssrc), "r"(bytes), "l"(pol)
                  : "memory");
+}
+__device__ __forceinline__ uint64_t policy_evict_last() {
+    uint64_t p;
+    asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;\n" : "=l"(p));
+    return p;
+}
+__device__ __forceinline__ uint64_t policy_evict_first() {
+    uint64_t p;
+    asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;\n" : "=l"(p));
+    return p;
 }
 __device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;\n" ::: "memory"); }
 __device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;\n" ::: "memory"); }
-__device__ __forceinline__ void bulk_wait_read_1() { asm volatile("cp.async.bulk.wait_group.read 1;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void bulk_wait_read() { asm volatile("cp.async.bulk.wait_group.read %0;\n" ::"n"(N) : "memory"); }
 __device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory"); }
 
 __device__ __forceinline__ uint32_t cluster_rank() {
@@ -762,23 +788,37 @@ __global__ void __launch_bounds__(kThreads, 1)
         const int cbeg = ((warp - 2) >> 2) * (kPairTile / 2);   // its half of the columns
         unsigned char *stg = smem + kStages * kStageBytes + (warp - 2) * kStageWarpBytes;
         const uint32_t stg_s = smem_u32(stg);
+        const uint64_t pol_last = policy_evict_last(), pol_first = policy_evict_first();
         int64_t unit = 0;
         bool ok = true;
         for (int64_t tile = pair; ok && tile < total_tiles; tile += npairs) {
             int64_t tm, tn;
             const OzJob &j = resolve_tile(jobs, num_jobs, tile_list, tile, tm, tn);
             const int64_t r0 = tm * kPairTile + half + q * 32, row = r0 + lane;
-            const int64_t m = j.m, n = j.n, ldo = j.ldo;
-            const bool row_ok = row < m;
-            const int erow = row_ok ? j.el[row] : 0;
-            const bool lower = j.lower != 0;
-            const int32_t *er = j.er;
+            const int64_t m = j.m, n = j.n, ldo = j.ldo, nkb = j.nkb;
+            const bool lower = j.lower != 0, accum = j.accum != 0;
+            const int erow = row < m ? j.el[row] : 0;
             double2 *out = j.out;
+            // The tile's column exponents, loaded once for all its units: lane l holds column
+            // colt + 32 c + l of chunk c in e0..e3 (rotated after each chunk, so the current chunk's
+            // are always in e0), with each chunk's range for the fast-path test.
+            const int64_t colt = tn * kPairTile + cbeg;
+            const int32_t *er = j.er;
+            int e0 = colt + lane < n ? __ldg(er + colt + lane) : 0;
+            int e1 = colt + 32 + lane < n ? __ldg(er + colt + 32 + lane) : 0;
+            int e2 = colt + 64 + lane < n ? __ldg(er + colt + 64 + lane) : 0;
+            int e3 = colt + 96 + lane < n ? __ldg(er + colt + 96 + lane) : 0;
+            int lo0 = __reduce_min_sync(0xffffffffu, e0), hi0 = __reduce_max_sync(0xffffffffu, e0);
+            int lo1 = __reduce_min_sync(0xffffffffu, e1), hi1 = __reduce_max_sync(0xffffffffu, e1);
+            int lo2 = __reduce_min_sync(0xffffffffu, e2), hi2 = __reduce_max_sync(0xffffffffu, e2);
+            int lo3 = __reduce_min_sync(0xffffffffu, e3), hi3 = __reduce_max_sync(0xffffffffu, e3);
             for (int t = 2; ok && t <= s + 1; ++t) {
                 const int ilo = max(1, t - s), ihi = min(s, t - 1);
                 const int64_t ck = chunk_kblocks(ihi - ilo + 1);
-                for (int64_t cb = 0; ok && cb < j.nkb; cb += ck) {
-                    const bool first = (t == 2 && cb == 0) && !j.accum;
+                const int kb = 2 - 5 * t + erow;
+                for (int64_t cb = 0; ok && cb < nkb; cb += ck) {
+                    const bool first = (t == 2 && cb == 0) && !accum;
+                    const uint64_t pol = (t == s + 1 && cb + ck >= nkb) ? pol_first : pol_last;
                     if (!pwait(&bars.tfull, (uint32_t)(unit & 1), 4, warp, (int)unit)) { ok = false; break; }
                     tc_fence_after();
                     // the previous unit's copies are complete: successive updates stay in order
@@ -796,46 +836,51 @@ __global__ void __launch_bounds__(kThreads, 1)
                             __syncwarp();
                             if (lane == 0) mbar_arrive_remote(tempty_leader);
                         }
-                        const int64_t colb = tn * kPairTile + c0;
-                        // the 32 column exponents: one coalesced load, then broadcasts
-                        const int ecl = colb + lane < n ? __ldg(er + colb + lane) : 0;
-                        const int kb = 2 - 5 * t + erow;
-                        const bool fast = __all_sync(0xffffffffu, pow2_ok(kb + __reduce_min_sync(0xffffffffu, ecl)) &&
-                                                                      pow2_ok(kb + __reduce_max_sync(0xffffffffu, ecl)));
+                        const int64_t colb = colt + (c0 - cbeg);
+                        const bool fast = __all_sync(0xffffffffu, pow2_ok(kb + lo0) && pow2_ok(kb + hi0));
+                        // 2^(kb + e_col) as an FP64 exponent bias: the row's part plus e_col << 20
+                        const uint32_t rbias = pow2_ebias(kb);
 #pragma unroll
                         for (int g4 = 0; g4 < 32; g4 += kStageCols, ++rd) {
-                            const uint32_t buf = (uint32_t)(rd & 1) * (kStageCols * 512);
-                            if (lane < kStageCols) bulk_wait_read_1();
+                            const uint32_t buf = (uint32_t)(rd % kDrainBufs) * (kStageCols * 512);
+                            if (lane < kStageCols) bulk_wait_read<kDrainBufs - 1>();
                             __syncwarp();
 #pragma unroll
                             for (int cc = 0; cc < kStageCols; ++cc) {
                                 const int c = g4 + cc;
-                                const int k = kb + __shfl_sync(0xffffffffu, ecl, c);
+                                const int ec = __shfl_sync(0xffffffffu, e0, c);
                                 double re, im;
                                 if (fast) {
-                                    const uint32_t eb = pow2_ebias(k);
+                                    const uint32_t eb = rbias + ((uint32_t)ec << 20);
                                     re = f32_pow2_to_f64_fast(vre[c], eb);
                                     im = f32_pow2_to_f64_fast(vim[c], eb);
                                 } else {
-                                    re = f32_pow2_to_f64_slow(vre[c], k);
-                                    im = f32_pow2_to_f64_slow(vim[c], k);
+                                    re = f32_pow2_to_f64_slow(vre[c], kb + ec);
+                                    im = f32_pow2_to_f64_slow(vim[c], kb + ec);
                                 }
                                 *reinterpret_cast<double2 *>(stg + buf + cc * 512 + lane * 16) = make_double2(re, im);
                             }
                             fence_async_smem();
                             __syncwarp();
+                            // lane cc issues the copy of the group's column cc (32 rows) and commits it
                             if (lane < kStageCols) {
                                 const int64_t col = colb + g4 + lane;
                                 const int64_t lo = lower ? max(r0, col) : r0, hi = min(r0 + 32, m);
                                 if (col < n && lo < hi) {
                                     const uint32_t src = stg_s + buf + lane * 512 + (uint32_t)(lo - r0) * 16;
                                     double2 *dst = out + lo + ldo * col;
-                                    if (first) bulk_store_g(dst, src, (uint32_t)(hi - lo) * 16);
-                                    else bulk_add_g(dst, src, (uint32_t)(hi - lo) * 16);
+                                    if (first) bulk_store_g(dst, src, (uint32_t)(hi - lo) * 16, pol);
+                                    else bulk_add_g(dst, src, (uint32_t)(hi - lo) * 16, pol);
                                 }
                                 bulk_commit();
                             }
                         }
+                        // next chunk's exponents and range into e0 / lo0 / hi0 (a cyclic rotation:
+                        // after the unit's four chunks the registers are back in order)
+                        const int xe = e0, xl = lo0, xh = hi0;
+                        e0 = e1; e1 = e2; e2 = e3; e3 = xe;
+                        lo0 = lo1; lo1 = lo2; lo2 = lo3; lo3 = xl;
+                        hi0 = hi1; hi1 = hi2; hi2 = hi3; hi3 = xh;
                     }
                     ++unit;
                 }
@@ -1463,6 +1508,7 @@ struct OzGroup {
     int *d_err = nullptr;
     bool pair = false;          // S/H on CTA-pair tiles
     bool sf = false;            // structure-factor form
+    int tbatch = 1;             // its types per combine batch
     SfTab sft{};                // its combine table (outputs patched per run)
     const double2 *sf_tab = nullptr;
 };
@@ -1636,6 +1682,7 @@ static int group_prepare_sf(OzakiPlan &oz, const OzGroupDesc &d, const std::vect
     g->kb = kb;
     g->d_err = oz.d_error;
     g->sf_tab = d.sf_tab;
+    g->tbatch = std::max(1, d.tbatch);
     std::vector<int64_t> G;
     for (auto &k : kb) G.push_back(k.G);
     g->rows = group_rows(G);
@@ -1729,7 +1776,7 @@ static int group_prepare_sf(OzakiPlan &oz, const OzGroupDesc &d, const std::vect
                 j.lk0 = t * g->bpad; j.rk0 = t * g->bpad;
                 j.nkb = tkb;
                 j.m = kb[k].G; j.n = kb[k].G;
-                j.out = which == 0 ? kb[k].PS : kb[k].PH;
+                j.out = (which == 0 ? kb[k].PS : kb[k].PH) + (t % g->tbatch) * kb[k].pstride;
                 j.ldo = kb[k].G;
                 j.el = g->dM.expo + g->row0[k];
                 j.er = (which == 0 ? g->dW.expo : g->dX.expo) + g->row0[k];
@@ -1997,11 +2044,15 @@ int ozaki_group_run(OzGroup *g, const DevSystem &sys, const KTable &ktab, cudaSt
                             : launch_prepared(g->maps_sh, g->s, g->d_err, jobs, g->n_jobs_sh, g->tiles_sh,
                                               g->d_list_sh, g->d_progress, st);
             if (e == cudaSuccess && nev >= 2 * g->nt) e = record(ev[2 * t + 1], st);
-            if (e == cudaSuccess) {
-                g->sft.type = t;
-                e = launch_sf_combine(g->sft, g->sf_tab, t == 0, st);
+            nl += 1;
+            // the batch's last type: its products into S and H
+            if (e == cudaSuccess && ((t + 1) % g->tbatch == 0 || t + 1 == g->nt)) {
+                const int t0 = t / g->tbatch * g->tbatch;
+                g->sft.type = t0;
+                g->sft.ntypes = t + 1 - t0;
+                e = launch_sf_combine(g->sft, g->sf_tab, t0 == 0, st);
+                nl += 1;
             }
-            nl += 2;
         }
         if (launches) *launches = nl;
         if (e != cudaSuccess) { g_oz_err = cudaGetErrorString(e); return HSDLA_ERR_CUDA; }

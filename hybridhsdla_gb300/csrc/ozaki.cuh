@@ -43,8 +43,9 @@ struct OzKBufs {
     double2 *M = nullptr;    // per-type rows M (2L nt x G), hoisted T application only
     double2 *Z = nullptr;    // per-type products Z (2L nt x G), hoisted T application only
     int64_t G = 0;
-    double2 *PS = nullptr;   // structure-factor form: per-type products (G x G, ld G)
-    double2 *PH = nullptr;
+    double2 *PS = nullptr;   // structure-factor form: per-type products (G x G, ld G), type
+    double2 *PH = nullptr;   // slot b of a combine batch at + b pstride
+    int64_t pstride = 0;
 };
 struct OzGroupDesc {
     int64_t twoL = 0, na = 0, nt = 0;
@@ -56,6 +57,7 @@ struct OzGroupDesc {
     bool sf = false;                       // structure-factor form (requires hoist)
     const double *wt = nullptr;            // its per-type S weights [nt][2L]
     const double2 *sf_tab = nullptr;       // its structure factors
+    int tbatch = 1;                        // its types per combine batch (product slots)
 };
 struct OzGroup;
 // scratch: rewritten by every run (may be shared by the groups of a plan); persist: owned by

@@ -44,8 +44,9 @@ __global__ void sf_table_kernel(const double2 *__restrict__ ex, const double2 *_
 
 constexpr int kSfTile = 32, kSfRows = 8;
 
-// out (+)= SF_t(g_col - g_row) * P over the lower triangle of every entry (S and H together),
-// one CTA per 32 x 32 tile; consecutive threads take consecutive rows of a column.
+// out (+)= sum over the batch's types t of SF_t(g_col - g_row) * P_t over the lower triangle of
+// every entry (S and H together), one CTA per 32 x 32 tile; consecutive threads take consecutive
+// rows of a column.  A batch of several types reads and writes S and H once.
 __global__ void __launch_bounds__(kSfTile * kSfRows) sf_combine_kernel(const __grid_constant__ SfTab tab,
                                                                        const double2 *__restrict__ sf, int first) {
     const int64_t tile = blockIdx.x;
@@ -69,10 +70,17 @@ __global__ void __launch_bounds__(kSfTile * kSfRows) sf_combine_kernel(const __g
         const int32_t *gc = E.g + 3 * col;
         const int64_t idx = ((int64_t)(gc[0] - gr0 + tab.dx) * tab.ny + (gc[1] - gr1 + tab.dy)) * tab.nz +
                             (gc[2] - gr2 + tab.dz);
-        const double2 f = sft[idx];
-        const double2 ps = E.PS[row + E.ldp * col], ph = E.PH[row + E.ldp * col];
+        const int64_t off = row + E.ldp * col;
+        double2 vs = make_double2(0.0, 0.0), vh = make_double2(0.0, 0.0);
+        for (int b = 0; b < tab.ntypes; ++b) {
+            const double2 f = sft[idx + b * tab.box];
+            const double2 ps = E.PS[off + b * E.pstride], ph = E.PH[off + b * E.pstride];
+            vs.x = fma(f.x, ps.x, fma(-f.y, ps.y, vs.x));
+            vs.y = fma(f.x, ps.y, fma(f.y, ps.x, vs.y));
+            vh.x = fma(f.x, ph.x, fma(-f.y, ph.y, vh.x));
+            vh.y = fma(f.x, ph.y, fma(f.y, ph.x, vh.y));
+        }
         double2 *so = E.S + row + E.ldo * col, *ho = E.H + row + E.ldo * col;
-        double2 vs = cmul_d(f, ps), vh = cmul_d(f, ph);
         if (!first) {
             const double2 s0 = *so, h0 = *ho;
             vs.x += s0.x; vs.y += s0.y;

@@ -44,6 +44,8 @@ def _check(res, sys_, kps):
 def test_groups_of_one_kpoint_match_one_group(ctx, prec, monkeypatch):
     import torch
     s = synth.make_system("t1")                     # three k-points (one at Gamma)
+    # the same type batches in both plans (a budget-chosen batch would differ): types {0, 1}, {2}
+    monkeypatch.setenv("HSDLA_TYPE_BATCH", "2")
     one = ctx.plan(s, precision=prec, num_slices=11 if prec == "ozaki" else 0)
     o1 = one.alloc_outputs()
     one.execute(o1)

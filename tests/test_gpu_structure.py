@@ -59,3 +59,18 @@ def test_structure_factor_form_is_used(ctx):
     _, r_pa = _run(ctx, s, "fp64", False)
     ratio = r_pa["dominant_flop"] / r_sf["dominant_flop"]
     assert abs(ratio - s.num_atoms / s.num_types) < 1e-9, ratio
+
+
+@pytest.mark.parametrize("precision", ["fp64", "ozaki"])
+@pytest.mark.parametrize("batch", ["1", "2", "3"])
+def test_type_batches_of_the_combine(ctx, precision, batch, monkeypatch):
+    """The combine of one type at a time, of two (a full batch and a partial one over c1's four
+    types) and of three: every split agrees with the oracle."""
+    monkeypatch.setenv("HSDLA_TYPE_BATCH", batch)
+    s = synth.make_system("c1")
+    res, _ = _run(ctx, s, precision, True)
+    for (H, S), kp in zip(res, s.kpoints):
+        Hr, Sr = oracle.reference_hs(s, kp)
+        for X, R in ((H, Hr), (S, Sr)):
+            fro, mx = oracle.lower_errors(X, R)
+            assert fro < TOL and mx < TOL, (batch, precision, fro, mx)
