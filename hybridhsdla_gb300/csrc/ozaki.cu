@@ -245,13 +245,13 @@ __device__ bool grid_lockstep(int *progress, int n, int epoch, volatile int *abo
     }
 }
 
-// x * 2^k as a double for an FP32 accumulator x (an exact integer, |x| <= 2^24), built with
+// x * 2^k as a double for an FP32 accumulator x (a multiple of 2^-5 below 2^25), built with
 // integer operations: GB300's FP64 pipe is a small fraction of its integer pipes, and a drain
 // converts 2^16 values per CTA.  (f & 0x7fffffff) >> 3 puts the FP32 exponent and the top 20
 // mantissa bits exactly where the FP64 high word keeps them, so rebasing the exponent is one
 // add of (1023 - 127 + k) << 20; the low word takes the last 3 mantissa bits.  Valid for
 // k in [kPow2Lo, kPow2Hi] (the result stays normal); pow2_ok() checks that once per column.
-constexpr int kPow2Lo = -1022, kPow2Hi = 999;
+constexpr int kPow2Lo = -1017, kPow2Hi = 997;
 __device__ __forceinline__ bool pow2_ok(int k) { return k >= kPow2Lo && k <= kPow2Hi; }
 __device__ __forceinline__ double f32_pow2_to_f64_fast(uint32_t f, uint32_t ebias) {
     const uint32_t a = f & 0x7fffffffu;
@@ -613,11 +613,24 @@ struct __align__(8) PairBarriers {
     uint64_t tempty;             // leader: 16 epilogue warps (both CTAs) drained the accumulator
 };
 
+// Accumulation units of a pair launch, in drain order.  Unit u sums, per K-chunk, the digit pairs
+// (i, t - i) of diagonal t = t[u] into the FP32 accumulator and drains it with weight 2^(2-5t).
+// A merged unit also sums the pairs (i, t + 1 - i) of the next diagonal, with the left digits
+// scaled by 2^-5 (planes 2s .. 4s-1 of the left operand): the two diagonals share one drain.
+constexpr int kMaxUnits = kOzMaxSlices + 1;
+constexpr uint8_t kUnitMerged = 1;
+struct PairUnits {
+    int32_t n;
+    int8_t t[kMaxUnits];
+    uint8_t flags[kMaxUnits];
+};
+
 __global__ void __launch_bounds__(kThreads, 1)
     oz_pair_kernel(const __grid_constant__ CUtensorMap map0, const __grid_constant__ CUtensorMap map1,
                    const __grid_constant__ CUtensorMap map2, const __grid_constant__ CUtensorMap map3,
                    const OzJob *__restrict__ jobs, int num_jobs, int64_t total_tiles, int s, int *err,
-                   const int4 *__restrict__ tile_list, int *progress, int sync_every, int slack) {
+                   const int4 *__restrict__ tile_list, int *progress, int sync_every, int slack,
+                   const __grid_constant__ PairUnits units) {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     unsigned char *smem = reinterpret_cast<unsigned char *>(
         (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
@@ -681,29 +694,33 @@ __global__ void __launch_bounds__(kThreads, 1)
                 int64_t tm, tn;
                 const OzJob &j = resolve_tile(jobs, num_jobs, tile_list, tile, tm, tn);
                 const CUtensorMap *lm = map_of(j.lmap), *rm = map_of(j.rmap);
-                for (int t = 2; ok && t <= s + 1; ++t) {
-                    const int ilo = max(1, t - s), ihi = min(s, t - 1);
-                    const int64_t ck = chunk_kblocks(ihi - ilo + 1);
+                for (int u = 0; ok && u < units.n; ++u) {
+                    const int t = units.t[u], merged = (units.flags[u] & kUnitMerged) ? 1 : 0;
+                    const int64_t ck = merged ? j.nkb : chunk_kblocks(min(s, t - 1) - max(1, t - s) + 1);
                     for (int64_t cb = 0; ok && cb < j.nkb; cb += ck) {
                         const int64_t ce = min(j.nkb, cb + ck);
                         for (int64_t kb = cb; ok && kb < ce; ++kb) {
-                            for (int i = ilo; i <= ihi; ++i) {
-                                const int jj = t - i;
-                                if (leader && progress && issued > 0 && issued % sync_every == 0 &&
-                                    !grid_lockstep(progress, (int)npairs, (int)(issued / sync_every), &abort_flag,
-                                                   err, (int)pair, slack)) { ok = false; break; }
-                                if (!pwait(&bars.empty[stage], phase ^ 1, 1, stage, (int)issued)) { ok = false; break; }
-                                unsigned char *st = smem + stage * kStageBytes;
-                                if (leader) mbar_expect_tx(&bars.full[stage], 2 * kStageBytes);
-                                const uint32_t fb = full0_leader + stage * 8;
-                                const int xl = (int)(j.lk0 + kb * kKBlock), xr = (int)(j.rk0 + kb * kKBlock);
-                                const int64_t yl = j.lrow0 + tm * kPairTile + half, yr = j.rrow0 + tn * kPairTile + half;
-                                tma_load_2d_pair(st, lm, fb, xl, (int)((2 * (i - 1)) * j.lplane + yl));
-                                tma_load_2d_pair(st + 16384, lm, fb, xl, (int)((2 * (i - 1) + 1) * j.lplane + yl));
-                                tma_load_2d_pair(st + 32768, rm, fb, xr, (int)((2 * (jj - 1)) * j.rplane + yr));
-                                tma_load_2d_pair(st + 49152, rm, fb, xr, (int)((2 * (jj - 1) + 1) * j.rplane + yr));
-                                ++issued;
-                                if (++stage == kStages) { stage = 0; phase ^= 1; }
+                            for (int part = 0; ok && part <= merged; ++part) {
+                                const int tt = t + part, ilo = max(1, tt - s), ihi = min(s, tt - 1);
+                                for (int i = ilo; i <= ihi; ++i) {
+                                    const int jj = tt - i;
+                                    const int lp = (part ? 2 * s : 0) + 2 * (i - 1);   // scaled planes of a merged part
+                                    if (leader && progress && issued > 0 && issued % sync_every == 0 &&
+                                        !grid_lockstep(progress, (int)npairs, (int)(issued / sync_every), &abort_flag,
+                                                       err, (int)pair, slack)) { ok = false; break; }
+                                    if (!pwait(&bars.empty[stage], phase ^ 1, 1, stage, (int)issued)) { ok = false; break; }
+                                    unsigned char *st = smem + stage * kStageBytes;
+                                    if (leader) mbar_expect_tx(&bars.full[stage], 2 * kStageBytes);
+                                    const uint32_t fb = full0_leader + stage * 8;
+                                    const int xl = (int)(j.lk0 + kb * kKBlock), xr = (int)(j.rk0 + kb * kKBlock);
+                                    const int64_t yl = j.lrow0 + tm * kPairTile + half, yr = j.rrow0 + tn * kPairTile + half;
+                                    tma_load_2d_pair(st, lm, fb, xl, (int)(lp * j.lplane + yl));
+                                    tma_load_2d_pair(st + 16384, lm, fb, xl, (int)((lp + 1) * j.lplane + yl));
+                                    tma_load_2d_pair(st + 32768, rm, fb, xr, (int)((2 * (jj - 1)) * j.rplane + yr));
+                                    tma_load_2d_pair(st + 49152, rm, fb, xr, (int)((2 * (jj - 1) + 1) * j.rplane + yr));
+                                    ++issued;
+                                    if (++stage == kStages) { stage = 0; phase ^= 1; }
+                                }
                             }
                         }
                     }
@@ -732,32 +749,35 @@ __global__ void __launch_bounds__(kThreads, 1)
             for (int64_t tile = pair; ok && tile < total_tiles; tile += npairs) {
                 int64_t tm_, tn_;
                 const OzJob &j = resolve_tile(jobs, num_jobs, tile_list, tile, tm_, tn_);
-                for (int t = 2; ok && t <= s + 1; ++t) {
-                    const int ilo = max(1, t - s), ihi = min(s, t - 1);
-                    const int64_t ck = chunk_kblocks(ihi - ilo + 1);
+                for (int u = 0; ok && u < units.n; ++u) {
+                    const int t = units.t[u], merged = (units.flags[u] & kUnitMerged) ? 1 : 0;
+                    const int64_t ck = merged ? j.nkb : chunk_kblocks(min(s, t - 1) - max(1, t - s) + 1);
                     for (int64_t cb = 0; ok && cb < j.nkb; cb += ck) {
                         const int64_t ce = min(j.nkb, cb + ck);
                         if (!pwait(&bars.tempty, (uint32_t)((unit & 1) ^ 1), 2, stage, (int)unit)) { ok = false; break; }
                         tc_fence_after();
                         bool first = true;
                         for (int64_t kb = cb; ok && kb < ce; ++kb) {
-                            for (int i = ilo; i <= ihi; ++i) {
-                                if (!pwait(&bars.full[stage], phase, 3, stage, (int)unit)) { ok = false; break; }
-                                tc_fence_after();
-                                const uint32_t a_re = sbase + stage * kStageBytes, a_im = a_re + 16384;
-                                const uint32_t b_re = a_re + 32768, b_im = a_re + 49152;
+                            for (int part = 0; ok && part <= merged; ++part) {
+                                const int tt = t + part, ilo = max(1, tt - s), ihi = min(s, tt - 1);
+                                for (int i = ilo; i <= ihi; ++i) {
+                                    if (!pwait(&bars.full[stage], phase, 3, stage, (int)unit)) { ok = false; break; }
+                                    tc_fence_after();
+                                    const uint32_t a_re = sbase + stage * kStageBytes, a_im = a_re + 16384;
+                                    const uint32_t b_re = a_re + 32768, b_im = a_re + 49152;
 #pragma unroll
-                                for (int kk = 0; kk < kKBlock / 32; ++kk) {
-                                    const uint32_t off = kk * 32;
-                                    const uint32_t acc = first ? 0u : 1u;
-                                    mma_f8_pair(d_re, sw128_desc(a_re + off), sw128_desc(b_re + off), id_pos, acc);
-                                    mma_f8_pair(d_re, sw128_desc(a_im + off), sw128_desc(b_im + off), id_pos, 1u);
-                                    mma_f8_pair(d_im, sw128_desc(a_re + off), sw128_desc(b_im + off), id_pos, acc);
-                                    mma_f8_pair(d_im, sw128_desc(a_im + off), sw128_desc(b_re + off), id_neg, 1u);
-                                    first = false;
+                                    for (int kk = 0; kk < kKBlock / 32; ++kk) {
+                                        const uint32_t off = kk * 32;
+                                        const uint32_t acc = first ? 0u : 1u;
+                                        mma_f8_pair(d_re, sw128_desc(a_re + off), sw128_desc(b_re + off), id_pos, acc);
+                                        mma_f8_pair(d_re, sw128_desc(a_im + off), sw128_desc(b_im + off), id_pos, 1u);
+                                        mma_f8_pair(d_im, sw128_desc(a_re + off), sw128_desc(b_im + off), id_pos, acc);
+                                        mma_f8_pair(d_im, sw128_desc(a_im + off), sw128_desc(b_re + off), id_neg, 1u);
+                                        first = false;
+                                    }
+                                    mma_commit_pair(&bars.empty[stage]);
+                                    if (++stage == kStages) { stage = 0; phase ^= 1; }
                                 }
-                                mma_commit_pair(&bars.empty[stage]);
-                                if (++stage == kStages) { stage = 0; phase ^= 1; }
                             }
                         }
                         if (!ok) break;
@@ -812,13 +832,15 @@ __global__ void __launch_bounds__(kThreads, 1)
             int lo1 = __reduce_min_sync(0xffffffffu, e1), hi1 = __reduce_max_sync(0xffffffffu, e1);
             int lo2 = __reduce_min_sync(0xffffffffu, e2), hi2 = __reduce_max_sync(0xffffffffu, e2);
             int lo3 = __reduce_min_sync(0xffffffffu, e3), hi3 = __reduce_max_sync(0xffffffffu, e3);
-            for (int t = 2; ok && t <= s + 1; ++t) {
-                const int ilo = max(1, t - s), ihi = min(s, t - 1);
-                const int64_t ck = chunk_kblocks(ihi - ilo + 1);
+            for (int u = 0; ok && u < units.n; ++u) {
+                const int t = units.t[u];
+                const uint8_t fl = units.flags[u];
+                const int64_t ck =
+                    (fl & kUnitMerged) ? nkb : chunk_kblocks(min(s, t - 1) - max(1, t - s) + 1);
                 const int kb = 2 - 5 * t + erow;
                 for (int64_t cb = 0; ok && cb < nkb; cb += ck) {
-                    const bool first = (t == 2 && cb == 0) && !accum;
-                    const uint64_t pol = (t == s + 1 && cb + ck >= nkb) ? pol_first : pol_last;
+                    const bool first = (u == 0 && cb == 0) && !accum;
+                    const uint64_t pol = (u == units.n - 1 && cb + ck >= nkb) ? pol_first : pol_last;
                     if (!pwait(&bars.tfull, (uint32_t)(unit & 1), 4, warp, (int)unit)) { ok = false; break; }
                     tc_fence_after();
                     // the previous unit's copies are complete: successive updates stay in order
@@ -933,6 +955,9 @@ struct SliceTab {
     const double *v2 = nullptr;
     uint8_t *digits2 = nullptr;
     int32_t *expo2 = nullptr;
+    // 1: the (first) operand's digits also go, scaled by 2^-5, to planes 2s .. 4s-1 (the left
+    // operand of merged accumulation units)
+    int scaled = 0;
     SliceEntry e[kMaxGroup];
 };
 
@@ -941,19 +966,26 @@ __device__ __forceinline__ uint32_t pack4_e4m3(int d0, int d1, int d2, int d3) {
     const uint32_t hi = __nv_cvt_float2_to_fp8x2(make_float2((float)d2, (float)d3), __NV_SATFINITE, __NV_E4M3);
     return lo | (hi << 16);
 }
+// Four e4m3 digits (|d| <= 16) times 2^-5: every nonzero digit is normal with exponent field >= 7
+// (|d| >= 1), so subtracting 5 from the field (0x28 from the byte, no borrow) scales it exactly
+// (d / 32 >= 2^-5 stays normal); zeros keep their bytes.
+__device__ __forceinline__ uint32_t scale4_e4m3_2m5(uint32_t w) {
+    return w - (0x28282828u & __vcmpne4(w & 0x7f7f7f7fu, 0u));
+}
 
 // The planes of U = X + B from the least significant: plane i (0 = most significant) holds
 // ((U >> 5 (s-1-i)) & 31) - 16 for i >= 1, and the top plane the rest, U >> 5 (s-1) in
 // [-16, 16].  A running arithmetic shift by 5 leaves each field in the low bits in turn (the low
 // bits are the same for arithmetic and logical shifts).
-template <int kVec>
+// kScaled: each digit also goes, times 2^-5 (exact in e4m3 for |d| <= 16: d / 32 >= 2^-5 is
+// normal), to plane 2s + 2i + part.
+template <int kVec, bool kScaled>
 __device__ __forceinline__ void write_part(const long long (&x)[kVec], int part, int s, uint8_t *row, int64_t plane) {
     long long u[kVec];
 #pragma unroll
     for (int v = 0; v < kVec; ++v) u[v] = x[v];
-#pragma unroll
-    for (int step = 0; step < kOzMaxSlices; ++step) {
-        if (step >= s) break;
+#pragma unroll 1
+    for (int step = 0; step < s; ++step) {
         const int i = s - 1 - step;
         int d[kVec];
 #pragma unroll
@@ -962,19 +994,23 @@ __device__ __forceinline__ void write_part(const long long (&x)[kVec], int part,
             u[v] >>= 5;
         }
         uint8_t *dst = row + (int64_t)(2 * i + part) * plane;
-        if (kVec == 8)
-            *reinterpret_cast<uint2 *>(dst) =
-                make_uint2(pack4_e4m3(d[0], d[1], d[2], d[3]), pack4_e4m3(d[4 % kVec], d[5 % kVec], d[6 % kVec], d[7 % kVec]));
-        else
-            *reinterpret_cast<uint32_t *>(dst) = pack4_e4m3(d[0], d[1], d[2], d[3]);
+        const uint32_t w0 = pack4_e4m3(d[0], d[1], d[2], d[3]);
+        const uint32_t w1 = kVec == 8 ? pack4_e4m3(d[4 % kVec], d[5 % kVec], d[6 % kVec], d[7 % kVec]) : 0u;
+        if (kVec == 8) *reinterpret_cast<uint2 *>(dst) = make_uint2(w0, w1);
+        else *reinterpret_cast<uint32_t *>(dst) = w0;
+        if (kScaled) {
+            uint8_t *dsc = row + (int64_t)(2 * s + 2 * i + part) * plane;
+            if (kVec == 8) *reinterpret_cast<uint2 *>(dsc) = make_uint2(scale4_e4m3_2m5(w0), scale4_e4m3_2m5(w1));
+            else *reinterpret_cast<uint32_t *>(dsc) = scale4_e4m3_2m5(w0);
+        }
     }
 }
 
-template <int kVec>
+template <int kVec, bool kScaled = false>
 __device__ __forceinline__ void write_planes(const long long (&ur)[kVec], const long long (&ui)[kVec], int s,
                                              uint8_t *row, int64_t plane) {
-    write_part<kVec>(ur, 0, s, row, plane);
-    write_part<kVec>(ui, 1, s, row, plane);
+    write_part<kVec, kScaled>(ur, 0, s, row, plane);
+    write_part<kVec, kScaled>(ui, 1, s, row, plane);
 }
 
 __device__ __forceinline__ double block_max(double m, double *red) {
@@ -1035,7 +1071,7 @@ __device__ __noinline__ void weighted_chunk(const double2 *zc, const double *vv,
     write_planes<kV>(xr, xi, s, row, plane);
 }
 
-template <bool kDual>
+template <bool kDual, bool kScaled>
 __global__ void __launch_bounds__(kSliceThreads, 1) oz_slice_kernel(const __grid_constant__ SliceTab tab) {
     // values per thread and step of the digit pass (the dual pass keeps two operands' state)
     constexpr int kV = kDual ? 4 : kSliceVec;
@@ -1105,7 +1141,7 @@ __global__ void __launch_bounds__(kSliceThreads, 1) oz_slice_kernel(const __grid
                 xi[u] = B + rint_pow2(z.y, kx);
             }
         }
-        write_planes<kV>(xr, xi, s, tab.digits + r * pitch + kp0, plane);
+        write_planes<kV, kScaled>(xr, xi, s, tab.digits + r * pitch + kp0, plane);
         if (kDual)      // the chunk again (an L1 hit) for the weighted operand
             weighted_chunk<kV>(zc, v2 + b * rpb + rr0, nv, kw, B, s, tab.digits2 + r * pitch + kp0, plane);
     }
@@ -1215,8 +1251,10 @@ SliceTab slice_table(const double2 *Z, int64_t ldz, const double *v, int64_t Kin
 }
 
 cudaError_t slice_launch(const SliceTab &t, cudaStream_t st) {
-    if (t.digits2) oz_slice_kernel<true><<<(unsigned)t.plane_rows, kSliceThreads, 0, st>>>(t);
-    else oz_slice_kernel<false><<<(unsigned)t.plane_rows, kSliceThreads, 0, st>>>(t);
+    if (t.digits2 && t.scaled) oz_slice_kernel<true, true><<<(unsigned)t.plane_rows, kSliceThreads, 0, st>>>(t);
+    else if (t.digits2) oz_slice_kernel<true, false><<<(unsigned)t.plane_rows, kSliceThreads, 0, st>>>(t);
+    else if (t.scaled) oz_slice_kernel<false, true><<<(unsigned)t.plane_rows, kSliceThreads, 0, st>>>(t);
+    else oz_slice_kernel<false, false><<<(unsigned)t.plane_rows, kSliceThreads, 0, st>>>(t);
     return cudaGetLastError();
 }
 
@@ -1235,6 +1273,34 @@ bool use_pair() {
     static const bool b = env_int("HSDLA_PAIR", 1) != 0;
     return b;
 }
+
+// Accumulation units of a pair launch (see PairUnits).  Diagonals t and t + 1 share a unit when
+// the left operand carries the 2^-5-scaled planes, each fits one K-chunk, and either the sum
+// stays exact -- every partial sum a multiple of 2^-5 below 2^19, with |sum| <= nkb 128 x 2
+// (re/im) x 256 (|product|) x (n_t + n_{t+1} / 32) -- or t >= kLooseT, where even an FP32
+// rounding (2^-24 of the sum) stays far below the result's FP64 precision.  The low-order
+// diagonals are not small everywhere: in a Gram element (S_gg) the products d_p(M_k) d_p(W_k) of
+// rows with w_k = 1 add up with one sign, so diagonal 2p carries ~K 2^8 2^(2-10p) whatever the
+// size of S_gg -- from t = 9 on below 2^-26 of S_gg, and exact here anyway (|sum| ~ 2^14).
+constexpr int kLooseT = 9;
+PairUnits pair_units(int s, int64_t nkb, bool merge) {
+    PairUnits p;
+    memset(&p, 0, sizeof(p));
+    auto pairs = [&](int t) { return std::min(s, t - 1) - std::max(1, t - s) + 1; };
+    for (int t = 2; t <= s + 1;) {
+        bool m = false;
+        if (merge && t + 1 <= s + 1 && chunk_kblocks(pairs(t)) >= nkb && chunk_kblocks(pairs(t + 1)) >= nkb) {
+            const int64_t bound = nkb * kKBlock * 2 * 256;
+            m = t >= kLooseT || bound * (32 * pairs(t) + pairs(t + 1)) <= ((int64_t)1 << 24);
+        }
+        p.t[p.n] = (int8_t)t;
+        p.flags[p.n] = m ? kUnitMerged : 0;
+        ++p.n;
+        t += m ? 2 : 1;
+    }
+    return p;
+}
+PairUnits pair_units_plain(int s) { return pair_units(s, 0, false); }
 
 // Host-built tile schedule.  Persistent CTAs take tiles g, g + grid, ... so tiles that are
 // close in the list run at the same time and share their operand panels in L2.  Lower-
@@ -1507,6 +1573,7 @@ struct OzGroup {
     int *d_progress = nullptr;
     int *d_err = nullptr;
     bool pair = false;          // S/H on CTA-pair tiles
+    PairUnits units{};          // their accumulation units
     bool sf = false;            // structure-factor form
     int tbatch = 1;             // its types per combine batch
     SfTab sft{};                // its combine table (outputs patched per run)
@@ -1542,7 +1609,7 @@ int upload_schedule(std::vector<OzJob> &jobs, OzJob *d_jobs, int4 *d_list, int64
 // Launch of a prepared pair-tile job table: clusters of two CTAs, one per SM, as many pairs as
 // can be resident (at most one per tile); cooperative when the lockstep slots are given.
 cudaError_t launch_pair(const CUtensorMap *maps, int s, int *d_err, const OzJob *d_jobs, int n_jobs, int64_t total,
-                        const int4 *d_list, int *d_progress, cudaStream_t st) {
+                        const int4 *d_list, int *d_progress, cudaStream_t st, const PairUnits &units) {
     if (total <= 0) return cudaSuccess;
     const size_t smem = (size_t)kStages * kStageBytes + kPairStageBytes + 1024;
     cudaError_t e = cudaFuncSetAttribute(oz_pair_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -1589,7 +1656,7 @@ cudaError_t launch_pair(const CUtensorMap *maps, int s, int *d_err, const OzJob 
     static const int sync_every = (int)std::max<int64_t>(8, env_int("HSDLA_SYNC_EVERY", kSyncEvery));
     static const int slack = (int)std::max<int64_t>(1, env_int("HSDLA_SYNC_SLACK", 1));
     return cudaLaunchKernelEx(&cfg, oz_pair_kernel, maps[0], maps[1], maps[2], maps[3], d_jobs, n_jobs, total, s,
-                              d_err, d_list, lockstep ? d_progress : (int *)nullptr, sync_every, slack);
+                              d_err, d_list, lockstep ? d_progress : (int *)nullptr, sync_every, slack, units);
 }
 
 // Launch of a prepared job table (no host synchronisation; capturable).
@@ -1640,9 +1707,13 @@ static int64_t atom_stride(int64_t twoL) { return round_up(twoL, 16); }
 int64_t ozaki_group_bytes(int s, int64_t twoL, int64_t na, int64_t nt, const std::vector<int64_t> &G, int panels,
                           bool hoist, bool sf) {
     const int64_t bpad = atom_stride(twoL), rows = group_rows(G);
-    if (sf) {      // M, M diag(w_t) and Z digits: each type's rows on whole k-blocks
+    if (sf) {      // M (with its scaled copy on pair tiles), M diag(w_t) and Z digits: each
+                   // type's rows on whole k-blocks
         const int64_t KT = round_up(twoL, kKBlock) * nt;
-        return 3 * (round_up(2 * s * rows * (KT + pitch_pad()), 1024) + round_up(4 * rows, 1024)) + 4096;
+        auto dig = [&](int64_t planes) {
+            return round_up(planes * rows * (KT + pitch_pad()), 1024) + round_up(4 * rows, 1024);
+        };
+        return dig((use_pair() ? 4 : 2) * s) + 2 * dig(2 * s) + 4096;
     }
     const int64_t Kp = round_up(bpad * panel_atoms(na, panels), kKBlock);
     const int64_t Kx = hoist ? std::max(Kp, round_up(bpad * nt, kKBlock)) : Kp;
@@ -1691,16 +1762,19 @@ static int group_prepare_sf(OzakiPlan &oz, const OzGroupDesc &d, const std::vect
     const int s = g->s;
     Arena ar{reinterpret_cast<char *>(ws)};
     Arena keep{reinterpret_cast<char *>(persist)};
-    auto carve_rows = [&](DigitOperand &o) {
+    auto carve_rows = [&](DigitOperand &o, int planes) {
         o.plane_rows = g->rows;
         o.Kpad = KT;
         o.pitch = KT + pitch_pad();
-        o.digits = ar.take<uint8_t>(2 * s * o.plane_rows * o.pitch);
+        o.digits = ar.take<uint8_t>(planes * o.plane_rows * o.pitch);
         o.expo = ar.take<int32_t>(o.plane_rows);
     };
-    carve_rows(g->dM);        // M
-    carve_rows(g->dW);        // M diag(w_t)
-    carve_rows(g->dX);        // Z
+    // M: the S/H products' left operand; on pair tiles with its digits scaled by 2^-5 as well
+    // (planes 2s .. 4s-1), the merged accumulation units' left digits
+    g->pair = use_pair();
+    carve_rows(g->dM, g->pair ? 4 * s : 2 * s);
+    carve_rows(g->dW, 2 * s);    // M diag(w_t)
+    carve_rows(g->dX, 2 * s);    // Z
     carve_operand(keep, g->dT, s, d.nt * d.twoL, tkb * kKBlock);
     const int64_t nk = g->nk;
     int64_t tiles_t = 0, tiles_sh = 0;
@@ -1723,6 +1797,7 @@ static int group_prepare_sf(OzakiPlan &oz, const OzGroupDesc &d, const std::vect
         return t;
     };
     g->tM = table(g->dM, 0);              // dual: M and M diag(w_t)
+    g->tM.scaled = g->pair ? 1 : 0;
     g->tM.v2 = d.wt;
     g->tM.digits2 = g->dW.digits;
     g->tM.expo2 = g->dW.expo;
@@ -1734,7 +1809,7 @@ static int group_prepare_sf(OzakiPlan &oz, const OzGroupDesc &d, const std::vect
     cudaError_t e = slice(d.Tfull, d.twoL, nullptr, d.twoL, d.nt * d.twoL, d.twoL, g->bpad, s, g->dT, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) { g_oz_err = cudaGetErrorString(e); return fail(HSDLA_ERR_CUDA); }
-    int rc = make_map(g->dM, s);
+    int rc = make_map(g->dM, g->pair ? 2 * s : s);
     if (!rc) rc = make_map(g->dW, s);
     if (!rc) rc = make_map(g->dX, s);
     if (!rc) rc = make_map(g->dT, s);
@@ -1759,8 +1834,9 @@ static int group_prepare_sf(OzakiPlan &oz, const OzGroupDesc &d, const std::vect
     rc = upload_schedule(jt, g->d_jobs_t, g->d_list_t, g->tiles_t);
     if (rc) return fail(rc);
     g->maps_t[0] = g->dM.map; g->maps_t[1] = g->dM.map; g->maps_t[2] = g->dM.map; g->maps_t[3] = g->dT.map;
-    // per type: S_t = M_t^H diag(w_t) M_t and H_t = M_t^H Z_t into the products
-    g->pair = use_pair();
+    // per type: S_t = M_t^H diag(w_t) M_t and H_t = M_t^H Z_t into the products; on pair tiles
+    // with merged accumulation units (HSDLA_MERGE=0: one per diagonal)
+    g->units = g->pair ? pair_units(s, tkb, env_int("HSDLA_MERGE", 1) != 0) : pair_units_plain(s);
     const int64_t tile = g->pair ? kPairTile : kTileN;
     g->n_jobs_sh = 2 * g->nk;
     std::vector<OzJob> all;
@@ -1958,6 +2034,7 @@ int ozaki_group_prepare(OzakiPlan &oz, const OzGroupDesc &d, const std::vector<O
     g->maps_t[1] = g->maps_t[0]; g->maps_t[2] = g->maps_t[0]; g->maps_t[3] = g->dT.map;
     // (c) S and H jobs of every panel; outputs are patched per run, later panels accumulate
     g->pair = use_pair();
+    g->units = pair_units_plain(g->s);
     const int64_t tile = g->pair ? kPairTile : kTileN;
     g->n_jobs_sh = 2 * g->nk;
     for (int pi = 0; pi < g->panels; ++pi) {
@@ -2040,7 +2117,7 @@ int ozaki_group_run(OzGroup *g, const DevSystem &sys, const KTable &ktab, cudaSt
             if (nev >= 2 * g->nt) e = record(ev[2 * t], st);
             if (e == cudaSuccess)
                 e = g->pair ? launch_pair(g->maps_sh, g->s, g->d_err, jobs, g->n_jobs_sh, g->tiles_sh, g->d_list_sh,
-                                          g->d_progress, st)
+                                          g->d_progress, st, g->units)
                             : launch_prepared(g->maps_sh, g->s, g->d_err, jobs, g->n_jobs_sh, g->tiles_sh,
                                               g->d_list_sh, g->d_progress, st);
             if (e == cudaSuccess && nev >= 2 * g->nt) e = record(ev[2 * t + 1], st);
@@ -2090,7 +2167,7 @@ int ozaki_group_run(OzGroup *g, const DevSystem &sys, const KTable &ktab, cudaSt
         const OzJob *jobs = g->d_jobs_sh + (int64_t)g->n_jobs_sh * pi;
         if (e == cudaSuccess)
             e = g->pair ? launch_pair(g->maps_sh, g->s, g->d_err, jobs, g->n_jobs_sh, g->tiles_sh, g->d_list_sh,
-                                      g->d_progress, st)
+                                      g->d_progress, st, g->units)
                         : launch_prepared(g->maps_sh, g->s, g->d_err, jobs, g->n_jobs_sh, g->tiles_sh, g->d_list_sh,
                                           g->d_progress, st);
         nl += 1;

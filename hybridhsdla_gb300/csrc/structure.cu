@@ -18,6 +18,7 @@ __device__ __forceinline__ double2 cmul_d(double2 a, double2 b) {
     return make_double2(fma(a.x, b.x, -a.y * b.y), fma(a.x, b.y, a.y * b.x));
 }
 
+
 // sf[t][(ix ny + iy) nz + iz] = sum over the atoms of type t of ex[a][ix] ey[a][iy] ez[a][iz],
 // the atoms listed type by type (order[type_begin[t] .. type_begin[t+1])).
 __global__ void sf_table_kernel(const double2 *__restrict__ ex, const double2 *__restrict__ ey,
