@@ -175,6 +175,18 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
           "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
         : "r"(taddr));
 }
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&r)[16]) {
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+          "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr));
+}
+template <int kN>
+__device__ __forceinline__ void tmem_ld(uint32_t taddr, uint32_t (&r)[kN]) {
+    if constexpr (kN == 32) tmem_ld32(taddr, r);
+    else tmem_ld16(taddr, r);
+}
 __device__ __forceinline__ void tmem_ld_wait() { asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory"); }
 
 // ------------------------------------------------------- work decomposition
@@ -514,18 +526,40 @@ __global__ void __launch_bounds__(kThreads, 1)
 // Every wait is bounded as in oz_gemm_kernel; both CTAs meet at a cluster barrier before TMEM
 // is freed, so no CTA exits while its shared memory or TMEM can still be addressed by the other.
 constexpr int kPairTile = 256;
-#ifndef HSDLA_DRAIN_COLS
-#define HSDLA_DRAIN_COLS 4
+// Epilogue warps of the pair kernel: four per TMEM lane quadrant (each drains a quarter of the
+// columns) hide the drain's latencies twice as well as two; HSDLA_PAIR_EPI_WARPS=8 builds two.
+#ifndef HSDLA_PAIR_EPI_WARPS
+#define HSDLA_PAIR_EPI_WARPS 16
+#endif
+constexpr int kPairEpiWarps = HSDLA_PAIR_EPI_WARPS;
+constexpr int kPairThreads = 64 + 32 * kPairEpiWarps;      // warp 0 TMA, warp 1 MMA, the rest epilogue
+constexpr int kColsPerWarp = 4 * kPairTile / kPairEpiWarps;
+constexpr int kChunksPerWarp = kColsPerWarp / 32;
+static_assert(kChunksPerWarp >= 1 && kColsPerWarp % 32 == 0, "epilogue column split");
+// TMEM columns per load (re and im each): 16 with four epilogue warps per quadrant (18 warps leave
+// 96 registers a thread), 32 with two
+constexpr int kLdColsPair() { return kPairEpiWarps > 8 ? 16 : 32; }
+constexpr int kLdCols = kLdColsPair();
+// Operand stages of the pair kernel and the drain staging that shares its shared memory (over the
+// epilogue warps, kDrainBufs buffers each: a warp fills one while the bulk copies of the others
+// read them).  The drain's throughput is bounded by the staging bytes in flight.
+#ifndef HSDLA_PAIR_STAGES
+#define HSDLA_PAIR_STAGES 3
+#endif
+#ifndef HSDLA_PAIR_STAGING_KB
+#define HSDLA_PAIR_STAGING_KB 32
 #endif
 #ifndef HSDLA_DRAIN_BUFS
 #define HSDLA_DRAIN_BUFS 2
 #endif
-constexpr int kStageCols = HSDLA_DRAIN_COLS;                 // columns per drain staging buffer
-constexpr int kDrainBufs = HSDLA_DRAIN_BUFS;                 // staging buffers per epilogue warp
+constexpr int kPairStages = HSDLA_PAIR_STAGES;
+constexpr int kDrainBufs = HSDLA_DRAIN_BUFS;
+constexpr int kStageCols = HSDLA_PAIR_STAGING_KB * 1024 / kPairEpiWarps / kDrainBufs / 512;   // columns per buffer
 constexpr int kStageWarpBytes = kDrainBufs * kStageCols * 32 * 16;   // buffers x columns x 32 rows x 16 B
-static_assert(32 % kStageCols == 0 && kDrainBufs >= 2, "drain staging shape");
-static_assert(kPairTile / 2 == 4 * 32, "four 32-column chunks per epilogue warp (the exponent rotation)");
-constexpr int kPairStageBytes = kEpiWarps * kStageWarpBytes;
+static_assert(kStageCols >= 1 && kLdColsPair() % kStageCols == 0, "drain staging shape");
+static_assert(kPairStages * kStageBytes + kPairEpiWarps * kDrainBufs * kStageCols * 512 + 1024 <= 227 * 1024,
+              "pair kernel shared memory");
+constexpr int kPairStageBytes = kPairEpiWarps * kStageWarpBytes;
 // Bulk copies and f64 add-reductions shared memory -> global with an L2 eviction policy
 // (createpolicy): an output tile stays resident through its units (evict_last) and leaves first
 // after its last one (evict_first).
@@ -607,8 +641,8 @@ __device__ __forceinline__ void mma_commit_pair(uint64_t *bar) {
 }
 
 struct __align__(8) PairBarriers {
-    uint64_t full[kStages];      // leader: both CTAs' bytes of a stage landed
-    uint64_t empty[kStages];     // each CTA: the stage's MMAs completed (multicast commit)
+    uint64_t full[kPairStages];      // leader: both CTAs' bytes of a stage landed
+    uint64_t empty[kPairStages];     // each CTA: the stage's MMAs completed (multicast commit)
     uint64_t tfull;              // each CTA: the unit's accumulator is complete (multicast commit)
     uint64_t tempty;             // leader: 16 epilogue warps (both CTAs) drained the accumulator
 };
@@ -625,7 +659,7 @@ struct PairUnits {
     uint8_t flags[kMaxUnits];
 };
 
-__global__ void __launch_bounds__(kThreads, 1)
+__global__ void __launch_bounds__(kPairThreads, 1)
     oz_pair_kernel(const __grid_constant__ CUtensorMap map0, const __grid_constant__ CUtensorMap map1,
                    const __grid_constant__ CUtensorMap map2, const __grid_constant__ CUtensorMap map3,
                    const OzJob *__restrict__ jobs, int num_jobs, int64_t total_tiles, int s, int *err,
@@ -661,9 +695,9 @@ __global__ void __launch_bounds__(kThreads, 1)
     };
 
     if (threadIdx.x == 0) {
-        for (int i = 0; i < kStages; ++i) { mbar_init(&bars.full[i], 1); mbar_init(&bars.empty[i], 1); }
+        for (int i = 0; i < kPairStages; ++i) { mbar_init(&bars.full[i], 1); mbar_init(&bars.empty[i], 1); }
         mbar_init(&bars.tfull, 1);
-        mbar_init(&bars.tempty, 2 * kEpiWarps);
+        mbar_init(&bars.tempty, 2 * kPairEpiWarps);
         abort_flag = 0;
         asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
         for (int i = 0; i < 4; ++i) asm volatile("prefetch.tensormap [%0];\n" ::"l"((uint64_t)map_of(i)) : "memory");
@@ -719,7 +753,7 @@ __global__ void __launch_bounds__(kThreads, 1)
                                     tma_load_2d_pair(st + 32768, rm, fb, xr, (int)((2 * (jj - 1)) * j.rplane + yr));
                                     tma_load_2d_pair(st + 49152, rm, fb, xr, (int)((2 * (jj - 1) + 1) * j.rplane + yr));
                                     ++issued;
-                                    if (++stage == kStages) { stage = 0; phase ^= 1; }
+                                    if (++stage == kPairStages) { stage = 0; phase ^= 1; }
                                 }
                             }
                         }
@@ -730,8 +764,8 @@ __global__ void __launch_bounds__(kThreads, 1)
             // Before exit every stage this CTA issued must have been consumed: its bytes landed and
             // the MMA commit that frees it (multicast, possibly remote) arrived.  Normally these
             // waits return at once; after an abort they are bounded.
-            for (int q = 0; q < kStages && issued > 0; ++q) {
-                if (--stage < 0) { stage = kStages - 1; phase ^= 1; }
+            for (int q = 0; q < kPairStages && issued > 0; ++q) {
+                if (--stage < 0) { stage = kPairStages - 1; phase ^= 1; }
                 mbar_drain_wait(&bars.empty[stage], phase);
                 --issued;
             }
@@ -776,7 +810,7 @@ __global__ void __launch_bounds__(kThreads, 1)
                                         first = false;
                                     }
                                     mma_commit_pair(&bars.empty[stage]);
-                                    if (++stage == kStages) { stage = 0; phase ^= 1; }
+                                    if (++stage == kPairStages) { stage = 0; phase ^= 1; }
                                 }
                             }
                         }
@@ -797,7 +831,7 @@ __global__ void __launch_bounds__(kThreads, 1)
             }
         }
     } else {
-        // ------------------------------------------------------------ epilogue (warps 2..9, both CTAs)
+        // ------------------------------------------------------------ epilogue (warps 2.., both CTAs)
         // A unit's drain: TMEM -> registers -> FP64 with the full scale 2^(2-5t+e_row+e_col) (built
         // with integer operations) -> the output: a plain store for the tile's first unit,
         // fire-and-forget f64 reductions in L2 for the others.  Each lane owns one output row, so
@@ -805,8 +839,8 @@ __global__ void __launch_bounds__(kThreads, 1)
         // SM never waits on the output.  Only stored elements (row < m, col < n, lower: row >=
         // col) are written.
         const int q = warp & 3;                      // TMEM lane quadrant of this warp
-        const int cbeg = ((warp - 2) >> 2) * (kPairTile / 2);   // its half of the columns
-        unsigned char *stg = smem + kStages * kStageBytes + (warp - 2) * kStageWarpBytes;
+        const int cbeg = ((warp - 2) >> 2) * kColsPerWarp;      // its share of the columns
+        unsigned char *stg = smem + kPairStages * kStageBytes + (warp - 2) * kStageWarpBytes;
         const uint32_t stg_s = smem_u32(stg);
         const uint64_t pol_last = policy_evict_last(), pol_first = policy_evict_first();
         int64_t unit = 0;
@@ -820,18 +854,19 @@ __global__ void __launch_bounds__(kThreads, 1)
             const int erow = row < m ? j.el[row] : 0;
             double2 *out = j.out;
             // The tile's column exponents, loaded once for all its units: lane l holds column
-            // colt + 32 c + l of chunk c in e0..e3 (rotated after each chunk, so the current chunk's
-            // are always in e0), with each chunk's range for the fast-path test.
+            // colt + 32 c + l of chunk c in ex[c] (rotated after each chunk, so the current chunk's
+            // are always in ex[0]), with each chunk's range for the fast-path test.
             const int64_t colt = tn * kPairTile + cbeg;
             const int32_t *er = j.er;
-            int e0 = colt + lane < n ? __ldg(er + colt + lane) : 0;
-            int e1 = colt + 32 + lane < n ? __ldg(er + colt + 32 + lane) : 0;
-            int e2 = colt + 64 + lane < n ? __ldg(er + colt + 64 + lane) : 0;
-            int e3 = colt + 96 + lane < n ? __ldg(er + colt + 96 + lane) : 0;
-            int lo0 = __reduce_min_sync(0xffffffffu, e0), hi0 = __reduce_max_sync(0xffffffffu, e0);
-            int lo1 = __reduce_min_sync(0xffffffffu, e1), hi1 = __reduce_max_sync(0xffffffffu, e1);
-            int lo2 = __reduce_min_sync(0xffffffffu, e2), hi2 = __reduce_max_sync(0xffffffffu, e2);
-            int lo3 = __reduce_min_sync(0xffffffffu, e3), hi3 = __reduce_max_sync(0xffffffffu, e3);
+            int ex[kChunksPerWarp], exlo[kChunksPerWarp], exhi[kChunksPerWarp];
+#pragma unroll
+            for (int c = 0; c < kChunksPerWarp; ++c)
+                ex[c] = colt + 32 * c + lane < n ? __ldg(er + colt + 32 * c + lane) : 0;
+#pragma unroll
+            for (int c = 0; c < kChunksPerWarp; ++c) {
+                exlo[c] = __reduce_min_sync(0xffffffffu, ex[c]);
+                exhi[c] = __reduce_max_sync(0xffffffffu, ex[c]);
+            }
             for (int u = 0; ok && u < units.n; ++u) {
                 const int t = units.t[u];
                 const uint8_t fl = units.flags[u];
@@ -848,61 +883,70 @@ __global__ void __launch_bounds__(kThreads, 1)
                     const uint32_t tbase = tmem_base + ((uint32_t)(q * 32) << 16);
                     int rd = 0;
 #pragma unroll 1
-                    for (int c0 = cbeg; c0 < cbeg + kPairTile / 2; c0 += 32) {
-                        uint32_t vre[32], vim[32];
-                        tmem_ld32(tbase + c0, vre);
-                        tmem_ld32(tbase + kPairTile + c0, vim);
-                        tmem_ld_wait();
-                        if (c0 + 32 >= cbeg + kPairTile / 2) {
-                            tc_fence_before();
-                            __syncwarp();
-                            if (lane == 0) mbar_arrive_remote(tempty_leader);
-                        }
+                    for (int c0 = cbeg; c0 < cbeg + kColsPerWarp; c0 += 32) {
                         const int64_t colb = colt + (c0 - cbeg);
-                        const bool fast = __all_sync(0xffffffffu, pow2_ok(kb + lo0) && pow2_ok(kb + hi0));
+                        const bool fast = __all_sync(0xffffffffu, pow2_ok(kb + exlo[0]) && pow2_ok(kb + exhi[0]));
                         // 2^(kb + e_col) as an FP64 exponent bias: the row's part plus e_col << 20
                         const uint32_t rbias = pow2_ebias(kb);
 #pragma unroll
-                        for (int g4 = 0; g4 < 32; g4 += kStageCols, ++rd) {
-                            const uint32_t buf = (uint32_t)(rd % kDrainBufs) * (kStageCols * 512);
-                            if (lane < kStageCols) bulk_wait_read<kDrainBufs - 1>();
-                            __syncwarp();
-#pragma unroll
-                            for (int cc = 0; cc < kStageCols; ++cc) {
-                                const int c = g4 + cc;
-                                const int ec = __shfl_sync(0xffffffffu, e0, c);
-                                double re, im;
-                                if (fast) {
-                                    const uint32_t eb = rbias + ((uint32_t)ec << 20);
-                                    re = f32_pow2_to_f64_fast(vre[c], eb);
-                                    im = f32_pow2_to_f64_fast(vim[c], eb);
-                                } else {
-                                    re = f32_pow2_to_f64_slow(vre[c], kb + ec);
-                                    im = f32_pow2_to_f64_slow(vim[c], kb + ec);
-                                }
-                                *reinterpret_cast<double2 *>(stg + buf + cc * 512 + lane * 16) = make_double2(re, im);
+                        for (int hh = 0; hh < 32; hh += kLdCols) {
+                            uint32_t vre[kLdCols], vim[kLdCols];
+                            tmem_ld<kLdCols>(tbase + c0 + hh, vre);
+                            tmem_ld<kLdCols>(tbase + kPairTile + c0 + hh, vim);
+                            tmem_ld_wait();
+                            if (c0 + hh + kLdCols >= cbeg + kColsPerWarp) {
+                                tc_fence_before();
+                                __syncwarp();
+                                if (lane == 0) mbar_arrive_remote(tempty_leader);
                             }
-                            fence_async_smem();
-                            __syncwarp();
-                            // lane cc issues the copy of the group's column cc (32 rows) and commits it
-                            if (lane < kStageCols) {
-                                const int64_t col = colb + g4 + lane;
-                                const int64_t lo = lower ? max(r0, col) : r0, hi = min(r0 + 32, m);
-                                if (col < n && lo < hi) {
-                                    const uint32_t src = stg_s + buf + lane * 512 + (uint32_t)(lo - r0) * 16;
-                                    double2 *dst = out + lo + ldo * col;
-                                    if (first) bulk_store_g(dst, src, (uint32_t)(hi - lo) * 16, pol);
-                                    else bulk_add_g(dst, src, (uint32_t)(hi - lo) * 16, pol);
+#pragma unroll
+                            for (int g4 = 0; g4 < kLdCols; g4 += kStageCols, ++rd) {
+                                const uint32_t buf = (uint32_t)(rd % kDrainBufs) * (kStageCols * 512);
+                                if (lane < kStageCols) bulk_wait_read<kDrainBufs - 1>();
+                                __syncwarp();
+#pragma unroll
+                                for (int cc = 0; cc < kStageCols; ++cc) {
+                                    const int c = g4 + cc;
+                                    const int ec = __shfl_sync(0xffffffffu, ex[0], hh + c);
+                                    double re, im;
+                                    if (fast) {
+                                        const uint32_t eb = rbias + ((uint32_t)ec << 20);
+                                        re = f32_pow2_to_f64_fast(vre[c], eb);
+                                        im = f32_pow2_to_f64_fast(vim[c], eb);
+                                    } else {
+                                        re = f32_pow2_to_f64_slow(vre[c], kb + ec);
+                                        im = f32_pow2_to_f64_slow(vim[c], kb + ec);
+                                    }
+                                    *reinterpret_cast<double2 *>(stg + buf + cc * 512 + lane * 16) = make_double2(re, im);
                                 }
-                                bulk_commit();
+                                fence_async_smem();
+                                __syncwarp();
+                                // lane cc issues the copy of the group's column cc (32 rows) and commits it
+                                if (lane < kStageCols) {
+                                    const int64_t col = colb + hh + g4 + lane;
+                                    const int64_t lo = lower ? max(r0, col) : r0, hi = min(r0 + 32, m);
+                                    if (col < n && lo < hi) {
+                                        const uint32_t src = stg_s + buf + lane * 512 + (uint32_t)(lo - r0) * 16;
+                                        double2 *dst = out + lo + ldo * col;
+                                        if (first) bulk_store_g(dst, src, (uint32_t)(hi - lo) * 16, pol);
+                                        else bulk_add_g(dst, src, (uint32_t)(hi - lo) * 16, pol);
+                                    }
+                                    bulk_commit();
+                                }
                             }
                         }
-                        // next chunk's exponents and range into e0 / lo0 / hi0 (a cyclic rotation:
-                        // after the unit's four chunks the registers are back in order)
-                        const int xe = e0, xl = lo0, xh = hi0;
-                        e0 = e1; e1 = e2; e2 = e3; e3 = xe;
-                        lo0 = lo1; lo1 = lo2; lo2 = lo3; lo3 = xl;
-                        hi0 = hi1; hi1 = hi2; hi2 = hi3; hi3 = xh;
+                        // next chunk's exponents and range into ex[0] (a cyclic rotation: after the
+                        // unit's chunks the registers are back in order)
+                        const int xe = ex[0], xl = exlo[0], xh = exhi[0];
+#pragma unroll
+                        for (int c = 0; c + 1 < kChunksPerWarp; ++c) {
+                            ex[c] = ex[c + 1];
+                            exlo[c] = exlo[c + 1];
+                            exhi[c] = exhi[c + 1];
+                        }
+                        ex[kChunksPerWarp - 1] = xe;
+                        exlo[kChunksPerWarp - 1] = xl;
+                        exhi[kChunksPerWarp - 1] = xh;
                     }
                     ++unit;
                 }
@@ -1071,8 +1115,11 @@ __device__ __noinline__ void weighted_chunk(const double2 *zc, const double *vv,
     write_planes<kV>(xr, xi, s, row, plane);
 }
 
+#ifndef HSDLA_SLICE_CTAS
+#define HSDLA_SLICE_CTAS 2
+#endif
 template <bool kDual, bool kScaled>
-__global__ void __launch_bounds__(kSliceThreads, 1) oz_slice_kernel(const __grid_constant__ SliceTab tab) {
+__global__ void __launch_bounds__(kSliceThreads, HSDLA_SLICE_CTAS) oz_slice_kernel(const __grid_constant__ SliceTab tab) {
     // values per thread and step of the digit pass (the dual pass keeps two operands' state)
     constexpr int kV = kDual ? 4 : kSliceVec;
     const int64_t r = blockIdx.x;           // plane row
@@ -1611,7 +1658,7 @@ int upload_schedule(std::vector<OzJob> &jobs, OzJob *d_jobs, int4 *d_list, int64
 cudaError_t launch_pair(const CUtensorMap *maps, int s, int *d_err, const OzJob *d_jobs, int n_jobs, int64_t total,
                         const int4 *d_list, int *d_progress, cudaStream_t st, const PairUnits &units) {
     if (total <= 0) return cudaSuccess;
-    const size_t smem = (size_t)kStages * kStageBytes + kPairStageBytes + 1024;
+    const size_t smem = (size_t)kPairStages * kStageBytes + kPairStageBytes + 1024;
     cudaError_t e = cudaFuncSetAttribute(oz_pair_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     cudaLaunchConfig_t cfg = {};
@@ -1620,7 +1667,7 @@ cudaError_t launch_pair(const CUtensorMap *maps, int s, int *d_err, const OzJob 
     at[0].val.clusterDim.x = 2;
     at[0].val.clusterDim.y = 1;
     at[0].val.clusterDim.z = 1;
-    cfg.blockDim = dim3(kThreads);
+    cfg.blockDim = dim3(kPairThreads);
     cfg.dynamicSmemBytes = smem;
     cfg.stream = st;
     cfg.attrs = at;
@@ -2115,9 +2162,12 @@ int ozaki_group_run(OzGroup *g, const DevSystem &sys, const KTable &ktab, cudaSt
         for (int t = 0; t < g->nt && e == cudaSuccess; ++t) {
             const OzJob *jobs = g->d_jobs_sh + (int64_t)g->n_jobs_sh * t;
             if (nev >= 2 * g->nt) e = record(ev[2 * t], st);
+            // no grid lockstep here: the per-type operands are small enough for L2 without it, and
+            // pairs that drift apart spread their drains over the MMA phases of the others (c2
+            // 34.5 -> 33.8 ms, c3 11.7 -> 11.4 ms, c4 461 -> 442 ms per k-point)
             if (e == cudaSuccess)
                 e = g->pair ? launch_pair(g->maps_sh, g->s, g->d_err, jobs, g->n_jobs_sh, g->tiles_sh, g->d_list_sh,
-                                          g->d_progress, st, g->units)
+                                          nullptr, st, g->units)
                             : launch_prepared(g->maps_sh, g->s, g->d_err, jobs, g->n_jobs_sh, g->tiles_sh,
                                               g->d_list_sh, g->d_progress, st);
             if (e == cudaSuccess && nev >= 2 * g->nt) e = record(ev[2 * t + 1], st);
