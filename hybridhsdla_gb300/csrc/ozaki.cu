@@ -1275,16 +1275,17 @@ struct Arena {
     }
 };
 
-int64_t operand_bytes(int s, int64_t rows, int64_t Kpad) {
+// planes: digit planes (2s; 4s with the 2^-5-scaled copies of a merged-unit left operand)
+int64_t operand_bytes(int s, int64_t rows, int64_t Kpad, int planes = 0) {
     const int64_t pr = round_up(rows, kTileM) + kTileM;
-    return round_up(2 * s * pr * (Kpad + pitch_pad()), 1024) + round_up(4 * pr, 1024);
+    return round_up((planes ? planes : 2 * s) * pr * (Kpad + pitch_pad()), 1024) + round_up(4 * pr, 1024);
 }
 
-void carve_operand(Arena &a, DigitOperand &d, int s, int64_t rows, int64_t Kpad) {
+void carve_operand(Arena &a, DigitOperand &d, int s, int64_t rows, int64_t Kpad, int planes = 0) {
     d.plane_rows = round_up(rows, kTileM) + kTileM;
     d.Kpad = Kpad;
     d.pitch = Kpad + pitch_pad();
-    d.digits = a.take<uint8_t>(2 * s * d.plane_rows * d.pitch);
+    d.digits = a.take<uint8_t>((planes ? planes : 2 * s) * d.plane_rows * d.pitch);
     d.expo = a.take<int32_t>(d.plane_rows);
 }
 
@@ -1621,6 +1622,7 @@ struct OzGroup {
     int *d_err = nullptr;
     bool pair = false;          // S/H on CTA-pair tiles
     PairUnits units{};          // their accumulation units
+    PairUnits units_t{};        // the T application's (structure-factor form on pair tiles)
     bool sf = false;            // structure-factor form
     int tbatch = 1;             // its types per combine batch
     SfTab sft{};                // its combine table (outputs patched per run)
@@ -1778,7 +1780,8 @@ int64_t ozaki_group_persist_bytes(int s, int64_t twoL, int64_t na, int64_t nt, c
         tiles_t += std::max(na, nt) * ((twoL + kTileM - 1) / kTileM) * T;
         tiles_sh += T * (T + 1);
     }
-    return operand_bytes(s, nt * twoL, bpad) + round_up(sizeof(OzJob) * nk * (std::max(na, nt) + 2), 1024) +
+    return operand_bytes(s, nt * twoL, bpad, use_pair() ? 4 * s : 2 * s) +
+           round_up(sizeof(OzJob) * nk * (std::max(na, nt) + 2), 1024) +
            round_up(sizeof(OzJob) * 2 * nk * panels, 1024) + round_up(sizeof(int4) * (tiles_t + panels), 1024) +
            round_up(sizeof(int4) * (tiles_sh + 1), 1024) + round_up(sizeof(int) * kProgressCap, 1024) + 8192;
 }
@@ -1822,7 +1825,8 @@ static int group_prepare_sf(OzakiPlan &oz, const OzGroupDesc &d, const std::vect
     carve_rows(g->dM, g->pair ? 4 * s : 2 * s);
     carve_rows(g->dW, 2 * s);    // M diag(w_t)
     carve_rows(g->dX, 2 * s);    // Z
-    carve_operand(keep, g->dT, s, d.nt * d.twoL, tkb * kKBlock);
+    // T: the left operand of the T application, with its scaled copy on pair tiles
+    carve_operand(keep, g->dT, s, d.nt * d.twoL, tkb * kKBlock, g->pair ? 4 * s : 2 * s);
     const int64_t nk = g->nk;
     int64_t tiles_t = 0, tiles_sh = 0;
     for (int64_t x : G) {
@@ -1853,13 +1857,15 @@ static int group_prepare_sf(OzakiPlan &oz, const OzGroupDesc &d, const std::vect
     p.tX = table(g->dX, 1);
     g->pan.push_back(p);
     g->panels = 1;
-    cudaError_t e = slice(d.Tfull, d.twoL, nullptr, d.twoL, d.nt * d.twoL, d.twoL, g->bpad, s, g->dT, st);
+    SliceTab tT = slice_table(d.Tfull, d.twoL, nullptr, d.twoL, d.nt * d.twoL, d.twoL, g->bpad, s, g->dT);
+    tT.scaled = g->pair ? 1 : 0;
+    cudaError_t e = slice_launch(tT, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) { g_oz_err = cudaGetErrorString(e); return fail(HSDLA_ERR_CUDA); }
     int rc = make_map(g->dM, g->pair ? 2 * s : s);
     if (!rc) rc = make_map(g->dW, s);
     if (!rc) rc = make_map(g->dX, s);
-    if (!rc) rc = make_map(g->dT, s);
+    if (!rc) rc = make_map(g->dT, g->pair ? 2 * s : s);
     if (rc) return fail(rc);
     // T application per type: Z_t = T_t M_t
     std::vector<OzJob> jt;
@@ -1878,7 +1884,9 @@ static int group_prepare_sf(OzakiPlan &oz, const OzGroupDesc &d, const std::vect
             jt.push_back(j);
         }
     g->n_jobs_t = (int)jt.size();
-    rc = upload_schedule(jt, g->d_jobs_t, g->d_list_t, g->tiles_t);
+    // on pair tiles (256 x 256: one tile row per type) in merged accumulation units
+    rc = upload_schedule(jt, g->d_jobs_t, g->d_list_t, g->tiles_t, g->pair ? kPairTile : kTileN);
+    g->units_t = g->pair ? pair_units(s, tkb, env_int("HSDLA_MERGE", 1) != 0) : pair_units_plain(s);
     if (rc) return fail(rc);
     g->maps_t[0] = g->dM.map; g->maps_t[1] = g->dM.map; g->maps_t[2] = g->dM.map; g->maps_t[3] = g->dT.map;
     // per type: S_t = M_t^H diag(w_t) M_t and H_t = M_t^H Z_t into the products; on pair tiles
@@ -2155,8 +2163,10 @@ int ozaki_group_run(OzGroup *g, const DevSystem &sys, const KTable &ktab, cudaSt
     if (g->sf) {
         e = slice_launch(g->tM, st);                      // M and M diag(w_t)
         if (e == cudaSuccess)
-            e = launch_prepared(g->maps_t, g->s, g->d_err, g->d_jobs_t, g->n_jobs_t, g->tiles_t, g->d_list_t, nullptr,
-                                st);
+            e = g->pair ? launch_pair(g->maps_t, g->s, g->d_err, g->d_jobs_t, g->n_jobs_t, g->tiles_t, g->d_list_t,
+                                      nullptr, st, g->units_t)
+                        : launch_prepared(g->maps_t, g->s, g->d_err, g->d_jobs_t, g->n_jobs_t, g->tiles_t,
+                                          g->d_list_t, nullptr, st);
         if (e == cudaSuccess) e = slice_launch(g->pan[0].tX, st);    // Z
         nl += 3;
         for (int t = 0; t < g->nt && e == cudaSuccess; ++t) {
