@@ -45,6 +45,7 @@ WORKLOAD_TEXT = {
     "c2": "c2: cubic a=24 bohr, 128 atoms / 8 types, lmax 10, n_G 8000, 1 k-point",
     "c3": "c3: 17.6x17.6x25.2 bohr, 64 atoms / 4 types, lmax 8, 64 k-points (4x4x4), n_G 6000-6600, CUDA graph",
     "c4": "c4: cubic a=40 bohr, 512 atoms / 16 types, lmax 10, 4 k-points, n_G 19800-20700, CUDA graph",
+    "c2t1": "c2t1: c2's cell and n_G 8000 with 16 atoms of one type (one per-type S/H launch of c2's shape)",
 }
 PROFILE_SUMMARY = os.path.join(ROOT, "profiles", "oz_pair_c2.md")
 
@@ -299,7 +300,8 @@ def run_ours(args):
     traffic = _traffic_from_profile() if args.workload == "c2" else None
     roof = {"bound": "tensor", "achieved": achieved, "peak": fp8_peak, "unit": "TFLOP/s",
             "frac": achieved / fp8_peak, "traffic": traffic,
-            "kernel": "oz_pair_kernel (S and H lower-triangle digit products, CTA-pair 256x256 tiles)",
+            "kernel": "oz_pair_kernel (one type's S and H lower-triangle digit products per launch, "
+                      "CTA-pair 256x256 tiles; achieved and traffic per launch)",
             "peak_source": f"2 x {src} bf16 burst (FP8 e4m3 dense rate = 2x bf16 on tcgen05)"}
 
     cpu = None

@@ -122,6 +122,10 @@ CONFIGS: Dict[str, dict] = {
     # 512 atoms / 16 types, lmax 10, 4 k-points, n_G ~20000
     "c4": dict(cell=(40.0, 40.0, 40.0), atoms=512, types=16, rmt=1.9, min_sep=3.8,
                lmax=10, kpts="mp4x1", n_g=(19000, 21000), seed=1004),
+    # c2's cell and basis with one type of 16 atoms: one per-type S/H launch of c2's shape on a
+    # few GB of device memory (the case profiled in full)
+    "c2t1": dict(cell=(24.0, 24.0, 24.0), atoms=16, types=1, rmt=2.0, min_sep=4.0,
+                 lmax=10, kpts=[(0.1, 0.2, 0.3)], n_g=8000, seed=1002),
     # tiny cases for fast parity tests
     "t0": dict(cell=(9.0, 9.5, 10.0), atoms=3, types=2, rmt=2.0, min_sep=4.2,
                lmax=3, kpts=[(0.1, 0.2, 0.3)], n_g=37, seed=7),
