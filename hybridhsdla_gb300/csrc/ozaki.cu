@@ -553,12 +553,13 @@ constexpr int kLdCols = kLdColsPair();
 #define HSDLA_DRAIN_BUFS 2
 #endif
 constexpr int kPairStages = HSDLA_PAIR_STAGES;
+constexpr int kPairStagesHalf = 4;          // 48 KB stages of the half-width tiles
+constexpr int kPairStagesMax = kPairStages > kPairStagesHalf ? kPairStages : kPairStagesHalf;
 constexpr int kDrainBufs = HSDLA_DRAIN_BUFS;
 constexpr int kStageCols = HSDLA_PAIR_STAGING_KB * 1024 / kPairEpiWarps / kDrainBufs / 512;   // columns per buffer
 constexpr int kStageWarpBytes = kDrainBufs * kStageCols * 32 * 16;   // buffers x columns x 32 rows x 16 B
 static_assert(kStageCols >= 1 && kLdColsPair() % kStageCols == 0, "drain staging shape");
-static_assert(kPairStages * kStageBytes + kPairEpiWarps * kDrainBufs * kStageCols * 512 + 1024 <= 227 * 1024,
-              "pair kernel shared memory");
+
 constexpr int kPairStageBytes = kPairEpiWarps * kStageWarpBytes;
 // Bulk copies and f64 add-reductions shared memory -> global with an L2 eviction policy
 // (createpolicy): an output tile stays resident through its units (evict_last) and leaves first
@@ -641,10 +642,10 @@ __device__ __forceinline__ void mma_commit_pair(uint64_t *bar) {
 }
 
 struct __align__(8) PairBarriers {
-    uint64_t full[kPairStages];      // leader: both CTAs' bytes of a stage landed
-    uint64_t empty[kPairStages];     // each CTA: the stage's MMAs completed (multicast commit)
-    uint64_t tfull;              // each CTA: the unit's accumulator is complete (multicast commit)
-    uint64_t tempty;             // leader: 16 epilogue warps (both CTAs) drained the accumulator
+    uint64_t full[kPairStagesMax];   // leader: both CTAs' bytes of a stage landed
+    uint64_t empty[kPairStagesMax];  // each CTA: the stage's MMAs completed (multicast commit)
+    uint64_t tfull[2];           // each CTA: a TMEM buffer's accumulator is complete (multicast commit)
+    uint64_t tempty[2];          // leader: the epilogue warps of both CTAs drained the buffer
 };
 
 // Accumulation units of a pair launch, in drain order.  Unit u sums, per K-chunk, the digit pairs
@@ -659,12 +660,40 @@ struct PairUnits {
     uint8_t flags[kMaxUnits];
 };
 
+// Tile shape of a pair launch.  kHalves = 1: one 256 x 256 accumulator (re + im, all 512 TMEM
+// columns), so a unit's MMAs wait while the previous unit drains.  kHalves = 2: every unit runs
+// as two halves of 128 output columns (MMA N = 128) into alternating TMEM buffers, so one half
+// drains while the other computes; the left operand is staged once per half (1.5x the operand
+// traffic of kHalves = 1) and the right operand's stage holds 64 rows per CTA (its own tensor map).
+template <int kHalves>
+struct PairShape {
+    static constexpr int kN = kPairTile / kHalves;             // output columns of a unit half
+    static constexpr int kBRows = kN / 2;                      // right-operand rows a CTA stages
+    static constexpr int kStageBytes = 2 * kTileM * kKBlock + 2 * kBRows * kKBlock;
+    static constexpr int kStages = kHalves == 1 ? kPairStages : kPairStagesHalf;
+    static constexpr int kBufCols = 2 * kN;                    // TMEM columns of a buffer (re + im)
+    static constexpr int kColsPerWarp = 4 * kN / kPairEpiWarps;   // per quadrant: 4 warps share kN
+    static constexpr int kChunks = kColsPerWarp / 32;
+    static constexpr size_t kSmem = (size_t)kStages * kStageBytes + kPairStageBytes + 1024;
+    static_assert(kChunks >= 1 && kColsPerWarp % 32 == 0, "epilogue column split");
+    static_assert(kStages <= kPairStagesMax, "stage barriers");
+    static_assert(kSmem <= 227 * 1024, "pair kernel shared memory");
+};
+__host__ __device__ constexpr uint32_t idesc_f8_pair_n(bool negA, int n) {
+    return (1u << 4) | ((negA ? 1u : 0u) << 13) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(kPairTile >> 4) << 24);
+}
+
+template <int kHalves>
 __global__ void __launch_bounds__(kPairThreads, 1)
     oz_pair_kernel(const __grid_constant__ CUtensorMap map0, const __grid_constant__ CUtensorMap map1,
                    const __grid_constant__ CUtensorMap map2, const __grid_constant__ CUtensorMap map3,
                    const OzJob *__restrict__ jobs, int num_jobs, int64_t total_tiles, int s, int *err,
                    const int4 *__restrict__ tile_list, int *progress, int sync_every, int slack,
                    const __grid_constant__ PairUnits units) {
+    using Shape = PairShape<kHalves>;
+    constexpr int kStages = Shape::kStages;
+    constexpr int kStageB = Shape::kStageBytes;
+    constexpr int kN = Shape::kN;
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     unsigned char *smem = reinterpret_cast<unsigned char *>(
         (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
@@ -695,9 +724,8 @@ __global__ void __launch_bounds__(kPairThreads, 1)
     };
 
     if (threadIdx.x == 0) {
-        for (int i = 0; i < kPairStages; ++i) { mbar_init(&bars.full[i], 1); mbar_init(&bars.empty[i], 1); }
-        mbar_init(&bars.tfull, 1);
-        mbar_init(&bars.tempty, 2 * kPairEpiWarps);
+        for (int i = 0; i < kStages; ++i) { mbar_init(&bars.full[i], 1); mbar_init(&bars.empty[i], 1); }
+        for (int b = 0; b < 2; ++b) { mbar_init(&bars.tfull[b], 1); mbar_init(&bars.tempty[b], 2 * kPairEpiWarps); }
         abort_flag = 0;
         asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
         for (int i = 0; i < 4; ++i) asm volatile("prefetch.tensormap [%0];\n" ::"l"((uint64_t)map_of(i)) : "memory");
@@ -714,8 +742,9 @@ __global__ void __launch_bounds__(kPairThreads, 1)
     tc_fence_after();
     const uint32_t tmem_base = tmem_base_sh;
     const uint32_t full0_leader = mapa_rank(smem_u32(&bars.full[0]), 0);
-    const uint32_t tempty_leader = mapa_rank(smem_u32(&bars.tempty), 0);
-    const int64_t half = (int64_t)rank * (kPairTile / 2);
+    const uint32_t tempty0_leader = mapa_rank(smem_u32(&bars.tempty[0]), 0);
+    const int64_t half = (int64_t)rank * (kPairTile / 2);     // this CTA's rows of a tile
+    const int64_t bhalf = (int64_t)rank * Shape::kBRows;        // this CTA's right-operand rows of a half
 
     if (warp == 0) {
         // ------------------------------------------------------------ TMA producers (both CTAs)
@@ -733,27 +762,31 @@ __global__ void __launch_bounds__(kPairThreads, 1)
                     const int64_t ck = merged ? j.nkb : chunk_kblocks(min(s, t - 1) - max(1, t - s) + 1);
                     for (int64_t cb = 0; ok && cb < j.nkb; cb += ck) {
                         const int64_t ce = min(j.nkb, cb + ck);
-                        for (int64_t kb = cb; ok && kb < ce; ++kb) {
-                            for (int part = 0; ok && part <= merged; ++part) {
-                                const int tt = t + part, ilo = max(1, tt - s), ihi = min(s, tt - 1);
-                                for (int i = ilo; i <= ihi; ++i) {
-                                    const int jj = tt - i;
-                                    const int lp = (part ? 2 * s : 0) + 2 * (i - 1);   // scaled planes of a merged part
-                                    if (leader && progress && issued > 0 && issued % sync_every == 0 &&
-                                        !grid_lockstep(progress, (int)npairs, (int)(issued / sync_every), &abort_flag,
-                                                       err, (int)pair, slack)) { ok = false; break; }
-                                    if (!pwait(&bars.empty[stage], phase ^ 1, 1, stage, (int)issued)) { ok = false; break; }
-                                    unsigned char *st = smem + stage * kStageBytes;
-                                    if (leader) mbar_expect_tx(&bars.full[stage], 2 * kStageBytes);
-                                    const uint32_t fb = full0_leader + stage * 8;
-                                    const int xl = (int)(j.lk0 + kb * kKBlock), xr = (int)(j.rk0 + kb * kKBlock);
-                                    const int64_t yl = j.lrow0 + tm * kPairTile + half, yr = j.rrow0 + tn * kPairTile + half;
-                                    tma_load_2d_pair(st, lm, fb, xl, (int)(lp * j.lplane + yl));
-                                    tma_load_2d_pair(st + 16384, lm, fb, xl, (int)((lp + 1) * j.lplane + yl));
-                                    tma_load_2d_pair(st + 32768, rm, fb, xr, (int)((2 * (jj - 1)) * j.rplane + yr));
-                                    tma_load_2d_pair(st + 49152, rm, fb, xr, (int)((2 * (jj - 1) + 1) * j.rplane + yr));
-                                    ++issued;
-                                    if (++stage == kPairStages) { stage = 0; phase ^= 1; }
+                        for (int h = 0; ok && h < kHalves; ++h) {
+                            for (int64_t kb = cb; ok && kb < ce; ++kb) {
+                                for (int part = 0; ok && part <= merged; ++part) {
+                                    const int tt = t + part, ilo = max(1, tt - s), ihi = min(s, tt - 1);
+                                    for (int i = ilo; i <= ihi; ++i) {
+                                        const int jj = tt - i;
+                                        const int lp = (part ? 2 * s : 0) + 2 * (i - 1);   // scaled planes of a merged part
+                                        if (leader && progress && issued > 0 && issued % sync_every == 0 &&
+                                            !grid_lockstep(progress, (int)npairs, (int)(issued / sync_every),
+                                                           &abort_flag, err, (int)pair, slack)) { ok = false; break; }
+                                        if (!pwait(&bars.empty[stage], phase ^ 1, 1, stage, (int)issued)) { ok = false; break; }
+                                        unsigned char *st = smem + stage * kStageB;
+                                        if (leader) mbar_expect_tx(&bars.full[stage], 2 * kStageB);
+                                        const uint32_t fb = full0_leader + stage * 8;
+                                        const int xl = (int)(j.lk0 + kb * kKBlock), xr = (int)(j.rk0 + kb * kKBlock);
+                                        const int64_t yl = j.lrow0 + tm * kPairTile + half;
+                                        const int64_t yr = j.rrow0 + tn * kPairTile + h * kN + bhalf;
+                                        tma_load_2d_pair(st, lm, fb, xl, (int)(lp * j.lplane + yl));
+                                        tma_load_2d_pair(st + 16384, lm, fb, xl, (int)((lp + 1) * j.lplane + yl));
+                                        tma_load_2d_pair(st + 32768, rm, fb, xr, (int)((2 * (jj - 1)) * j.rplane + yr));
+                                        tma_load_2d_pair(st + 32768 + Shape::kBRows * kKBlock, rm, fb, xr,
+                                                         (int)((2 * (jj - 1) + 1) * j.rplane + yr));
+                                        ++issued;
+                                        if (++stage == kStages) { stage = 0; phase ^= 1; }
+                                    }
                                 }
                             }
                         }
@@ -764,8 +797,8 @@ __global__ void __launch_bounds__(kPairThreads, 1)
             // Before exit every stage this CTA issued must have been consumed: its bytes landed and
             // the MMA commit that frees it (multicast, possibly remote) arrived.  Normally these
             // waits return at once; after an abort they are bounded.
-            for (int q = 0; q < kPairStages && issued > 0; ++q) {
-                if (--stage < 0) { stage = kPairStages - 1; phase ^= 1; }
+            for (int q = 0; q < kStages && issued > 0; ++q) {
+                if (--stage < 0) { stage = kStages - 1; phase ^= 1; }
                 mbar_drain_wait(&bars.empty[stage], phase);
                 --issued;
             }
@@ -775,11 +808,11 @@ __global__ void __launch_bounds__(kPairThreads, 1)
         if (lane == 0 && leader) {
             int stage = 0;
             uint32_t phase = 0;
-            int64_t unit = 0;
+            int64_t unit = 0;            // unit chunks issued (each uses every buffer once)
+            int hb = 0;                  // buffer of a partially issued half
             bool ok = true;
-            const uint32_t id_pos = idesc_f8_pair(false), id_neg = idesc_f8_pair(true);
+            const uint32_t id_pos = idesc_f8_pair_n(false, kN), id_neg = idesc_f8_pair_n(true, kN);
             const uint32_t sbase = smem_u32(smem);
-            const uint32_t d_re = tmem_base, d_im = tmem_base + kPairTile;
             for (int64_t tile = pair; ok && tile < total_tiles; tile += npairs) {
                 int64_t tm_, tn_;
                 const OzJob &j = resolve_tile(jobs, num_jobs, tile_list, tile, tm_, tn_);
@@ -788,46 +821,53 @@ __global__ void __launch_bounds__(kPairThreads, 1)
                     const int64_t ck = merged ? j.nkb : chunk_kblocks(min(s, t - 1) - max(1, t - s) + 1);
                     for (int64_t cb = 0; ok && cb < j.nkb; cb += ck) {
                         const int64_t ce = min(j.nkb, cb + ck);
-                        if (!pwait(&bars.tempty, (uint32_t)((unit & 1) ^ 1), 2, stage, (int)unit)) { ok = false; break; }
-                        tc_fence_after();
-                        bool first = true;
-                        for (int64_t kb = cb; ok && kb < ce; ++kb) {
-                            for (int part = 0; ok && part <= merged; ++part) {
-                                const int tt = t + part, ilo = max(1, tt - s), ihi = min(s, tt - 1);
-                                for (int i = ilo; i <= ihi; ++i) {
-                                    if (!pwait(&bars.full[stage], phase, 3, stage, (int)unit)) { ok = false; break; }
-                                    tc_fence_after();
-                                    const uint32_t a_re = sbase + stage * kStageBytes, a_im = a_re + 16384;
-                                    const uint32_t b_re = a_re + 32768, b_im = a_re + 49152;
+                        for (int h = 0; ok && h < kHalves; ++h) {
+                            hb = h;
+                            const uint32_t d_re = tmem_base + h * Shape::kBufCols, d_im = d_re + kN;
+                            if (!pwait(&bars.tempty[h], (uint32_t)((unit & 1) ^ 1), 2, stage, (int)unit)) { ok = false; break; }
+                            tc_fence_after();
+                            bool first = true;
+                            for (int64_t kb = cb; ok && kb < ce; ++kb) {
+                                for (int part = 0; ok && part <= merged; ++part) {
+                                    const int tt = t + part, ilo = max(1, tt - s), ihi = min(s, tt - 1);
+                                    for (int i = ilo; i <= ihi; ++i) {
+                                        if (!pwait(&bars.full[stage], phase, 3, stage, (int)unit)) { ok = false; break; }
+                                        tc_fence_after();
+                                        const uint32_t a_re = sbase + stage * kStageB, a_im = a_re + 16384;
+                                        const uint32_t b_re = a_re + 32768, b_im = b_re + Shape::kBRows * kKBlock;
 #pragma unroll
-                                    for (int kk = 0; kk < kKBlock / 32; ++kk) {
-                                        const uint32_t off = kk * 32;
-                                        const uint32_t acc = first ? 0u : 1u;
-                                        mma_f8_pair(d_re, sw128_desc(a_re + off), sw128_desc(b_re + off), id_pos, acc);
-                                        mma_f8_pair(d_re, sw128_desc(a_im + off), sw128_desc(b_im + off), id_pos, 1u);
-                                        mma_f8_pair(d_im, sw128_desc(a_re + off), sw128_desc(b_im + off), id_pos, acc);
-                                        mma_f8_pair(d_im, sw128_desc(a_im + off), sw128_desc(b_re + off), id_neg, 1u);
-                                        first = false;
+                                        for (int kk = 0; kk < kKBlock / 32; ++kk) {
+                                            const uint32_t off = kk * 32;
+                                            const uint32_t acc = first ? 0u : 1u;
+                                            mma_f8_pair(d_re, sw128_desc(a_re + off), sw128_desc(b_re + off), id_pos, acc);
+                                            mma_f8_pair(d_re, sw128_desc(a_im + off), sw128_desc(b_im + off), id_pos, 1u);
+                                            mma_f8_pair(d_im, sw128_desc(a_re + off), sw128_desc(b_im + off), id_pos, acc);
+                                            mma_f8_pair(d_im, sw128_desc(a_im + off), sw128_desc(b_re + off), id_neg, 1u);
+                                            first = false;
+                                        }
+                                        mma_commit_pair(&bars.empty[stage]);
+                                        if (++stage == kStages) { stage = 0; phase ^= 1; }
                                     }
-                                    mma_commit_pair(&bars.empty[stage]);
-                                    if (++stage == kPairStages) { stage = 0; phase ^= 1; }
                                 }
                             }
+                            if (!ok) break;
+                            mma_commit_pair(&bars.tfull[h]);
                         }
                         if (!ok) break;
-                        mma_commit_pair(&bars.tfull);
                         ++unit;
                     }
                 }
             }
             if (!ok) {
-                // a partially issued unit may still be running: commit it and wait (bounded)
-                mma_commit_pair(&bars.tfull);
-                mbar_drain_wait(&bars.tfull, (uint32_t)(unit & 1));
+                // a partially issued half may still be running: commit it and wait (bounded)
+                mma_commit_pair(&bars.tfull[hb]);
+                mbar_drain_wait(&bars.tfull[hb], (uint32_t)(unit & 1));
             } else if (unit > 0) {
                 // the last unit's MMAs and both CTAs' drains of it
-                mbar_drain_wait(&bars.tfull, (uint32_t)((unit - 1) & 1));
-                mbar_drain_wait(&bars.tempty, (uint32_t)((unit - 1) & 1));
+                for (int h = 0; h < kHalves; ++h) {
+                    mbar_drain_wait(&bars.tfull[h], (uint32_t)((unit - 1) & 1));
+                    mbar_drain_wait(&bars.tempty[h], (uint32_t)((unit - 1) & 1));
+                }
             }
         }
     } else {
@@ -838,12 +878,14 @@ __global__ void __launch_bounds__(kPairThreads, 1)
         // successive updates of an element come from one thread and stay in program order; the
         // SM never waits on the output.  Only stored elements (row < m, col < n, lower: row >=
         // col) are written.
+        constexpr int kCols = Shape::kColsPerWarp, kCh = Shape::kChunks;
         const int q = warp & 3;                      // TMEM lane quadrant of this warp
-        const int cbeg = ((warp - 2) >> 2) * kColsPerWarp;      // its share of the columns
-        unsigned char *stg = smem + kPairStages * kStageBytes + (warp - 2) * kStageWarpBytes;
+        const int cbeg = ((warp - 2) >> 2) * kCols;  // its share of a buffer's columns
+        unsigned char *stg = smem + kStages * kStageB + (warp - 2) * kStageWarpBytes;
         const uint32_t stg_s = smem_u32(stg);
         const uint64_t pol_last = policy_evict_last(), pol_first = policy_evict_first();
         int64_t unit = 0;
+        int rd = 0;                                  // staged buffers so far (the ring position)
         bool ok = true;
         for (int64_t tile = pair; ok && tile < total_tiles; tile += npairs) {
             int64_t tm, tn;
@@ -854,18 +896,20 @@ __global__ void __launch_bounds__(kPairThreads, 1)
             const int erow = row < m ? j.el[row] : 0;
             double2 *out = j.out;
             // The tile's column exponents, loaded once for all its units: lane l holds column
-            // colt + 32 c + l of chunk c in ex[c] (rotated after each chunk, so the current chunk's
-            // are always in ex[0]), with each chunk's range for the fast-path test.
-            const int64_t colt = tn * kPairTile + cbeg;
+            // tn*256 + h*kN + cbeg + 32c + l of half h, chunk c in ex[h kCh + c], with each chunk's
+            // range for the fast-path test.  The registers rotate after each chunk, so the current
+            // chunk's are always in ex[0] (after a unit's chunks they are back in order).
             const int32_t *er = j.er;
-            int ex[kChunksPerWarp], exlo[kChunksPerWarp], exhi[kChunksPerWarp];
+            int ex[kHalves * kCh], exlo[kHalves * kCh], exhi[kHalves * kCh];
 #pragma unroll
-            for (int c = 0; c < kChunksPerWarp; ++c)
-                ex[c] = colt + 32 * c + lane < n ? __ldg(er + colt + 32 * c + lane) : 0;
+            for (int x = 0; x < kHalves * kCh; ++x) {
+                const int64_t col = tn * kPairTile + (x / kCh) * kN + cbeg + 32 * (x % kCh) + lane;
+                ex[x] = col < n ? __ldg(er + col) : 0;
+            }
 #pragma unroll
-            for (int c = 0; c < kChunksPerWarp; ++c) {
-                exlo[c] = __reduce_min_sync(0xffffffffu, ex[c]);
-                exhi[c] = __reduce_max_sync(0xffffffffu, ex[c]);
+            for (int x = 0; x < kHalves * kCh; ++x) {
+                exlo[x] = __reduce_min_sync(0xffffffffu, ex[x]);
+                exhi[x] = __reduce_max_sync(0xffffffffu, ex[x]);
             }
             for (int u = 0; ok && u < units.n; ++u) {
                 const int t = units.t[u];
@@ -873,81 +917,83 @@ __global__ void __launch_bounds__(kPairThreads, 1)
                 const int64_t ck =
                     (fl & kUnitMerged) ? nkb : chunk_kblocks(min(s, t - 1) - max(1, t - s) + 1);
                 const int kb = 2 - 5 * t + erow;
+                // 2^(kb + e_col) as an FP64 exponent bias: the row's part plus e_col << 20
+                const uint32_t rbias = pow2_ebias(kb);
                 for (int64_t cb = 0; ok && cb < nkb; cb += ck) {
                     const bool first = (u == 0 && cb == 0) && !accum;
                     const uint64_t pol = (u == units.n - 1 && cb + ck >= nkb) ? pol_first : pol_last;
-                    if (!pwait(&bars.tfull, (uint32_t)(unit & 1), 4, warp, (int)unit)) { ok = false; break; }
-                    tc_fence_after();
-                    // the previous unit's copies are complete: successive updates stay in order
-                    if (lane < kStageCols) bulk_wait_all();
-                    const uint32_t tbase = tmem_base + ((uint32_t)(q * 32) << 16);
-                    int rd = 0;
 #pragma unroll 1
-                    for (int c0 = cbeg; c0 < cbeg + kColsPerWarp; c0 += 32) {
-                        const int64_t colb = colt + (c0 - cbeg);
-                        const bool fast = __all_sync(0xffffffffu, pow2_ok(kb + exlo[0]) && pow2_ok(kb + exhi[0]));
-                        // 2^(kb + e_col) as an FP64 exponent bias: the row's part plus e_col << 20
-                        const uint32_t rbias = pow2_ebias(kb);
+                    for (int h = 0; h < kHalves; ++h) {
+                        if (!pwait(&bars.tfull[h], (uint32_t)(unit & 1), 4, warp, (int)unit)) { ok = false; break; }
+                        tc_fence_after();
+                        // the previous half's copies are complete: successive updates stay in order
+                        if (lane < kStageCols) bulk_wait_all();
+                        const uint32_t tbase = tmem_base + ((uint32_t)(q * 32) << 16) + h * Shape::kBufCols;
+#pragma unroll 1
+                        for (int c = 0; c < kCh; ++c) {
+                            const int64_t colb = tn * kPairTile + h * kN + cbeg + 32 * c;
+                            const bool fast = __all_sync(0xffffffffu, pow2_ok(kb + exlo[0]) && pow2_ok(kb + exhi[0]));
 #pragma unroll
-                        for (int hh = 0; hh < 32; hh += kLdCols) {
-                            uint32_t vre[kLdCols], vim[kLdCols];
-                            tmem_ld<kLdCols>(tbase + c0 + hh, vre);
-                            tmem_ld<kLdCols>(tbase + kPairTile + c0 + hh, vim);
-                            tmem_ld_wait();
-                            if (c0 + hh + kLdCols >= cbeg + kColsPerWarp) {
-                                tc_fence_before();
-                                __syncwarp();
-                                if (lane == 0) mbar_arrive_remote(tempty_leader);
-                            }
-#pragma unroll
-                            for (int g4 = 0; g4 < kLdCols; g4 += kStageCols, ++rd) {
-                                const uint32_t buf = (uint32_t)(rd % kDrainBufs) * (kStageCols * 512);
-                                if (lane < kStageCols) bulk_wait_read<kDrainBufs - 1>();
-                                __syncwarp();
-#pragma unroll
-                                for (int cc = 0; cc < kStageCols; ++cc) {
-                                    const int c = g4 + cc;
-                                    const int ec = __shfl_sync(0xffffffffu, ex[0], hh + c);
-                                    double re, im;
-                                    if (fast) {
-                                        const uint32_t eb = rbias + ((uint32_t)ec << 20);
-                                        re = f32_pow2_to_f64_fast(vre[c], eb);
-                                        im = f32_pow2_to_f64_fast(vim[c], eb);
-                                    } else {
-                                        re = f32_pow2_to_f64_slow(vre[c], kb + ec);
-                                        im = f32_pow2_to_f64_slow(vim[c], kb + ec);
-                                    }
-                                    *reinterpret_cast<double2 *>(stg + buf + cc * 512 + lane * 16) = make_double2(re, im);
+                            for (int hh = 0; hh < 32; hh += kLdCols) {
+                                uint32_t vre[kLdCols], vim[kLdCols];
+                                tmem_ld<kLdCols>(tbase + cbeg + 32 * c + hh, vre);
+                                tmem_ld<kLdCols>(tbase + kN + cbeg + 32 * c + hh, vim);
+                                tmem_ld_wait();
+                                if (c == kCh - 1 && hh + kLdCols >= 32) {
+                                    tc_fence_before();
+                                    __syncwarp();
+                                    if (lane == 0) mbar_arrive_remote(tempty0_leader + h * 8);
                                 }
-                                fence_async_smem();
-                                __syncwarp();
-                                // lane cc issues the copy of the group's column cc (32 rows) and commits it
-                                if (lane < kStageCols) {
-                                    const int64_t col = colb + hh + g4 + lane;
-                                    const int64_t lo = lower ? max(r0, col) : r0, hi = min(r0 + 32, m);
-                                    if (col < n && lo < hi) {
-                                        const uint32_t src = stg_s + buf + lane * 512 + (uint32_t)(lo - r0) * 16;
-                                        double2 *dst = out + lo + ldo * col;
-                                        if (first) bulk_store_g(dst, src, (uint32_t)(hi - lo) * 16, pol);
-                                        else bulk_add_g(dst, src, (uint32_t)(hi - lo) * 16, pol);
+#pragma unroll
+                                for (int g4 = 0; g4 < kLdCols; g4 += kStageCols, ++rd) {
+                                    const uint32_t buf = (uint32_t)(rd % kDrainBufs) * (kStageCols * 512);
+                                    if (lane < kStageCols) bulk_wait_read<kDrainBufs - 1>();
+                                    __syncwarp();
+#pragma unroll
+                                    for (int cc = 0; cc < kStageCols; ++cc) {
+                                        const int cl = g4 + cc;
+                                        const int ec = __shfl_sync(0xffffffffu, ex[0], hh + cl);
+                                        double re, im;
+                                        if (fast) {
+                                            const uint32_t eb = rbias + ((uint32_t)ec << 20);
+                                            re = f32_pow2_to_f64_fast(vre[cl], eb);
+                                            im = f32_pow2_to_f64_fast(vim[cl], eb);
+                                        } else {
+                                            re = f32_pow2_to_f64_slow(vre[cl], kb + ec);
+                                            im = f32_pow2_to_f64_slow(vim[cl], kb + ec);
+                                        }
+                                        *reinterpret_cast<double2 *>(stg + buf + cc * 512 + lane * 16) = make_double2(re, im);
                                     }
-                                    bulk_commit();
+                                    fence_async_smem();
+                                    __syncwarp();
+                                    // lane cc issues the copy of the group's column cc (32 rows) and commits it
+                                    if (lane < kStageCols) {
+                                        const int64_t col = colb + hh + g4 + lane;
+                                        const int64_t lo = lower ? max(r0, col) : r0, hi = min(r0 + 32, m);
+                                        if (col < n && lo < hi) {
+                                            const uint32_t src = stg_s + buf + lane * 512 + (uint32_t)(lo - r0) * 16;
+                                            double2 *dst = out + lo + ldo * col;
+                                            if (first) bulk_store_g(dst, src, (uint32_t)(hi - lo) * 16, pol);
+                                            else bulk_add_g(dst, src, (uint32_t)(hi - lo) * 16, pol);
+                                        }
+                                        bulk_commit();
+                                    }
                                 }
                             }
-                        }
-                        // next chunk's exponents and range into ex[0] (a cyclic rotation: after the
-                        // unit's chunks the registers are back in order)
-                        const int xe = ex[0], xl = exlo[0], xh = exhi[0];
+                            // the next chunk's exponents into ex[0]
+                            const int xe = ex[0], xl = exlo[0], xh = exhi[0];
 #pragma unroll
-                        for (int c = 0; c + 1 < kChunksPerWarp; ++c) {
-                            ex[c] = ex[c + 1];
-                            exlo[c] = exlo[c + 1];
-                            exhi[c] = exhi[c + 1];
+                            for (int x = 0; x + 1 < kHalves * kCh; ++x) {
+                                ex[x] = ex[x + 1];
+                                exlo[x] = exlo[x + 1];
+                                exhi[x] = exhi[x + 1];
+                            }
+                            ex[kHalves * kCh - 1] = xe;
+                            exlo[kHalves * kCh - 1] = xl;
+                            exhi[kHalves * kCh - 1] = xh;
                         }
-                        ex[kChunksPerWarp - 1] = xe;
-                        exlo[kChunksPerWarp - 1] = xl;
-                        exhi[kChunksPerWarp - 1] = xh;
                     }
+                    if (!ok) break;
                     ++unit;
                 }
             }
@@ -1220,6 +1266,7 @@ struct DigitOperand {
     int32_t *expo = nullptr;
     int64_t plane_rows = 0, Kpad = 0, pitch = 0;
     CUtensorMap map;
+    CUtensorMap map64;         // 64-row boxes: the right operand of half-width pair tiles
 };
 
 int64_t env_int(const char *name, int64_t dflt) {
@@ -1240,7 +1287,8 @@ int64_t pitch_pad() {
     return p;
 }
 
-int make_map(DigitOperand &d, int s) {
+// box_rows: rows of a TMA box (kTileM; 64 for the right operand of half-width pair tiles)
+int make_map(DigitOperand &d, int s, int box_rows = kTileM, CUtensorMap *dst = nullptr) {
     PFN_encodeTiled enc = get_encode();
     if (!enc) { g_oz_err = "cuTensorMapEncodeTiled unavailable"; return HSDLA_ERR_CUDA; }
     if (d.Kpad % 128 != 0 || d.pitch % 16 != 0 || d.pitch < d.Kpad ||
@@ -1252,9 +1300,9 @@ int make_map(DigitOperand &d, int s) {
     if (rows > INT32_MAX || d.Kpad > INT32_MAX) { g_oz_err = "digit operand too large for TMA"; return HSDLA_ERR_UNSUPPORTED; }
     cuuint64_t dims[2] = {(cuuint64_t)d.Kpad, (cuuint64_t)rows};
     cuuint64_t strides[1] = {(cuuint64_t)d.pitch};
-    cuuint32_t box[2] = {(cuuint32_t)kKBlock, (cuuint32_t)kTileM};
+    cuuint32_t box[2] = {(cuuint32_t)kKBlock, (cuuint32_t)box_rows};
     cuuint32_t es[2] = {1, 1};
-    CUresult r = enc(&d.map, CU_TENSOR_MAP_DATA_TYPE_UINT8, 2, d.digits, dims, strides, box, es,
+    CUresult r = enc(dst ? dst : &d.map, CU_TENSOR_MAP_DATA_TYPE_UINT8, 2, d.digits, dims, strides, box, es,
                      CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
                      CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) { g_oz_err = "cuTensorMapEncodeTiled failed"; return HSDLA_ERR_CUDA; }
@@ -1623,6 +1671,7 @@ struct OzGroup {
     bool pair = false;          // S/H on CTA-pair tiles
     PairUnits units{};          // their accumulation units
     PairUnits units_t{};        // the T application's (structure-factor form on pair tiles)
+    int halves = 1;             // 2: structure-factor launches on half-width pair tiles
     bool sf = false;            // structure-factor form
     int tbatch = 1;             // its types per combine batch
     SfTab sft{};                // its combine table (outputs patched per run)
@@ -1657,11 +1706,12 @@ int upload_schedule(std::vector<OzJob> &jobs, OzJob *d_jobs, int4 *d_list, int64
 
 // Launch of a prepared pair-tile job table: clusters of two CTAs, one per SM, as many pairs as
 // can be resident (at most one per tile); cooperative when the lockstep slots are given.
-cudaError_t launch_pair(const CUtensorMap *maps, int s, int *d_err, const OzJob *d_jobs, int n_jobs, int64_t total,
-                        const int4 *d_list, int *d_progress, cudaStream_t st, const PairUnits &units) {
+template <int kHalves>
+cudaError_t launch_pair_t(const CUtensorMap *maps, int s, int *d_err, const OzJob *d_jobs, int n_jobs, int64_t total,
+                          const int4 *d_list, int *d_progress, cudaStream_t st, const PairUnits &units) {
     if (total <= 0) return cudaSuccess;
-    const size_t smem = (size_t)kPairStages * kStageBytes + kPairStageBytes + 1024;
-    cudaError_t e = cudaFuncSetAttribute(oz_pair_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    const size_t smem = PairShape<kHalves>::kSmem;
+    cudaError_t e = cudaFuncSetAttribute(oz_pair_kernel<kHalves>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     cudaLaunchConfig_t cfg = {};
     cudaLaunchAttribute at[2];
@@ -1678,7 +1728,7 @@ cudaError_t launch_pair(const CUtensorMap *maps, int s, int *d_err, const OzJob 
     if (max_pairs == 0) {
         cfg.gridDim = dim3(2);
         int nc = 0;
-        e = cudaOccupancyMaxActiveClusters(&nc, (const void *)oz_pair_kernel, &cfg);
+        e = cudaOccupancyMaxActiveClusters(&nc, (const void *)oz_pair_kernel<kHalves>, &cfg);
         if (e != cudaSuccess) return e;
         if (nc < 1) return cudaErrorInvalidConfiguration;
         max_pairs = nc;
@@ -1704,8 +1754,16 @@ cudaError_t launch_pair(const CUtensorMap *maps, int s, int *d_err, const OzJob 
     // lockstep epoch (stages) and how many epochs a pair may lead the slowest one
     static const int sync_every = (int)std::max<int64_t>(8, env_int("HSDLA_SYNC_EVERY", kSyncEvery));
     static const int slack = (int)std::max<int64_t>(1, env_int("HSDLA_SYNC_SLACK", 1));
-    return cudaLaunchKernelEx(&cfg, oz_pair_kernel, maps[0], maps[1], maps[2], maps[3], d_jobs, n_jobs, total, s,
-                              d_err, d_list, lockstep ? d_progress : (int *)nullptr, sync_every, slack, units);
+    return cudaLaunchKernelEx(&cfg, oz_pair_kernel<kHalves>, maps[0], maps[1], maps[2], maps[3], d_jobs, n_jobs, total,
+                              s, d_err, d_list, lockstep ? d_progress : (int *)nullptr, sync_every, slack, units);
+}
+
+// halves = 2: the half-width tiles, whose right-operand maps (maps[j.rmap] of every job) must have
+// 64-row boxes (make_map(.., kPairTile / 4)); 1: 128-row boxes.
+cudaError_t launch_pair(const CUtensorMap *maps, int s, int *d_err, const OzJob *d_jobs, int n_jobs, int64_t total,
+                        const int4 *d_list, int *d_progress, cudaStream_t st, const PairUnits &units, int halves = 1) {
+    return halves == 2 ? launch_pair_t<2>(maps, s, d_err, d_jobs, n_jobs, total, d_list, d_progress, st, units)
+                       : launch_pair_t<1>(maps, s, d_err, d_jobs, n_jobs, total, d_list, d_progress, st, units);
 }
 
 // Launch of a prepared job table (no host synchronisation; capturable).
@@ -1866,6 +1924,11 @@ static int group_prepare_sf(OzakiPlan &oz, const OzGroupDesc &d, const std::vect
     if (!rc) rc = make_map(g->dW, s);
     if (!rc) rc = make_map(g->dX, s);
     if (!rc) rc = make_map(g->dT, g->pair ? 2 * s : s);
+    // half-width pair tiles (HSDLA_PAIR_HALVES=1: full width): the right operands' 64-row maps
+    g->halves = g->pair && env_int("HSDLA_PAIR_HALVES", 2) == 2 ? 2 : 1;
+    if (!rc && g->halves == 2) rc = make_map(g->dM, 2 * s, kPairTile / 4, &g->dM.map64);
+    if (!rc && g->halves == 2) rc = make_map(g->dW, s, kPairTile / 4, &g->dW.map64);
+    if (!rc && g->halves == 2) rc = make_map(g->dX, s, kPairTile / 4, &g->dX.map64);
     if (rc) return fail(rc);
     // T application per type: Z_t = T_t M_t
     std::vector<OzJob> jt;
@@ -1888,7 +1951,8 @@ static int group_prepare_sf(OzakiPlan &oz, const OzGroupDesc &d, const std::vect
     rc = upload_schedule(jt, g->d_jobs_t, g->d_list_t, g->tiles_t, g->pair ? kPairTile : kTileN);
     g->units_t = g->pair ? pair_units(s, tkb, env_int("HSDLA_MERGE", 1) != 0) : pair_units_plain(s);
     if (rc) return fail(rc);
-    g->maps_t[0] = g->dM.map; g->maps_t[1] = g->dM.map; g->maps_t[2] = g->dM.map; g->maps_t[3] = g->dT.map;
+    g->maps_t[0] = g->halves == 2 ? g->dM.map64 : g->dM.map;    // right operand
+    g->maps_t[1] = g->dM.map; g->maps_t[2] = g->dM.map; g->maps_t[3] = g->dT.map;
     // per type: S_t = M_t^H diag(w_t) M_t and H_t = M_t^H Z_t into the products; on pair tiles
     // with merged accumulation units (HSDLA_MERGE=0: one per diagonal)
     g->units = g->pair ? pair_units(s, tkb, env_int("HSDLA_MERGE", 1) != 0) : pair_units_plain(s);
@@ -1928,7 +1992,10 @@ static int group_prepare_sf(OzakiPlan &oz, const OzGroupDesc &d, const std::vect
     }
     e = cudaMemcpy(g->d_jobs_sh, all.data(), sizeof(OzJob) * all.size(), cudaMemcpyHostToDevice);
     if (e != cudaSuccess) { g_oz_err = cudaGetErrorString(e); return fail(HSDLA_ERR_CUDA); }
-    g->maps_sh[0] = g->dM.map; g->maps_sh[1] = g->dW.map; g->maps_sh[2] = g->dX.map; g->maps_sh[3] = g->dM.map;
+    g->maps_sh[0] = g->dM.map;
+    g->maps_sh[1] = g->halves == 2 ? g->dW.map64 : g->dW.map;   // right operands
+    g->maps_sh[2] = g->halves == 2 ? g->dX.map64 : g->dX.map;
+    g->maps_sh[3] = g->dM.map;
     *out = g;
     return HSDLA_OK;
 }
@@ -2164,7 +2231,7 @@ int ozaki_group_run(OzGroup *g, const DevSystem &sys, const KTable &ktab, cudaSt
         e = slice_launch(g->tM, st);                      // M and M diag(w_t)
         if (e == cudaSuccess)
             e = g->pair ? launch_pair(g->maps_t, g->s, g->d_err, g->d_jobs_t, g->n_jobs_t, g->tiles_t, g->d_list_t,
-                                      nullptr, st, g->units_t)
+                                      nullptr, st, g->units_t, g->halves)
                         : launch_prepared(g->maps_t, g->s, g->d_err, g->d_jobs_t, g->n_jobs_t, g->tiles_t,
                                           g->d_list_t, nullptr, st);
         if (e == cudaSuccess) e = slice_launch(g->pan[0].tX, st);    // Z
@@ -2177,7 +2244,7 @@ int ozaki_group_run(OzGroup *g, const DevSystem &sys, const KTable &ktab, cudaSt
             // 34.5 -> 33.8 ms, c3 11.7 -> 11.4 ms, c4 461 -> 442 ms per k-point)
             if (e == cudaSuccess)
                 e = g->pair ? launch_pair(g->maps_sh, g->s, g->d_err, jobs, g->n_jobs_sh, g->tiles_sh, g->d_list_sh,
-                                          nullptr, st, g->units)
+                                          nullptr, st, g->units, g->halves)
                             : launch_prepared(g->maps_sh, g->s, g->d_err, jobs, g->n_jobs_sh, g->tiles_sh,
                                               g->d_list_sh, g->d_progress, st);
             if (e == cudaSuccess && nev >= 2 * g->nt) e = record(ev[2 * t + 1], st);
