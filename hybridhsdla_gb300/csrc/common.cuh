@@ -102,6 +102,7 @@ struct SfEntry {
 };
 struct SfTab {
     int nk = 0, type = 0, ntypes = 1;             // the batch: types [type, type + ntypes) in slots 0..
+    int64_t col0 = 0, col1 = INT64_MAX;           // the columns combined (of every entry)
 
     int dx = 0, dy = 0, dz = 0, ny = 0, nz = 0;   // box offsets (half widths) and extents
     int64_t box = 0;                              // entries per type
@@ -112,7 +113,8 @@ struct SfTab {
 cudaError_t launch_sf_table(const double2 *ex, const double2 *ey, const double2 *ez, const int32_t *order,
                             const int32_t *type_begin, int nt, int nx, int ny, int nz, double2 *sf, cudaStream_t st);
 // S (+)= sum_b SF_{type+b} (.) PS_b and H (+)= sum_b SF_{type+b} (.) PH_b over the lower triangles
-// of every entry, b over the batch's type slots.
+// of every entry, b over the batch's type slots, in columns [tab.col0, tab.col1) (multiples of 32
+// but for the end).
 cudaError_t launch_sf_combine(const SfTab &tab, const double2 *sf, bool first, cudaStream_t st);
 
 // Fleur's packed lower triangle (row by row) of a column-major n x n matrix (device buffers).

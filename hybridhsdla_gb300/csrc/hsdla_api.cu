@@ -18,6 +18,7 @@
 #include <cstdio>
 #include <cstring>
 #include <map>
+#include <memory>
 #include <set>
 #include <string>
 #include <tuple>
@@ -42,6 +43,9 @@ struct hsdla_context {
     void *hout = nullptr;
     int64_t hout_bytes = 0;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr, evs[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+    // host-buffer entry points: downloads overlapped with the last combine run on this stream
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t ev_copy = nullptr;
     std::set<hsdla_plan *> plans;   // live plans, destroyed with the context
     // slice autotuner results: (L, atoms, types, n_G bucket, target) -> (slices, predicted error)
     std::map<std::tuple<int, int, int, int64_t, double>, std::pair<int, double>> tune_cache;
@@ -107,6 +111,14 @@ struct hsdla_plan {
     double2 *sf_tab = nullptr;
     SfTab sf_dims{};                 // box extents and offsets (entries filled per group)
     int tbatch = 1;                  // types whose products are combined into S and H in one pass
+    // hsdla_create_hs: the host outputs the last combine of each group downloads column block by
+    // column block on the context's copy stream (structure-factor form, no graph); `done` reports it
+    struct Download {
+        std::vector<hsdla_cx *> H, S;
+        std::vector<int64_t> ld;
+        bool done = false;
+    };
+    Download *dl = nullptr;
     double est_err = 0.0;            // autotuner's predicted relative error
     int launches = 0;
 };
@@ -265,18 +277,20 @@ int validate(hsdla_context *ctx, const hsdla_system *s, const hsdla_kpoint *kpts
         for (int q = 0; q < 3; ++q)
             if (!finite_all(reinterpret_cast<const double *>(T3[q]), 2 * (int64_t)L * L))
                 return set_err(ctx, HSDLA_ERR_INPUT, "T block %d of type %d not finite", q, t);
-        // T_AA and T_BB must be Hermitian (AtomData.cpp:138-139 asserts it)
+        // T_AA and T_BB must be Hermitian (AtomData.cpp:138-139 asserts it): squared magnitudes over
+        // the lower triangle (its mirror element is the pair's other half)
         for (int q = 0; q < 3; q += 2) {
-            double mx = 0.0, dev = 0.0;
+            double mx2 = 0.0, dev2 = 0.0;
             for (int c = 0; c < L; ++c)
-                for (int r = 0; r < L; ++r) {
+                for (int r = c; r < L; ++r) {
                     const hsdla_cx a = T3[q][r + (int64_t)L * c], b = T3[q][c + (int64_t)L * r];
-                    mx = std::max(mx, std::hypot(a.re, a.im));
-                    dev = std::max(dev, std::hypot(a.re - b.re, a.im + b.im));
+                    mx2 = std::max(mx2, std::max(a.re * a.re + a.im * a.im, b.re * b.re + b.im * b.im));
+                    const double dr = a.re - b.re, di = a.im + b.im;
+                    dev2 = std::max(dev2, dr * dr + di * di);
                 }
-            if (dev > 1e-12 * std::max(mx, 1e-300))
+            if (dev2 > 1e-24 * std::max(mx2, 1e-300))
                 return set_err(ctx, HSDLA_ERR_INPUT, "T_%s of type %d is not Hermitian (|T-T^H| = %.3g)",
-                               q == 0 ? "AA" : "BB", t, dev);
+                               q == 0 ? "AA" : "BB", t, std::sqrt(dev2));
         }
     }
     if (nk < 0 || (nk > 0 && !kpts)) return set_err(ctx, HSDLA_ERR_ARG, "bad k-point list");
@@ -291,21 +305,25 @@ int validate(hsdla_context *ctx, const hsdla_system *s, const hsdla_kpoint *kpts
 
 // Hermitian full 2L x 2L block of one type from the lower triangles of T_AA/T_BB
 // (zhemm 'L' semantics, h_and_s_stripped_v2.cpp:202,345) and the full T_AB.
-void build_tfull(const hsdla_system *s, int t, int L, std::vector<std::complex<double>> &out) {
+// The Hermitian 2L x 2L block [[T_AA, T_AB], [T_AB^H, T_BB]] of type t (column-major, ld 2L) into
+// out, from the lower triangles of T_AA and T_BB and all of T_AB.
+void build_tfull(const hsdla_system *s, int t, int L, std::complex<double> *out) {
     const int64_t LL = (int64_t)L * L, n = 2 * L;
     const auto *aa = reinterpret_cast<const std::complex<double> *>(s->type_t_aa) + t * LL;
     const auto *ab = reinterpret_cast<const std::complex<double> *>(s->type_t_ab) + t * LL;
     const auto *bb = reinterpret_cast<const std::complex<double> *>(s->type_t_bb) + t * LL;
-    out.assign((size_t)n * n, 0.0);
-    for (int c = 0; c < n; ++c)
-        for (int r = 0; r < n; ++r) {
-            std::complex<double> v;
-            if (r < L && c < L) v = (r >= c) ? aa[r + L * c] : std::conj(aa[c + L * r]);
-            else if (r < L) v = ab[r + L * (c - L)];
-            else if (c < L) v = std::conj(ab[c + L * (r - L)]);
-            else v = (r >= c) ? bb[(r - L) + L * (c - L)] : std::conj(bb[(c - L) + L * (r - L)]);
-            out[r + (size_t)n * c] = v;
+    for (int c = 0; c < n; ++c) {
+        std::complex<double> *o = out + (size_t)n * c;
+        if (c < L) {
+            for (int r = 0; r < c; ++r) o[r] = std::conj(aa[c + L * r]);
+            for (int r = c; r < L; ++r) o[r] = aa[r + L * c];
+            for (int r = L; r < n; ++r) o[r] = std::conj(ab[c + L * (r - L)]);
+        } else {
+            for (int r = 0; r < L; ++r) o[r] = ab[r + L * (c - L)];
+            for (int r = L; r < c; ++r) o[r] = std::conj(bb[(c - L) + L * (r - L)]);
+            for (int r = c; r < n; ++r) o[r] = bb[(r - L) + L * (c - L)];
         }
+    }
 }
 
 template <typename T>
@@ -483,6 +501,8 @@ int hsdla_context_create(int device, hsdla_context **out) {
     }
     cudaEventCreate(&ctx->ev0);
     cudaEventCreate(&ctx->ev1);
+    cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking);
+    cudaEventCreateWithFlags(&ctx->ev_copy, cudaEventDisableTiming);
     for (auto &e : ctx->evs) cudaEventCreate(&e);
     *out = ctx;
     return HSDLA_OK;
@@ -496,6 +516,8 @@ void hsdla_context_destroy(hsdla_context *ctx) {
     if (ctx->ws) ctx_free(ctx, ctx->ws, ctx->ws_bytes);
     if (ctx->hout) ctx_free(ctx, ctx->hout, ctx->hout_bytes);
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
+    if (ctx->ev_copy) cudaEventDestroy(ctx->ev_copy);
+    if (ctx->copy_stream) cudaStreamDestroy(ctx->copy_stream);
     if (ctx->ev1) cudaEventDestroy(ctx->ev1);
     for (auto &e : ctx->evs) if (e) cudaEventDestroy(e);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
@@ -591,11 +613,7 @@ int hsdla_plan_create(hsdla_context *ctx, const hsdla_system *s, const hsdla_kpo
                 w[rB] = un; wsq[rB] = std::sqrt(un);
             }
     }
-    std::vector<std::complex<double>> tf_all((size_t)nt * 4 * L * L), tf;
-    for (int t = 0; t < nt; ++t) {
-        build_tfull(s, t, L, tf);
-        std::copy(tf.begin(), tf.end(), tf_all.begin() + (size_t)t * 4 * L * L);
-    }
+    const size_t tf_elems = (size_t)nt * 4 * L * L;
 
     // ---- one device block for all tables
     int64_t bytes = 0;
@@ -604,7 +622,7 @@ int hsdla_plan_create(hsdla_context *ctx, const hsdla_system *s, const hsdla_kpo
     add(sizeof(double) * nt); add(sizeof(int32_t) * nt);
     for (int q = 0; q < 5; ++q) add(sizeof(double) * nt * nl);
     add(sizeof(double) * L);
-    add(sizeof(double2) * tf_all.size());
+    add(sizeof(double2) * tf_elems);
     add(sizeof(double) * pl->twoLa); add(sizeof(double) * pl->twoLa);
     for (int i = 0; i < nk; ++i) add(sizeof(int32_t) * 3 * kpts[i].n_g);
     // structure-factor form: per-type weights, per-atom phase factors along each axis, the atoms
@@ -627,8 +645,9 @@ int hsdla_plan_create(hsdla_context *ctx, const hsdla_system *s, const hsdla_kpo
     rc = ctx_malloc(ctx, &pl->tables, bytes);
     if (rc) { delete pl; return rc; }
     pl->tables_bytes = bytes;
-    std::vector<char> host(upload_bytes, 0);
-    char *hp = host.data();
+    // staging of the uploaded part (left uninitialised: every byte that matters is written)
+    std::unique_ptr<char[]> host(new char[std::max<int64_t>(upload_bytes, 1)]);
+    char *hp = host.get();
     char *dp = reinterpret_cast<char *>(pl->tables);
     auto put = [&](const void *src, int64_t b) -> void * {
         void *d = dp;
@@ -652,7 +671,9 @@ int hsdla_plan_create(hsdla_context *ctx, const hsdla_system *s, const hsdla_kpo
     D.dE_u_dr = (const double *)put(s->type_dE_u_dr, sizeof(double) * nt * nl);
     D.inv_w = (const double *)put(inv_w.data(), sizeof(double) * nt * nl);
     D.ynorm = (const double *)put(yn.data(), sizeof(double) * L);
-    pl->Tfull = (double2 *)put(tf_all.data(), sizeof(double2) * tf_all.size());
+    for (int t = 0; t < nt; ++t)
+        build_tfull(s, t, L, reinterpret_cast<std::complex<double> *>(hp) + (size_t)t * 4 * L * L);
+    pl->Tfull = (double2 *)put(nullptr, sizeof(double2) * tf_elems);
     pl->w = (double *)put(w.data(), sizeof(double) * pl->twoLa);
     pl->wsqrt = (double *)put(wsq.data(), sizeof(double) * pl->twoLa);
     for (int i = 0; i < nk; ++i) {
@@ -701,7 +722,7 @@ int hsdla_plan_create(hsdla_context *ctx, const hsdla_system *s, const hsdla_kpo
         dm.ny = ext[1]; dm.nz = ext[2];
         dm.box = (int64_t)ext[0] * ext[1] * ext[2];
     }
-    cudaError_t e = cudaMemcpyAsync(pl->tables, host.data(), upload_bytes, cudaMemcpyHostToDevice, ctx->stream);
+    cudaError_t e = cudaMemcpyAsync(pl->tables, host.get(), upload_bytes, cudaMemcpyHostToDevice, ctx->stream);
     if (e == cudaSuccess && pl->sf)
         e = launch_sf_table(d_ex, d_ex + (size_t)na * ext[0], d_ex + (size_t)na * (ext[0] + ext[1]), d_order,
                             d_order + na, nt, ext[0], ext[1], ext[2], pl->sf_tab, ctx->stream);
@@ -1066,11 +1087,60 @@ void run_groups_flop(const hsdla_plan *pl, double *dom_flop) {
     for (const auto &g : pl->groups) run_groups_flop_one(pl, g, dom_flop);
 }
 
+// The last combine batch of a group [t0, t0 + ntypes).  With a host download pending (and no graph
+// capture) it runs in column blocks of kDownBlock, and after each block the copy stream downloads
+// that block of every k-point's H and S lower triangle while the next block is combined.
+int combine_last(hsdla_plan *pl, hsdla_plan::Group &g, int t0, int ntypes, cudaStream_t st, bool capturing) {
+    hsdla_context *ctx = pl->ctx;
+    SfTab tab = g.sft;
+    tab.type = t0;
+    tab.ntypes = ntypes;
+    if (!pl->dl || capturing) {
+        CUDA_TRY(ctx, launch_sf_combine(tab, pl->sf_tab, t0 == 0, st));
+        pl->launches++;
+        return HSDLA_OK;
+    }
+    int64_t gmax = 0;
+    for (int q = 0; q < g.ktab.nk; ++q) gmax = std::max(gmax, pl->kps[g.kidx[q]].n_g);
+    for (int64_t c0 = 0; c0 < gmax; c0 += kDownBlock) {
+        tab.col0 = c0;
+        tab.col1 = c0 + kDownBlock;
+        CUDA_TRY(ctx, launch_sf_combine(tab, pl->sf_tab, t0 == 0, st));
+        pl->launches++;
+        CUDA_TRY(ctx, cudaEventRecord(ctx->ev_copy, st));
+        CUDA_TRY(ctx, cudaStreamWaitEvent(ctx->copy_stream, ctx->ev_copy, 0));
+        for (int q = 0; q < g.ktab.nk; ++q) {
+            const int i = g.kidx[q];
+            const int64_t n = pl->kps[i].n_g;
+            if (c0 >= n) continue;
+            const int64_t w = std::min(kDownBlock, n - c0);
+            const SfEntry &E = g.sft.e[q];
+            const hsdla_cx *dS = reinterpret_cast<const hsdla_cx *>(E.S), *dH = reinterpret_cast<const hsdla_cx *>(E.H);
+            for (int m = 0; m < 2; ++m) {
+                hsdla_cx *host = m == 0 ? pl->dl->H[i] : pl->dl->S[i];
+                const hsdla_cx *dev = m == 0 ? dH : dS;
+                const int64_t ld = pl->dl->ld[i];
+                CUDA_TRY(ctx, cudaMemcpy2DAsync(host + c0 + ld * c0, ld * sizeof(hsdla_cx), dev + c0 + E.ldo * c0,
+                                                E.ldo * sizeof(hsdla_cx), (n - c0) * sizeof(hsdla_cx), w,
+                                                cudaMemcpyDeviceToHost, ctx->copy_stream));
+            }
+        }
+    }
+    pl->dl->done = true;
+    return HSDLA_OK;
+}
+
 // Enqueue every group's launches (no host synchronisation: capturable in a CUDA graph).
 int run_groups(hsdla_plan *pl, cudaStream_t st, bool timed, float *ms_ab, float *ms_dom, double *dom_flop) {
     hsdla_context *ctx = pl->ctx;
     pl->launches = 0;
     if (dom_flop) *dom_flop = 0.0;
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    CUDA_TRY(ctx, cudaStreamIsCapturing(st, &cap));
+    const bool capturing = cap != cudaStreamCaptureStatusNone;
+    // the structure-factor form's last combine batch of a group runs here (with the download)
+    const bool defer = pl->sf && pl->dl && !capturing;
+    const int last_t0 = (pl->nt - 1) / std::max(pl->tbatch, 1) * std::max(pl->tbatch, 1);
     for (auto &g : pl->groups) {
         if (timed) CUDA_TRY(ctx, cudaEventRecord(ctx->evs[0], st));
         if (!pl->external) {
@@ -1085,9 +1155,14 @@ int run_groups(hsdla_plan *pl, cudaStream_t st, bool timed, float *ms_ab, float 
         }
         if (g.oz) {
             int nl = 0;
-            const int rc = ozaki_group_run(g.oz, pl->dsys, g.ktab, st, g.ev_dom.data(), (int)g.ev_dom.size(), &nl);
+            const int rc =
+                ozaki_group_run(g.oz, pl->dsys, g.ktab, st, g.ev_dom.data(), (int)g.ev_dom.size(), &nl, defer);
             if (rc) return set_err(ctx, rc, "Ozaki group failed: %s", ozaki_last_error());
             pl->launches += nl;
+            if (defer) {
+                const int rcc = combine_last(pl, g, last_t0, pl->nt - last_t0, st, capturing);
+                if (rcc) return rcc;
+            }
         } else if (pl->sf) {
             CUDA_TRY(ctx, launch_fp64_jobs(g.d_jobs_t, g.n_jobs_t, g.tiles_t, st));
             pl->launches++;
@@ -1100,6 +1175,11 @@ int run_groups(hsdla_plan *pl, cudaStream_t st, bool timed, float *ms_ab, float 
                 // the batch's last type: its products into S and H
                 if ((t + 1) % pl->tbatch == 0 || t + 1 == pl->nt) {
                     const int t0 = t / pl->tbatch * pl->tbatch;
+                    if (t0 == last_t0) {
+                        const int rcc = combine_last(pl, g, t0, t + 1 - t0, st, capturing);
+                        if (rcc) return rcc;
+                        continue;
+                    }
                     g.sft.type = t0;
                     g.sft.ntypes = t + 1 - t0;
                     CUDA_TRY(ctx, launch_sf_combine(g.sft, pl->sf_tab, t0 == 0, st));
@@ -1460,14 +1540,35 @@ int hsdla_create_hs(hsdla_context *ctx, const hsdla_system *s, const hsdla_kpoin
         dS[i] = p; p += ng[i] * ng[i];
         dld[i] = std::max<int64_t>(ng[i], 1);
     }
-    // zero device outputs: the diagonal blocks of the download carry their upper triangles
-    cudaError_t e = cudaMemsetAsync(dout, 0, out_elems * sizeof(double2), ctx->stream);
+    // zero the diagonal blocks of the device outputs: the download of a column block starts at its
+    // first row, so it carries the block's upper triangle, which nothing else writes
+    cudaError_t e = cudaSuccess;
+    for (int i = 0; e == cudaSuccess && i < nk; ++i)
+        for (int m = 0; m < 2 && e == cudaSuccess; ++m)
+            for (int64_t c0 = 0; c0 < ng[i] && e == cudaSuccess; c0 += kDownBlock) {
+                const int64_t w = std::min(kDownBlock, ng[i] - c0);
+                hsdla_cx *d = (m == 0 ? dH[i] : dS[i]) + c0 + ng[i] * c0;
+                e = cudaMemset2DAsync(d, ng[i] * sizeof(hsdla_cx), 0, w * sizeof(hsdla_cx), w, ctx->stream);
+            }
+    // structure-factor form: the last combine downloads each column block as soon as it is done
+    hsdla_plan::Download dl;
+    dl.H.assign(H, H + nk);
+    dl.S.assign(S, S + nk);
+    dl.ld.assign(ld, ld + nk);
     if (e == cudaSuccess) {
+        pl->dl = &dl;
         rc = hsdla_plan_execute(pl, dH.data(), dS.data(), dld.data(), ctx->stream, rep);
+        pl->dl = nullptr;
     } else {
         rc = set_err(ctx, HSDLA_ERR_CUDA, "memset failed: %s", cudaGetErrorString(e));
     }
-    for (int i = 0; rc == HSDLA_OK && i < nk; ++i) {
+    if (rc == HSDLA_OK && dl.done) {
+        // the end-to-end event waits for the copy stream's downloads
+        e = cudaEventRecord(ctx->ev_copy, ctx->copy_stream);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(ctx->stream, ctx->ev_copy, 0);
+        if (e != cudaSuccess) rc = set_err(ctx, HSDLA_ERR_CUDA, "D2H copy failed: %s", cudaGetErrorString(e));
+    }
+    for (int i = 0; rc == HSDLA_OK && !dl.done && i < nk; ++i) {
         if (ng[i] == 0) continue;
         e = download_lower(H[i], ld[i], dH[i], ng[i], ctx->stream);
         if (e == cudaSuccess) e = download_lower(S[i], ld[i], dS[i], ng[i], ctx->stream);

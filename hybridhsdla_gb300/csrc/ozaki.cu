@@ -2223,7 +2223,7 @@ static cudaError_t record(cudaEvent_t ev, cudaStream_t st) {
 // panel).  With several panels the events span the panels' S/H launches and the slicing between
 // them.
 int ozaki_group_run(OzGroup *g, const DevSystem &sys, const KTable &ktab, cudaStream_t st, const cudaEvent_t *ev,
-                    int nev, int *launches) {
+                    int nev, int *launches, bool defer_last_combine) {
     const cudaEvent_t ev0 = nev >= 2 ? ev[0] : nullptr, ev1 = nev >= 2 ? ev[nev - 1] : nullptr;
     int nl = 0;
     cudaError_t e = cudaSuccess;
@@ -2249,8 +2249,10 @@ int ozaki_group_run(OzGroup *g, const DevSystem &sys, const KTable &ktab, cudaSt
                                               g->d_list_sh, g->d_progress, st);
             if (e == cudaSuccess && nev >= 2 * g->nt) e = record(ev[2 * t + 1], st);
             nl += 1;
-            // the batch's last type: its products into S and H
-            if (e == cudaSuccess && ((t + 1) % g->tbatch == 0 || t + 1 == g->nt)) {
+            // the batch's last type: its products into S and H (the caller combines the group's last
+            // batch when it defers it)
+            if (e == cudaSuccess && ((t + 1) % g->tbatch == 0 || t + 1 == g->nt) &&
+                !(defer_last_combine && t + 1 == g->nt)) {
                 const int t0 = t / g->tbatch * g->tbatch;
                 g->sft.type = t0;
                 g->sft.ntypes = t + 1 - t0;

@@ -75,9 +75,10 @@ void ozaki_group_set_outputs(OzGroup *g, double2 *const *S, double2 *const *H, c
 void ozaki_group_set_sf(OzGroup *g, const SfTab &t);
 // Enqueues the group's launches (slices, T application, phases, S/H products); no host sync.
 // ev: event pairs recorded around the S/H product launches (one pair, or one per type in the
-// structure-factor form; nev events, may be 0).
+// structure-factor form; nev events, may be 0).  defer_last_combine: the structure-factor form's
+// last combine batch is left to the caller.
 int ozaki_group_run(OzGroup *g, const DevSystem &sys, const KTable &ktab, cudaStream_t st, const cudaEvent_t *ev,
-                    int nev, int *launches);
+                    int nev, int *launches, bool defer_last_combine = false);
 void ozaki_group_destroy(OzGroup *g);
 
 int ozaki_plan_init(OzakiPlan &oz, int num_slices, double target);

@@ -47,7 +47,9 @@ constexpr int kSfTile = 32, kSfRows = 8;
 
 // out (+)= sum over the batch's types t of SF_t(g_col - g_row) * P_t over the lower triangle of
 // every entry (S and H together), one CTA per 32 x 32 tile; consecutive threads take consecutive
-// rows of a column.  A batch of several types reads and writes S and H once.
+// rows of a column.  A batch of several types reads and writes S and H once.  The tiles of an
+// entry are its tile columns [tc0, tc1) (a column range of the launch), each from the diagonal
+// tile down.
 __global__ void __launch_bounds__(kSfTile * kSfRows) sf_combine_kernel(const __grid_constant__ SfTab tab,
                                                                        const double2 *__restrict__ sf, int first) {
     const int64_t tile = blockIdx.x;
@@ -55,10 +57,17 @@ __global__ void __launch_bounds__(kSfTile * kSfRows) sf_combine_kernel(const __g
     while (k + 1 < tab.nk && tab.e[k + 1].tile_begin <= tile) ++k;
     const SfEntry &E = tab.e[k];
     const int64_t b = tile - E.tile_begin;
-    int64_t tr = (int64_t)((sqrt(8.0 * (double)b + 1.0) - 1.0) * 0.5);
-    while (tr * (tr + 1) / 2 > b) --tr;
-    while ((tr + 1) * (tr + 2) / 2 <= b) ++tr;
-    const int64_t tc = b - tr * (tr + 1) / 2;
+    // tile column tc: the last one whose first tile is at or before b (tiles before tile column
+    // c: sum_{c'=tc0}^{c-1} (T - c'))
+    const int64_t T = (E.n + kSfTile - 1) / kSfTile, tc0 = tab.col0 / kSfTile;
+    auto before = [&](int64_t c) { return (c - tc0) * T - (c * (c - 1) - tc0 * (tc0 - 1)) / 2; };
+    int64_t lo = tc0, hi = (min(E.n, tab.col1) + kSfTile - 1) / kSfTile - 1;
+    while (lo < hi) {
+        const int64_t mid = (lo + hi + 1) / 2;
+        if (before(mid) <= b) lo = mid;
+        else hi = mid - 1;
+    }
+    const int64_t tc = lo, tr = tc + (b - before(tc));
     const int64_t row = tr * kSfTile + threadIdx.x;
     if (row >= E.n) return;
     const int32_t *gr = E.g + 3 * row;
@@ -105,10 +114,13 @@ cudaError_t launch_sf_table(const double2 *ex, const double2 *ey, const double2 
 
 int64_t sf_tab_tiles(SfTab &tab) {
     int64_t total = 0;
+    const int64_t tc0 = tab.col0 / kSfTile;
     for (int k = 0; k < tab.nk; ++k) {
         const int64_t T = (tab.e[k].n + kSfTile - 1) / kSfTile;
+        const int64_t tc1 = (std::min(tab.e[k].n, tab.col1) + kSfTile - 1) / kSfTile;   // (col1 may be INT64_MAX)
         tab.e[k].tile_begin = total;
-        total += T * (T + 1) / 2;
+        // tile columns [tc0, tc1), T - c tiles each
+        if (tc1 > tc0) total += (tc1 - tc0) * T - (tc1 * (tc1 - 1) - tc0 * (tc0 - 1)) / 2;
     }
     return total;
 }
