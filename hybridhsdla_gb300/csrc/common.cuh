@@ -101,7 +101,8 @@ struct SfEntry {
     int64_t tile_begin = 0;
 };
 struct SfTab {
-    int nk = 0, type = 0, ntypes = 1;             // the batch: types [type, type + ntypes) in slots 0..
+    int nk = 0, type = 0, ntypes = 1;             // the batch: types [type, type + ntypes) in slots
+    int slot0 = 0;                                // slot0, slot0 + 1, ...
     int64_t col0 = 0, col1 = INT64_MAX;           // the columns combined (of every entry)
 
     int dx = 0, dy = 0, dz = 0, ny = 0, nz = 0;   // box offsets (half widths) and extents

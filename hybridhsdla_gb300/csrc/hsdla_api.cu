@@ -46,6 +46,12 @@ struct hsdla_context {
     // host-buffer entry points: downloads overlapped with the last combine run on this stream
     cudaStream_t copy_stream = nullptr;
     cudaEvent_t ev_copy = nullptr;
+    // device blocks of at most kCacheBlockMax released by plans, kept for the next plan (a plan's
+    // tables and job lists come and go with every hsdla_create_hs): size -> pointer, and the live
+    // blocks' sizes
+    std::multimap<int64_t, void *> cache;
+    std::map<void *, int64_t> live;
+    int64_t cached_bytes = 0;
     std::set<hsdla_plan *> plans;   // live plans, destroyed with the context
     // slice autotuner results: (L, atoms, types, n_G bucket, target) -> (slices, predicted error)
     std::map<std::tuple<int, int, int, int64_t, double>, std::pair<int, double>> tune_cache;
@@ -144,26 +150,72 @@ int set_err(hsdla_context *ctx, int code, const char *fmt, ...) {
             return set_err((ctx), HSDLA_ERR_CUDA, "%s failed: %s", #call, cudaGetErrorString(e_));    \
     } while (0)
 
+constexpr int64_t kCacheBlockMax = (int64_t)256 << 20;    // larger blocks are freed, not kept
+constexpr int64_t kCacheBytesMax = (int64_t)1 << 30;       // at most this much kept
+
+// Returns every kept block to the driver.
+void ctx_cache_release(hsdla_context *ctx) {
+    if (ctx->cache.empty()) return;
+    cudaDeviceSynchronize();
+    for (auto &b : ctx->cache) cudaFree(b.second);
+    ctx->mem_used -= ctx->cached_bytes;
+    ctx->cache.clear();
+    ctx->cached_bytes = 0;
+}
+
+// Device allocations of the context.  Blocks up to kCacheBlockMax are served from the blocks
+// earlier plans released when one of at most twice the size is kept; the memory cap counts kept
+// blocks as used (they are released first when a request would exceed it).
 int ctx_malloc(hsdla_context *ctx, void **p, int64_t bytes) {
     *p = nullptr;
     if (bytes <= 0) return HSDLA_OK;
+    // a cap below what the context holds: kept blocks go first, and every request is checked
+    if (ctx->mem_cap > 0 && ctx->mem_used > ctx->mem_cap) ctx_cache_release(ctx);
+    if (bytes <= kCacheBlockMax && (ctx->mem_cap == 0 || ctx->mem_used <= ctx->mem_cap)) {
+        auto it = ctx->cache.lower_bound(bytes);
+        if (it != ctx->cache.end() && it->first <= 2 * bytes) {
+            *p = it->second;
+            ctx->live[*p] = it->first;
+            ctx->cached_bytes -= it->first;
+            ctx->cache.erase(it);
+            return HSDLA_OK;
+        }
+    }
+    if (ctx->mem_cap > 0 && ctx->mem_used + bytes > ctx->mem_cap) ctx_cache_release(ctx);
     if (ctx->mem_cap > 0 && ctx->mem_used + bytes > ctx->mem_cap)
         return set_err(ctx, HSDLA_ERR_NOMEM, "device allocation of %lld bytes exceeds the cap (%lld used of %lld)",
                        (long long)bytes, (long long)ctx->mem_used, (long long)ctx->mem_cap);
     cudaError_t e = cudaMalloc(p, (size_t)bytes);
+    if (e != cudaSuccess && !ctx->cache.empty()) {
+        cudaGetLastError();
+        ctx_cache_release(ctx);
+        e = cudaMalloc(p, (size_t)bytes);
+    }
     if (e != cudaSuccess) {
         cudaGetLastError();
         *p = nullptr;
         return set_err(ctx, HSDLA_ERR_NOMEM, "cudaMalloc(%lld) failed: %s", (long long)bytes, cudaGetErrorString(e));
     }
     ctx->mem_used += bytes;
+    ctx->live[*p] = bytes;
     return HSDLA_OK;
 }
 
+// Releases a block of ctx_malloc.  Callers release only blocks no queued work still uses (they
+// synchronise first where it could); a kept block is handed out again in stream order only after
+// that.
 void ctx_free(hsdla_context *ctx, void *p, int64_t bytes) {
     if (!p) return;
+    auto it = ctx->live.find(p);
+    const int64_t size = it != ctx->live.end() ? it->second : bytes;
+    if (it != ctx->live.end()) ctx->live.erase(it);
+    if (size <= kCacheBlockMax && ctx->cached_bytes + size <= kCacheBytesMax) {
+        ctx->cache.emplace(size, p);
+        ctx->cached_bytes += size;
+        return;
+    }
     cudaFree(p);
-    ctx->mem_used -= bytes;
+    ctx->mem_used -= size;
 }
 
 // Workspace of at least `bytes`, owned by the context (reused across calls).
@@ -515,6 +567,7 @@ void hsdla_context_destroy(hsdla_context *ctx) {
     while (!ctx->plans.empty()) hsdla_plan_destroy(*ctx->plans.begin());
     if (ctx->ws) ctx_free(ctx, ctx->ws, ctx->ws_bytes);
     if (ctx->hout) ctx_free(ctx, ctx->hout, ctx->hout_bytes);
+    ctx_cache_release(ctx);
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
     if (ctx->ev_copy) cudaEventDestroy(ctx->ev_copy);
     if (ctx->copy_stream) cudaStreamDestroy(ctx->copy_stream);
@@ -1095,6 +1148,7 @@ int combine_last(hsdla_plan *pl, hsdla_plan::Group &g, int t0, int ntypes, cudaS
     SfTab tab = g.sft;
     tab.type = t0;
     tab.ntypes = ntypes;
+    tab.slot0 = t0 % std::max(pl->tbatch, 1);
     if (!pl->dl || capturing) {
         CUDA_TRY(ctx, launch_sf_combine(tab, pl->sf_tab, t0 == 0, st));
         pl->launches++;
@@ -1160,7 +1214,8 @@ int run_groups(hsdla_plan *pl, cudaStream_t st, bool timed, float *ms_ab, float 
             if (rc) return set_err(ctx, rc, "Ozaki group failed: %s", ozaki_last_error());
             pl->launches += nl;
             if (defer) {
-                const int rcc = combine_last(pl, g, last_t0, pl->nt - last_t0, st, capturing);
+                const int t0 = ozaki_group_last_combine(g.oz);
+                const int rcc = combine_last(pl, g, t0, pl->nt - t0, st, capturing);
                 if (rcc) return rcc;
             }
         } else if (pl->sf) {
@@ -1227,7 +1282,8 @@ void hsdla_plan_destroy(hsdla_plan *pl) {
     if (!pl) return;
     hsdla_context *ctx = pl->ctx;
     cudaSetDevice(ctx->device);
-    cudaStreamSynchronize(ctx->stream);
+    // all of the plan's work done (on any stream) before its blocks can be handed out again
+    cudaDeviceSynchronize();
     release_groups(pl);
     if (pl->d_jobs) ctx_free(ctx, pl->d_jobs, pl->jobs_cap * sizeof(Fp64Job));
     if (pl->tables) ctx_free(ctx, pl->tables, pl->tables_bytes);

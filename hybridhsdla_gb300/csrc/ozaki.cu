@@ -1674,6 +1674,11 @@ struct OzGroup {
     int halves = 1;             // 2: structure-factor launches on half-width pair tiles
     bool sf = false;            // structure-factor form
     int tbatch = 1;             // its types per combine batch
+    // with one batch: the first side_types types are combined on a side stream while the S/H
+    // launches of the others run (the combine is FP64-bound, the products tensor-bound)
+    int side_types = 0;
+    cudaStream_t side = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     SfTab sft{};                // its combine table (outputs patched per run)
     const double2 *sf_tab = nullptr;
 };
@@ -1862,6 +1867,19 @@ static int group_prepare_sf(OzakiPlan &oz, const OzGroupDesc &d, const std::vect
     g->d_err = oz.d_error;
     g->sf_tab = d.sf_tab;
     g->tbatch = std::max(1, d.tbatch);
+    // HSDLA_COMBINE_OVERLAP=1: the first half of the combine on a side stream, next to the S/H
+    // launches of the other types.  Off by default: on the 8000-column workload the co-running
+    // combine slowed the S/H launches by more than it saved (31.7 against 31.4 ms per k-point).
+    if (g->tbatch >= d.nt && d.nt >= 2 && env_int("HSDLA_COMBINE_OVERLAP", 0) != 0) {
+        g->side_types = (int)(d.nt / 2);
+        if (cudaStreamCreateWithFlags(&g->side, cudaStreamNonBlocking) != cudaSuccess ||
+            cudaEventCreateWithFlags(&g->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+            cudaEventCreateWithFlags(&g->ev_join, cudaEventDisableTiming) != cudaSuccess) {
+            g_oz_err = "side stream creation failed";
+            ozaki_group_destroy(g);
+            return HSDLA_ERR_CUDA;
+        }
+    }
     std::vector<int64_t> G;
     for (auto &k : kb) G.push_back(k.G);
     g->rows = group_rows(G);
@@ -2196,6 +2214,10 @@ int ozaki_group_prepare(OzakiPlan &oz, const OzGroupDesc &d, const std::vector<O
 }
 
 void ozaki_group_set_sf(OzGroup *g, const SfTab &t) { g->sft = t; }
+int ozaki_group_last_combine(const OzGroup *g) {
+    if (g->side_types > 0) return g->side_types;
+    return (g->nt - 1) / g->tbatch * g->tbatch;
+}
 
 void ozaki_group_set_outputs(OzGroup *g, double2 *const *S, double2 *const *H, const int64_t *ld) {
     for (int pi = 0; pi < g->panels; ++pi) {
@@ -2249,6 +2271,35 @@ int ozaki_group_run(OzGroup *g, const DevSystem &sys, const KTable &ktab, cudaSt
                                               g->d_list_sh, g->d_progress, st);
             if (e == cudaSuccess && nev >= 2 * g->nt) e = record(ev[2 * t + 1], st);
             nl += 1;
+            if (g->side_types > 0) {
+                // the first side_types types' products into S and H on the side stream, then the
+                // rest (the caller's when it defers the last combine)
+                if (e == cudaSuccess && t + 1 == g->side_types) {
+                    SfTab tab = g->sft;
+                    tab.type = 0;
+                    tab.ntypes = g->side_types;
+                    tab.slot0 = 0;
+                    // plain records: under graph capture they fork the side stream into the graph
+                    // and join it back
+                    e = cudaEventRecord(g->ev_fork, st);
+                    if (e == cudaSuccess) e = cudaStreamWaitEvent(g->side, g->ev_fork, 0);
+                    if (e == cudaSuccess) e = launch_sf_combine(tab, g->sf_tab, true, g->side);
+                    if (e == cudaSuccess) e = cudaEventRecord(g->ev_join, g->side);
+                    nl += 1;
+                }
+                if (e == cudaSuccess && t + 1 == g->nt) {
+                    e = cudaStreamWaitEvent(st, g->ev_join, 0);
+                    if (e == cudaSuccess && !defer_last_combine) {
+                        SfTab tab = g->sft;
+                        tab.type = g->side_types;
+                        tab.ntypes = g->nt - g->side_types;
+                        tab.slot0 = g->side_types;
+                        e = launch_sf_combine(tab, g->sf_tab, false, st);
+                        nl += 1;
+                    }
+                }
+                continue;
+            }
             // the batch's last type: its products into S and H (the caller combines the group's last
             // batch when it defers it)
             if (e == cudaSuccess && ((t + 1) % g->tbatch == 0 || t + 1 == g->nt) &&
@@ -2310,6 +2361,9 @@ int ozaki_group_run(OzGroup *g, const DevSystem &sys, const KTable &ktab, cudaSt
 void ozaki_group_destroy(OzGroup *g) {
     if (!g) return;
     if (g->h_jobs_sh) cudaFreeHost(g->h_jobs_sh);
+    if (g->ev_fork) cudaEventDestroy(g->ev_fork);
+    if (g->ev_join) cudaEventDestroy(g->ev_join);
+    if (g->side) cudaStreamDestroy(g->side);
     delete g;
 }
 

@@ -73,6 +73,9 @@ int ozaki_group_prepare(OzakiPlan &oz, const OzGroupDesc &d, const std::vector<O
 void ozaki_group_set_outputs(OzGroup *g, double2 *const *S, double2 *const *H, const int64_t *ld);
 // Structure-factor form: the group's combine table (outputs of this run, per-type products).
 void ozaki_group_set_sf(OzGroup *g, const SfTab &t);
+// Structure-factor form: the first type of the group's last combine (types [t0, nt), adding to
+// S and H unless t0 = 0): what ozaki_group_run leaves to its caller with defer_last_combine.
+int ozaki_group_last_combine(const OzGroup *g);
 // Enqueues the group's launches (slices, T application, phases, S/H products); no host sync.
 // ev: event pairs recorded around the S/H product launches (one pair, or one per type in the
 // structure-factor form; nev events, may be 0).  defer_last_combine: the structure-factor form's

@@ -43,7 +43,8 @@ __global__ void sf_table_kernel(const double2 *__restrict__ ex, const double2 *_
     }
 }
 
-constexpr int kSfTile = 32, kSfRows = 8;
+// 128-thread CTAs (32 rows x 4 column lanes): small enough to share an SM with a pair launch
+constexpr int kSfTile = 32, kSfRows = 4;
 
 // out (+)= sum over the batch's types t of SF_t(g_col - g_row) * P_t over the lower triangle of
 // every entry (S and H together), one CTA per 32 x 32 tile; consecutive threads take consecutive
@@ -84,7 +85,7 @@ __global__ void __launch_bounds__(kSfTile * kSfRows) sf_combine_kernel(const __g
         double2 vs = make_double2(0.0, 0.0), vh = make_double2(0.0, 0.0);
         for (int b = 0; b < tab.ntypes; ++b) {
             const double2 f = sft[idx + b * tab.box];
-            const double2 ps = E.PS[off + b * E.pstride], ph = E.PH[off + b * E.pstride];
+            const double2 ps = E.PS[off + (tab.slot0 + b) * E.pstride], ph = E.PH[off + (tab.slot0 + b) * E.pstride];
             vs.x = fma(f.x, ps.x, fma(-f.y, ps.y, vs.x));
             vs.y = fma(f.x, ps.y, fma(f.y, ps.x, vs.y));
             vh.x = fma(f.x, ph.x, fma(-f.y, ph.y, vh.x));

@@ -74,3 +74,20 @@ def test_type_batches_of_the_combine(ctx, precision, batch, monkeypatch):
         for X, R in ((H, Hr), (S, Sr)):
             fro, mx = oracle.lower_errors(X, R)
             assert fro < TOL and mx < TOL, (batch, precision, fro, mx)
+
+
+@pytest.mark.parametrize("knob", [("HSDLA_PAIR_HALVES", "1"), ("HSDLA_COMBINE_OVERLAP", "1"), ("HSDLA_MERGE", "0")])
+def test_structure_factor_variants(ctx, knob, monkeypatch):
+    """Full-width pair tiles, the half of the combine on a side stream, and one accumulation unit
+    per digit diagonal: each agrees with the oracle (c1: four types, 3000 columns, so the combine
+    of the host-buffer entry point runs in several 512-column blocks)."""
+    monkeypatch.setenv(*knob)
+    s = synth.make_system("c1")
+    res, _ = _run(ctx, s, "ozaki", True)
+    for (H, S), kp in zip(res, s.kpoints):
+        Hr, Sr = oracle.reference_hs(s, kp)
+        for X, R in ((H, Hr), (S, Sr)):
+            fro, mx = oracle.lower_errors(X, R)
+            assert fro < TOL and mx < TOL, (knob, fro, mx)
+        iu = np.triu_indices(kp.n_g, 1)
+        assert np.all(H[iu] == 0) and np.all(S[iu] == 0)
