@@ -816,11 +816,14 @@ __global__ void __launch_bounds__(kPairThreads, 1)
             for (int64_t tile = pair; ok && tile < total_tiles; tile += npairs) {
                 int64_t tm_, tn_;
                 const OzJob &j = resolve_tile(jobs, num_jobs, tile_list, tile, tm_, tn_);
+                // the job's fields in registers: the asm statements below clobber memory, and the
+                // issuer must not reload them between MMAs
+                const int64_t jnkb = j.nkb;
                 for (int u = 0; ok && u < units.n; ++u) {
                     const int t = units.t[u], merged = (units.flags[u] & kUnitMerged) ? 1 : 0;
-                    const int64_t ck = merged ? j.nkb : chunk_kblocks(min(s, t - 1) - max(1, t - s) + 1);
-                    for (int64_t cb = 0; ok && cb < j.nkb; cb += ck) {
-                        const int64_t ce = min(j.nkb, cb + ck);
+                    const int64_t ck = merged ? jnkb : chunk_kblocks(min(s, t - 1) - max(1, t - s) + 1);
+                    for (int64_t cb = 0; ok && cb < jnkb; cb += ck) {
+                        const int64_t ce = min(jnkb, cb + ck);
                         for (int h = 0; ok && h < kHalves; ++h) {
                             hb = h;
                             const uint32_t d_re = tmem_base + h * Shape::kBufCols, d_im = d_re + kN;
@@ -835,16 +838,25 @@ __global__ void __launch_bounds__(kPairThreads, 1)
                                         tc_fence_after();
                                         const uint32_t a_re = sbase + stage * kStageB, a_im = a_re + 16384;
                                         const uint32_t b_re = a_re + 32768, b_im = b_re + Shape::kBRows * kKBlock;
-#pragma unroll
-                                        for (int kk = 0; kk < kKBlock / 32; ++kk) {
-                                            const uint32_t off = kk * 32;
+                                        // The stage's four descriptors once; a 32-byte step along K adds 2
+                                        // to the start-address field (16-byte units; shared-memory
+                                        // addresses stay below 2^18, so the field never carries).  The
+                                        // single issuing thread has ~64 cycles per N = 128 MMA.
+                                        const uint64_t dar = sw128_desc(a_re), dai = sw128_desc(a_im);
+                                        const uint64_t dbr = sw128_desc(b_re), dbi = sw128_desc(b_im);
+                                        auto step = [&](uint32_t kk) {
+                                            const uint64_t o = 2u * kk;
                                             const uint32_t acc = first ? 0u : 1u;
-                                            mma_f8_pair(d_re, sw128_desc(a_re + off), sw128_desc(b_re + off), id_pos, acc);
-                                            mma_f8_pair(d_re, sw128_desc(a_im + off), sw128_desc(b_im + off), id_pos, 1u);
-                                            mma_f8_pair(d_im, sw128_desc(a_re + off), sw128_desc(b_im + off), id_pos, acc);
-                                            mma_f8_pair(d_im, sw128_desc(a_im + off), sw128_desc(b_re + off), id_neg, 1u);
+                                            mma_f8_pair(d_re, dar + o, dbr + o, id_pos, acc);
+                                            mma_f8_pair(d_re, dai + o, dbi + o, id_pos, 1u);
+                                            mma_f8_pair(d_im, dar + o, dbi + o, id_pos, acc);
+                                            mma_f8_pair(d_im, dai + o, dbr + o, id_neg, 1u);
                                             first = false;
-                                        }
+                                        };
+                                        // whole blocks as straight-line code: a bound on the steps (to skip
+                                        // the zero padding past 2L) slowed the launches by 2-10%
+#pragma unroll
+                                        for (int kk = 0; kk < kKBlock / 32; ++kk) step(kk);
                                         mma_commit_pair(&bars.empty[stage]);
                                         if (++stage == kStages) { stage = 0; phase ^= 1; }
                                     }
@@ -1861,7 +1873,10 @@ static int group_prepare_sf(OzakiPlan &oz, const OzGroupDesc &d, const std::vect
     g->nk = (int)kb.size();
     g->hoist = true;
     g->twoL = d.twoL; g->na = d.na; g->nt = d.nt;
-    g->bpad = round_up(d.twoL, kKBlock);                      // type stride along the contraction
+    // type stride along the contraction: whole 128-byte k-blocks (TMA boxes aligned to them; a
+    // 32-byte stride for lmax 8 put every other type's boxes across 128-byte lines: c3 10.3 -> 12.4 ms)
+    g->pair = use_pair();
+    g->bpad = round_up(d.twoL, kKBlock);
     const int64_t tkb = g->bpad / kKBlock, KT = g->bpad * d.nt;
     g->kb = kb;
     g->d_err = oz.d_error;
@@ -1897,7 +1912,6 @@ static int group_prepare_sf(OzakiPlan &oz, const OzGroupDesc &d, const std::vect
     };
     // M: the S/H products' left operand; on pair tiles with its digits scaled by 2^-5 as well
     // (planes 2s .. 4s-1), the merged accumulation units' left digits
-    g->pair = use_pair();
     carve_rows(g->dM, g->pair ? 4 * s : 2 * s);
     carve_rows(g->dW, 2 * s);    // M diag(w_t)
     carve_rows(g->dX, 2 * s);    // Z
