@@ -257,8 +257,12 @@ def run_ours(args):
     e2e_flop = sys_.flop_per_kpoint(G)
     h2d = sum(a.nbytes for a in (kp.g, tmats[0], tmats[1], tmats[2], sys_.u, sys_.u_dr, sys_.dE_u,
                                   sys_.dE_u_dr, sys_.dE_u_norm, sys_.atom_pos, sys_.atom_type, sys_.type_rmt))
-    # the download copies each 512-column block of H and S from its first row down
-    d2h = 2 * 16 * sum((G - c0) * min(512, G - c0) for c0 in range(0, G, 512))
+    if rep_e["outputs_in_place"]:
+        # the last combine wrote the lower triangles of H and S into the page-locked buffers
+        d2h = 2 * 16 * G * (G + 1) // 2
+    else:
+        # the download copies each 512-column block of H and S from its first row down
+        d2h = 2 * 16 * sum((G - c0) * min(512, G - c0) for c0 in range(0, G, 512))
 
     # ---- plain FP64 path on the first k-point, and the Ozaki error against it
     fp64 = None
@@ -331,6 +335,8 @@ def run_ours(args):
                 "e2e": {"value": ws * e2e_flop / e2e_s / 1e12, "unit": UNIT, "ms_per_kpoint": e2e_s * 1e3,
                         "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                         "calls_ms": [round(x, 2) for x in e2e_calls],
+                        "outputs": "written in place by the last combine" if rep_e["outputs_in_place"]
+                        else "downloaded by the copy engine",
                         "note": "hsdla_create_hs on the rank's first k-point, pinned host buffers; "
                                 "value = mean over calls_ms"},
                 "gpu_launches": launches,

@@ -96,7 +96,9 @@ cudaError_t launch_fp64_jobs(const Fp64Job *d_jobs, int num_jobs, int64_t total_
 struct SfEntry {
     const double2 *PS = nullptr, *PH = nullptr;   // per-type products, type slot b at + b pstride
     double2 *S = nullptr, *H = nullptr;
-    int64_t ldp = 0, ldo = 0, n = 0, pstride = 0;
+    // what a combine that is not the first adds to (NULL: S and H themselves, ldo)
+    const double2 *Si = nullptr, *Hi = nullptr;
+    int64_t ldp = 0, ldo = 0, n = 0, pstride = 0, ldi = 0;
     const int32_t *g = nullptr;
     int64_t tile_begin = 0;
 };

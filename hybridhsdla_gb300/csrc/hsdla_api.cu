@@ -122,7 +122,9 @@ struct hsdla_plan {
     struct Download {
         std::vector<hsdla_cx *> H, S;
         std::vector<int64_t> ld;
+        bool direct = false;   // every output is page-locked host memory the GPU can write
         bool done = false;
+        bool in_place = false;   // the combine wrote the host outputs
     };
     Download *dl = nullptr;
     double est_err = 0.0;            // autotuner's predicted relative error
@@ -149,6 +151,13 @@ int set_err(hsdla_context *ctx, int code, const char *fmt, ...) {
         if (e_ != cudaSuccess)                                                                        \
             return set_err((ctx), HSDLA_ERR_CUDA, "%s failed: %s", #call, cudaGetErrorString(e_));    \
     } while (0)
+
+// Environment switch: unset or empty -> dflt, "0" -> false, anything else -> true.
+bool env_flag(const char *name, bool dflt) {
+    const char *v = getenv(name);
+    if (!v || !*v) return dflt;
+    return strcmp(v, "0") != 0;
+}
 
 constexpr int64_t kCacheBlockMax = (int64_t)256 << 20;    // larger blocks are freed, not kept
 constexpr int64_t kCacheBytesMax = (int64_t)1 << 30;       // at most this much kept
@@ -1154,6 +1163,23 @@ int combine_last(hsdla_plan *pl, hsdla_plan::Group &g, int t0, int ntypes, cudaS
         pl->launches++;
         return HSDLA_OK;
     }
+    if (pl->dl->direct) {
+        // the combine writes the host outputs itself (page-locked memory, addressed over the
+        // CPU-GPU link), adding to the device sums of the earlier batches: no download
+        for (int q = 0; q < g.ktab.nk; ++q) {
+            const int i = g.kidx[q];
+            tab.e[q].Si = tab.e[q].S;
+            tab.e[q].Hi = tab.e[q].H;
+            tab.e[q].ldi = tab.e[q].ldo;
+            tab.e[q].H = reinterpret_cast<double2 *>(pl->dl->H[i]);
+            tab.e[q].S = reinterpret_cast<double2 *>(pl->dl->S[i]);
+            tab.e[q].ldo = pl->dl->ld[i];
+        }
+        CUDA_TRY(ctx, launch_sf_combine(tab, pl->sf_tab, t0 == 0, st));
+        pl->launches++;
+        pl->dl->done = pl->dl->in_place = true;
+        return HSDLA_OK;
+    }
     int64_t gmax = 0;
     for (int q = 0; q < g.ktab.nk; ++q) gmax = std::max(gmax, pl->kps[g.kidx[q]].n_g);
     for (int64_t c0 = 0; c0 < gmax; c0 += kDownBlock) {
@@ -1611,6 +1637,20 @@ int hsdla_create_hs(hsdla_context *ctx, const hsdla_system *s, const hsdla_kpoin
     dl.H.assign(H, H + nk);
     dl.S.assign(S, S + nk);
     dl.ld.assign(ld, ld + nk);
+    // page-locked host outputs that the GPU addresses directly (unified addressing): the last
+    // combine can write them in place (HSDLA_DIRECT_OUTPUT=0 keeps the download)
+    dl.direct = nk > 0 && env_flag("HSDLA_DIRECT_OUTPUT", true);
+    for (int i = 0; dl.direct && i < nk; ++i) {
+        if (ng[i] == 0) continue;
+        for (hsdla_cx *hp : {H[i], S[i]}) {
+            cudaPointerAttributes pa{};
+            if (cudaPointerGetAttributes(&pa, hp) != cudaSuccess || pa.type != cudaMemoryTypeHost ||
+                pa.devicePointer != (void *)hp) {
+                cudaGetLastError();
+                dl.direct = false;
+            }
+        }
+    }
     if (e == cudaSuccess) {
         pl->dl = &dl;
         rc = hsdla_plan_execute(pl, dH.data(), dS.data(), dld.data(), ctx->stream, rep);
@@ -1639,6 +1679,7 @@ int hsdla_create_hs(hsdla_context *ctx, const hsdla_system *s, const hsdla_kpoin
         rep->ms_total = ms;   // end-to-end: upload, compute, download
         rep->ms_per_kpoint = nk ? ms / nk : 0.0;
         rep->eff_tflops = ms > 0 ? pl->flop / (ms * 1e-3) / 1e12 : 0.0;
+        rep->outputs_in_place = dl.in_place ? 1 : 0;
     }
     hsdla_plan_destroy(pl);
     cudaEventDestroy(e0);

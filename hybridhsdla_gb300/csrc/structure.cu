@@ -93,7 +93,7 @@ __global__ void __launch_bounds__(kSfTile * kSfRows) sf_combine_kernel(const __g
         }
         double2 *so = E.S + row + E.ldo * col, *ho = E.H + row + E.ldo * col;
         if (!first) {
-            const double2 s0 = *so, h0 = *ho;
+            const double2 s0 = E.Si[row + E.ldi * col], h0 = E.Hi[row + E.ldi * col];
             vs.x += s0.x; vs.y += s0.y;
             vh.x += h0.x; vh.y += h0.y;
         }
@@ -128,6 +128,12 @@ int64_t sf_tab_tiles(SfTab &tab) {
 
 cudaError_t launch_sf_combine(const SfTab &tab, const double2 *sf, bool first, cudaStream_t st) {
     SfTab t = tab;
+    for (int k = 0; k < t.nk; ++k)
+        if (!t.e[k].Si) {
+            t.e[k].Si = t.e[k].S;
+            t.e[k].Hi = t.e[k].H;
+            t.e[k].ldi = t.e[k].ldo;
+        }
     const int64_t tiles = sf_tab_tiles(t);
     if (tiles <= 0) return cudaSuccess;
     if (tiles > 0x7fffffffLL) return cudaErrorInvalidValue;

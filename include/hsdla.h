@@ -33,7 +33,11 @@
  *     strict upper triangle untouched.  The host-buffer entry points (hsdla_create_hs,
  *     hsdla_contract_ab) download 512-column blocks from their first row down, which sets
  *     the strict upper triangle of the diagonal 512 x 512 blocks to zero and leaves the rest
- *     of it untouched (the reference leaves it unset as well).
+ *     of it untouched (the reference leaves it unset as well).  Where every H and S given to
+ *     hsdla_create_hs is page-locked host memory that the GPU addresses at the same pointer
+ *     (cudaHostAlloc, cudaMallocHost) and the plan takes the structure-factor form, the last
+ *     combine writes the lower triangles in place and the whole strict upper triangle stays
+ *     untouched (HSDLA_DIRECT_OUTPUT=0 keeps the download).
  */
 #ifndef HSDLA_H
 #define HSDLA_H
@@ -119,7 +123,8 @@ typedef struct hsdla_report {
     int32_t num_kpoints;
     int32_t kernel_launches;     /* kernels launched per execution */
     int32_t num_panels;          /* Ozaki: atom panels the contraction was streamed in (1 = resident) */
-    int32_t reserved[4];
+    int32_t outputs_in_place;    /* hsdla_create_hs: 1 = the GPU wrote the page-locked host H, S itself */
+    int32_t reserved[3];
 } hsdla_report;
 
 typedef struct hsdla_context hsdla_context;

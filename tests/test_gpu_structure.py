@@ -91,3 +91,33 @@ def test_structure_factor_variants(ctx, knob, monkeypatch):
             assert fro < TOL and mx < TOL, (knob, fro, mx)
         iu = np.triu_indices(kp.n_g, 1)
         assert np.all(H[iu] == 0) and np.all(S[iu] == 0)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "ozaki"])
+@pytest.mark.parametrize("batch", ["2", "8"])
+def test_outputs_written_in_place(ctx, precision, batch, monkeypatch):
+    """Page-locked host outputs: the last combine writes H and S itself (after earlier batches on
+    the device with a batch of 2 types) and the lower triangles equal, bit for bit, those of the
+    download into pageable buffers; the strict upper triangle is not touched at all."""
+    torch = pytest.importorskip("torch")
+    monkeypatch.setenv("HSDLA_TYPE_BATCH", batch)
+    s = synth.make_system("c1")
+    res_ref, rep_ref = _run(ctx, s, precision, True)
+    assert rep_ref["outputs_in_place"] == 0
+    outs, keep = [], []
+    for kp in s.kpoints:
+        pair = []
+        for _ in range(2):
+            t = torch.full((kp.n_g, kp.n_g), complex(7.0, -3.0), dtype=torch.complex128).pin_memory()
+            keep.append(t)
+            pair.append(t.numpy().T)       # column-major view of the page-locked buffer
+        outs.append(tuple(pair))
+    monkeypatch.setenv("HSDLA_SF", "1")
+    res, rep = ctx.create_hs(s, precision=precision, num_slices=11 if precision == "ozaki" else 0, out=outs)
+    assert rep["outputs_in_place"] == 1
+    for (H, S), (Hr, Sr), kp in zip(res, res_ref, s.kpoints):
+        il = np.tril_indices(kp.n_g)
+        iu = np.triu_indices(kp.n_g, 1)
+        for X, R in ((H, Hr), (S, Sr)):
+            assert np.array_equal(X[il], R[il])
+            assert np.all(X[iu] == complex(7.0, -3.0))
