@@ -191,8 +191,9 @@ __global__ void __launch_bounds__(kThreads) construct_ab_kernel(DevSystem sys, c
                 bu[tl] = -sys.u[tl] * kn * dfj[l] + sys.u_dr[tl] * fj[l];
             }
         }
-        // structure phase per atom, premultiplied by 4 pi / sqrt(Omega)
-        for (int j = threadIdx.x; j < na; j += blockDim.x) {
+        // structure phase per atom, premultiplied by 4 pi / sqrt(Omega) (only the per-atom rows C
+        // carry it)
+        for (int j = threadIdx.x; C && j < na; j += blockDim.x) {
             const double *p = sys.atom_pos + 3 * j;
             const double arg = 2 * kPi * (K0 * p[0] + K1 * p[1] + K2 * p[2]);
             double sn, cs;
@@ -244,12 +245,13 @@ __global__ void __launch_bounds__(kThreads) construct_ab_kernel(DevSystem sys, c
                     const int l = l_of[lm];
                     double2 out = make_double2(0.0, 0.0);
                     if (l <= sys.type_lmax[t]) {
+                        // conj(Y_lm) times the real prefactor, then the radial factor: the complex
+                        // product with a zero imaginary part, without its FP64 work on zeros
                         const int tl = t * nl + l;
-                        const double2 common = make_double2(sys.vol_prefac * sys.inv_w[tl], 0.0);
+                        const double c = sys.vol_prefac * sys.inv_w[tl];
                         const double2 y = ylm[lm];
-                        const double2 ycc = cmul(make_double2(y.x, -y.y), common);
                         const double f = isB ? bu[tl] : au[tl];
-                        out = make_double2(ycc.x * f, ycc.y * f);
+                        out = make_double2((y.x * c) * f, (-y.y * c) * f);
                     }
                     mcol[idx] = out;
                 }

@@ -36,6 +36,7 @@
 #include <cuda_fp8.h>
 
 #include <algorithm>
+#include <type_traits>
 #include <cstdio>
 #include <cstring>
 #include <vector>
@@ -1063,11 +1064,9 @@ struct SliceTab {
     SliceEntry e[kMaxGroup];
 };
 
-__device__ __forceinline__ uint32_t pack4_e4m3(int d0, int d1, int d2, int d3) {
-    const uint32_t lo = __nv_cvt_float2_to_fp8x2(make_float2((float)d0, (float)d1), __NV_SATFINITE, __NV_E4M3);
-    const uint32_t hi = __nv_cvt_float2_to_fp8x2(make_float2((float)d2, (float)d3), __NV_SATFINITE, __NV_E4M3);
-    return lo | (hi << 16);
-}
+// e4m3 byte of the digit idx - 16 (idx in [0, 32]), per CTA of the slicing kernel: a digit is
+// one shared-memory load instead of an integer-to-float conversion and half a packing conversion
+__shared__ uint8_t g_e4m3_lut[33];
 // Four e4m3 digits (|d| <= 16) times 2^-5: every nonzero digit is normal with exponent field >= 7
 // (|d| >= 1), so subtracting 5 from the field (0x28 from the byte, no borrow) scales it exactly
 // (d / 32 >= 2^-5 stays normal); zeros keep their bytes.
@@ -1089,15 +1088,15 @@ __device__ __forceinline__ void write_part(const long long (&x)[kVec], int part,
 #pragma unroll 1
     for (int step = 0; step < s; ++step) {
         const int i = s - 1 - step;
-        int d[kVec];
+        uint32_t w0 = 0, w1 = 0;
 #pragma unroll
         for (int v = 0; v < kVec; ++v) {
-            d[v] = i == 0 ? (int)u[v] : (int)(u[v] & 31) - 16;
+            const int idx = i == 0 ? (int)u[v] + 16 : (int)(u[v] & 31);
+            const uint32_t b = (uint32_t)g_e4m3_lut[idx] << (8 * (v & 3));
+            if (v < 4) w0 |= b; else w1 |= b;
             u[v] >>= 5;
         }
         uint8_t *dst = row + (int64_t)(2 * i + part) * plane;
-        const uint32_t w0 = pack4_e4m3(d[0], d[1], d[2], d[3]);
-        const uint32_t w1 = kVec == 8 ? pack4_e4m3(d[4 % kVec], d[5 % kVec], d[6 % kVec], d[7 % kVec]) : 0u;
         if (kVec == 8) *reinterpret_cast<uint2 *>(dst) = make_uint2(w0, w1);
         else *reinterpret_cast<uint32_t *>(dst) = w0;
         if (kScaled) {
@@ -1115,13 +1114,22 @@ __device__ __forceinline__ void write_planes(const long long (&ur)[kVec], const 
     write_part<kVec, kScaled>(ui, 1, s, row, plane);
 }
 
-__device__ __forceinline__ double block_max(double m, double *red) {
-    for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+// Maximum over the block of non-negative doubles given as bit patterns (which order like the
+// values), with integer operations: GB300's FP64 pipe takes 16 cycles per warp instruction, and
+// an FP64 max here was most of the slicing's FP64 work.
+__device__ __forceinline__ unsigned long long block_max_bits(unsigned long long m, unsigned long long *red) {
+    for (int o = 16; o > 0; o >>= 1) m = max(m, (unsigned long long)__shfl_xor_sync(0xffffffffu, m, o));
     if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
     __syncthreads();
-    double r = 0.0;
-    for (int i = 0; i < kSliceThreads / 32; ++i) r = fmax(r, red[i]);
+    unsigned long long r = 0;
+    for (int i = 0; i < kSliceThreads / 32; ++i) r = max(r, red[i]);
     return r;
+}
+// frexp's exponent of a positive finite double given as bits: x = f 2^e with f in [1/2, 1)
+__device__ __forceinline__ int frexp_exp_bits(unsigned long long b) {
+    const int E = (int)(b >> 52) & 0x7ff;
+    if (E) return E - 1022;
+    return -1010 - __clzll((long long)(b & 0xfffffffffffffull));   // subnormal: mantissa 2^-1074
 }
 
 // Integer-pipe helpers of the slicing (GB300's FP64 pipe runs ~1/64 of its integer rate).
@@ -1150,11 +1158,12 @@ __device__ __forceinline__ long long rint_pow2(double x, int k) {
     return (b >> 63) ? -(long long)q : (long long)q;
 }
 // v 2^k by an exponent add (v normal and the result normal), else ldexp
+__device__ __noinline__ double ldexp_out_of_line(double v, int k) { return ldexp(v, k); }
 __device__ __forceinline__ double scale_pow2(double v, int k) {
     const long long b = __double_as_longlong(v);
     const int E = (int)((b >> 52) & 0x7ff);
     if (E > 0 && E + k > 0 && E + k < 2047) return __longlong_as_double(b + ((long long)k << 52));
-    return ldexp(v, k);
+    return ldexp_out_of_line(v, k);    // (a call: inlined, its FP64 work was issued for every value)
 }
 
 // the weighted operand's digits of one chunk (kept out of line: inlined next to the first
@@ -1190,12 +1199,19 @@ __global__ void __launch_bounds__(kSliceThreads, HSDLA_SLICE_CTAS) oz_slice_kern
     const int Kin = (int)tab.Kin, rpb = (int)tab.rpb, bpad = (int)tab.bpad, Kpad = (int)tab.Kpad;
     const int64_t pitch = tab.pitch, plane_rows = tab.plane_rows;
     const int s = tab.s;
-    __shared__ double red[2][kSliceThreads / 32];
+    __shared__ unsigned long long red[2][kSliceThreads / 32];
+    // the digit table (read in pass 2, after the barrier of the row maximum)
+    if (threadIdx.x < 33) {
+        const float dv = (float)((int)threadIdx.x - 16);
+        g_e4m3_lut[threadIdx.x] = (uint8_t)(__nv_cvt_float2_to_fp8x2(make_float2(dv, 0.f), __NV_SATFINITE, __NV_E4M3) & 0xffu);
+    }
     // pass 1: column max of max(|re|, |im|) (times the row weight; the only FP64 multiply here)
     // Each thread reads 8 consecutive values per step (all loads of a step in flight together):
     // one value per thread and step kept too few bytes in flight to cover the memory latency.
+    // (the weighted and unweighted forms as separate loops: GB300 issues the FP64 multiplies of a
+    // predicated-off branch all the same, at 16 cycles per warp instruction)
     unsigned long long mx = 0, mx2 = 0;
-    if (live) {
+    auto pass1 = [&](auto weighted) {
         for (int k0 = threadIdx.x * kSliceVec; k0 < Kin; k0 += kSliceThreads * kSliceVec) {
             double2 z[kSliceVec];
 #pragma unroll
@@ -1204,18 +1220,23 @@ __global__ void __launch_bounds__(kSliceThreads, HSDLA_SLICE_CTAS) oz_slice_kern
             for (int u = 0; u < kSliceVec; ++u) {
                 const unsigned long long a = max(abs_bits(z[u].x), abs_bits(z[u].y));
                 if (k0 + u < Kin) {
-                    mx = max(mx, v ? abs_bits(__longlong_as_double((long long)a) * v[k0 + u]) : a);
+                    if constexpr (decltype(weighted)::value) mx = max(mx, abs_bits(__longlong_as_double((long long)a) * v[k0 + u]));
+                    else mx = max(mx, a);
                     if (kDual) mx2 = max(mx2, abs_bits(__longlong_as_double((long long)a) * v2[k0 + u]));
                 }
             }
         }
+    };
+    if (live) {
+        if (v) pass1(std::true_type{});
+        else pass1(std::false_type{});
     }
     int e = 0, e2 = 0;
-    const double m = block_max(__longlong_as_double((long long)mx), red[0]);
-    if (m > 0.0) frexp(m, &e);              // m < 2^e
+    const unsigned long long m = block_max_bits(mx, red[0]);
+    if (m > 0) e = frexp_exp_bits(m);       // max < 2^e
     if (kDual) {
-        const double m2 = block_max(__longlong_as_double((long long)mx2), red[1]);
-        if (m2 > 0.0) frexp(m2, &e2);
+        const unsigned long long m2 = block_max_bits(mx2, red[1]);
+        if (m2 > 0) e2 = frexp_exp_bits(m2);
     }
     if (threadIdx.x == 0) {
         tab.expo[r] = e;
@@ -1227,29 +1248,33 @@ __global__ void __launch_bounds__(kSliceThreads, HSDLA_SLICE_CTAS) oz_slice_kern
     for (int p = 0; p < s - 1; ++p) B |= 16ll << (5 * p);
     const int nb = Kpad / bpad;
     const int64_t plane = plane_rows * pitch;
-    for (int kp0 = threadIdx.x * kV; kp0 < Kpad; kp0 += kSliceThreads * kV) {
-        // a chunk never straddles a contraction block (bpad is a multiple of kV)
-        const int b = kp0 / bpad, rr0 = kp0 - b * bpad;
-        // number of live values of this chunk (a prefix: the block tail and Kin cut it from above)
-        const int nv = live && b < nb ? max(0, min(min(kV, rpb - rr0), Kin - (b * rpb + rr0))) : 0;
-        const double2 *zc = Zc + b * rpb + rr0;
-        long long xr[kV], xi[kV];
+    auto pass2 = [&](auto weighted) {
+        for (int kp0 = threadIdx.x * kV; kp0 < Kpad; kp0 += kSliceThreads * kV) {
+            // a chunk never straddles a contraction block (bpad is a multiple of kV)
+            const int b = kp0 / bpad, rr0 = kp0 - b * bpad;
+            // number of live values of this chunk (a prefix: the block tail and Kin cut it from above)
+            const int nv = live && b < nb ? max(0, min(min(kV, rpb - rr0), Kin - (b * rpb + rr0))) : 0;
+            const double2 *zc = Zc + b * rpb + rr0;
+            long long xr[kV], xi[kV];
 #pragma unroll
-        for (int u = 0; u < kV; ++u) {
-            const double2 z = u < nv ? zc[u] : make_double2(0.0, 0.0);
-            if (v && u < nv) {
-                const double sc = scale_pow2(v[b * rpb + rr0 + u], kx);
-                xr[u] = B + rint_pow2(z.x * sc, 0);
-                xi[u] = B + rint_pow2(z.y * sc, 0);
-            } else {
-                xr[u] = B + rint_pow2(z.x, kx);
-                xi[u] = B + rint_pow2(z.y, kx);
+            for (int u = 0; u < kV; ++u) {
+                const double2 z = u < nv ? zc[u] : make_double2(0.0, 0.0);
+                if constexpr (decltype(weighted)::value) {
+                    const double sc = u < nv ? scale_pow2(v[b * rpb + rr0 + u], kx) : 0.0;
+                    xr[u] = B + rint_pow2(z.x * sc, 0);
+                    xi[u] = B + rint_pow2(z.y * sc, 0);
+                } else {
+                    xr[u] = B + rint_pow2(z.x, kx);
+                    xi[u] = B + rint_pow2(z.y, kx);
+                }
             }
+            write_planes<kV, kScaled>(xr, xi, s, tab.digits + r * pitch + kp0, plane);
+            if (kDual)      // the chunk again (an L1 hit) for the weighted operand
+                weighted_chunk<kV>(zc, v2 + b * rpb + rr0, nv, kw, B, s, tab.digits2 + r * pitch + kp0, plane);
         }
-        write_planes<kV, kScaled>(xr, xi, s, tab.digits + r * pitch + kp0, plane);
-        if (kDual)      // the chunk again (an L1 hit) for the weighted operand
-            weighted_chunk<kV>(zc, v2 + b * rpb + rr0, nv, kw, B, s, tab.digits2 + r * pitch + kp0, plane);
-    }
+    };
+    if (v) pass2(std::true_type{});
+    else pass2(std::false_type{});
 }
 
 // ------------------------------------------------------------ host helpers
