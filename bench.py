@@ -361,7 +361,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--slices", type=int, default=0, help="Ozaki digit slices (0 = default)")
-    ap.add_argument("--ref-sample-ng", type=int, default=1500)
+    ap.add_argument("--ref-sample-ng", type=int, default=3200)   # ~11 s of CPU work per step
     ap.add_argument("--oracle-block", type=int, default=0,
                     help="compare the first k-point's top-left N x N block of H and S with the oracle")
     ap.add_argument("--skip-fp64", action="store_true")
