@@ -335,11 +335,103 @@ __global__ void __launch_bounds__(kThreads) apply_phase_kernel(DevSystem sys, co
     }
 }
 
+// The full Hermitian T block of a type, as the reference's zhemm('L') calls read it from the lower
+// triangles (h_and_s_stripped_v2.cpp:202,345).  One CTA column per type (blockIdx.y), threads over
+// the L x L entries (r fastest): each writes the four quadrant entries at (r, c) and folds its
+// checks into the CTA's, then one atomic each.
+constexpr int kTfThreads = 256;
+__global__ void __launch_bounds__(kTfThreads) tfull_kernel(const double2 *__restrict__ aa_all,
+                                                           const double2 *__restrict__ ab_all,
+                                                           const double2 *__restrict__ bb_all, int L, double2 *tf,
+                                                           unsigned long long *stats) {
+    const int t = blockIdx.y;
+    const int64_t LL = (int64_t)L * L, n = 2 * (int64_t)L;
+    const double2 *aa = aa_all + t * LL, *ab = ab_all + t * LL, *bb = bb_all + t * LL;
+    double2 *out = tf + t * 4 * LL;
+    unsigned int flags = 0;
+    unsigned long long st[4] = {0, 0, 0, 0};
+    auto bits = [](double v) { return (unsigned long long)__double_as_longlong(v); };
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < LL; e += (int64_t)gridDim.x * blockDim.x) {
+        const int r = (int)(e % L), c = (int)(e / L);
+        const int64_t i = r + (int64_t)L * c, iT = c + (int64_t)L * r;
+        const double2 a = aa[i], aT = aa[iT], b = bb[i], bT = bb[iT], x = ab[i], xT = ab[iT];
+        if (!isfinite(a.x) || !isfinite(a.y)) flags |= 1u;
+        if (!isfinite(x.x) || !isfinite(x.y)) flags |= 2u;
+        if (!isfinite(b.x) || !isfinite(b.y)) flags |= 4u;
+        const bool low = r >= c;
+        out[r + n * c] = low ? a : make_double2(aT.x, -aT.y);
+        out[(L + r) + n * (L + c)] = low ? b : make_double2(bT.x, -bT.y);
+        out[r + n * (L + c)] = x;
+        out[(L + r) + n * c] = make_double2(xT.x, -xT.y);
+        if (low) {
+            // |T|^2 of the pair and |T - T^H|^2 (the mirror element is the pair's other half)
+            st[0] = max(st[0], bits(fmax(a.x * a.x + a.y * a.y, aT.x * aT.x + aT.y * aT.y)));
+            st[1] = max(st[1], bits((a.x - aT.x) * (a.x - aT.x) + (a.y + aT.y) * (a.y + aT.y)));
+            st[2] = max(st[2], bits(fmax(b.x * b.x + b.y * b.y, bT.x * bT.x + bT.y * bT.y)));
+            st[3] = max(st[3], bits((b.x - bT.x) * (b.x - bT.x) + (b.y + bT.y) * (b.y + bT.y)));
+        }
+    }
+    __shared__ unsigned long long red[kTfThreads / 32][4];
+    __shared__ unsigned int fl[kTfThreads / 32];
+    for (int o = 16; o > 0; o >>= 1) {
+        flags |= __shfl_xor_sync(0xffffffffu, flags, o);
+        for (int q = 0; q < 4; ++q) st[q] = max(st[q], (unsigned long long)__shfl_xor_sync(0xffffffffu, st[q], o));
+    }
+    const int w = threadIdx.x >> 5;
+    if ((threadIdx.x & 31) == 0) {
+        fl[w] = flags;
+        for (int q = 0; q < 4; ++q) red[w][q] = st[q];
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int k = 1; k < kTfThreads / 32; ++k) {
+            flags |= fl[k];
+            for (int q = 0; q < 4; ++q) st[q] = max(st[q], red[k][q]);
+        }
+        if (flags) atomicOr(stats + 5 * t, (unsigned long long)flags);
+        for (int q = 0; q < 4; ++q)
+            if (st[q]) atomicMax(stats + 5 * t + 1 + q, st[q]);
+    }
+}
+
+__global__ void sf_phase_kernel(const double *pos, int na, int h0, int h1, int h2, int e0, int e1, int e2,
+                                double2 *ph) {
+    const int64_t n0 = (int64_t)na * e0, n1 = (int64_t)na * e1, total = n0 + n1 + (int64_t)na * e2;
+    for (int64_t o = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; o < total; o += (int64_t)gridDim.x * blockDim.x) {
+        int c, e, h;
+        int64_t q = o;
+        if (q < n0) { c = 0; e = e0; h = h0; }
+        else if (q < n0 + n1) { q -= n0; c = 1; e = e1; h = h1; }
+        else { q -= n0 + n1; c = 2; e = e2; h = h2; }
+        const int j = (int)(q / e), i = (int)(q % e);
+        double sn, cs;
+        sincos(2 * kPi * (double)(i - h) * pos[3 * j + c], &sn, &cs);
+        ph[o] = make_double2(cs, sn);
+    }
+}
+
 int sm_count() {
     int dev = 0, nsm = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
     return nsm;
+}
+
+cudaError_t launch_tfull(const double2 *aa, const double2 *ab, const double2 *bb, int nt, int L, double2 *tf,
+                         unsigned long long *stats, cudaStream_t st) {
+    if (nt <= 0 || L <= 0) return cudaSuccess;
+    const int64_t LL = (int64_t)L * L;
+    const dim3 grid((unsigned)std::min<int64_t>((LL + kTfThreads - 1) / kTfThreads, 64), (unsigned)nt);
+    tfull_kernel<<<grid, kTfThreads, 0, st>>>(aa, ab, bb, L, tf, stats);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_sf_phases(const double *pos, int na, const int *half, const int *ext, double2 *ph, cudaStream_t st) {
+    const int64_t total = (int64_t)na * (ext[0] + ext[1] + ext[2]);
+    if (total <= 0) return cudaSuccess;
+    const int64_t blocks = std::min<int64_t>((total + 255) / 256, 4096);
+    sf_phase_kernel<<<(unsigned)blocks, 256, 0, st>>>(pos, na, half[0], half[1], half[2], ext[0], ext[1], ext[2], ph);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_apply_phase_multi(const DevSystem &sys, const KTable &tab, cudaStream_t st) {

@@ -71,6 +71,17 @@ cudaError_t launch_apply_phase_multi(const DevSystem &sys, const KTable &tab, cu
 // its own rotation (M_t = C_a e^{-i 2pi K.tau_a} for every atom a of type t).
 cudaError_t launch_construct_ab(const DevSystem &sys, const DevKpoint &kp, double2 *C, int64_t ldc,
                                 cudaStream_t st, double2 *M = nullptr, int64_t ldm = 0);
+// The Hermitian 2L x 2L blocks [[T_AA, T_AB], [T_AB^H, T_BB]] of every type (column-major, ld 2L,
+// 4 L^2 apart) into tf, from the caller's lower triangles of T_AA and T_BB and all of T_AB (each
+// nt x L x L, column-major per type), with the input checks per type in stats[5 t .. 5 t + 4]
+// (zeroed by the caller): bit q of [0] set when block q (0 AA, 1 AB, 2 BB) holds a non-finite
+// value; [1], [2] = max |T|^2 and max |T - T^H|^2 over T_AA's lower triangle, [3], [4] the same
+// for T_BB (doubles as bit patterns).
+cudaError_t launch_tfull(const double2 *aa, const double2 *ab, const double2 *bb, int nt, int L, double2 *tf,
+                         unsigned long long *stats, cudaStream_t st);
+// Per-atom structure phases along each axis, ph[o] = e^{i 2pi (i - half_c) pos[3 j + c]} with o
+// running over c, then atom j, then i in [0, ext_c).
+cudaError_t launch_sf_phases(const double *pos, int na, const int *half, const int *ext, double2 *ph, cudaStream_t st);
 // X[2L a + r, g] = e^{i 2pi (k+g).tau_a} Z[2L t(a) + r, g]
 cudaError_t launch_apply_phase(const DevSystem &sys, const DevKpoint &kp, const double2 *Z, int64_t ldz,
                                double2 *X, int64_t ldx, cudaStream_t st);

@@ -52,6 +52,10 @@ struct hsdla_context {
     std::multimap<int64_t, void *> cache;
     std::map<void *, int64_t> live;
     int64_t cached_bytes = 0;
+    // page-locked staging of a plan's table upload (grows on demand; a plan's upload completes
+    // before hsdla_plan_create returns, so the next plan reuses it)
+    void *staging = nullptr;
+    int64_t staging_bytes = 0;
     std::set<hsdla_plan *> plans;   // live plans, destroyed with the context
     // slice autotuner results: (L, atoms, types, n_G bucket, target) -> (slices, predicted error)
     std::map<std::tuple<int, int, int, int64_t, double>, std::pair<int, double>> tune_cache;
@@ -309,7 +313,7 @@ int validate(hsdla_context *ctx, const hsdla_system *s, const hsdla_kpoint *kpts
     if (!(s->vol_cell > 0.0) || !std::isfinite(s->vol_cell))
         return set_err(ctx, HSDLA_ERR_INPUT, "vol_cell must be positive and finite");
     if (!finite_all(s->bmat, 9)) return set_err(ctx, HSDLA_ERR_INPUT, "bmat is not finite");
-    const int na = s->num_atoms, nt = s->num_types, nl = s->max_lmax + 1, L = nl * nl;
+    const int na = s->num_atoms, nt = s->num_types, nl = s->max_lmax + 1;
     for (int j = 0; j < na; ++j)
         if (s->atom_type[j] < 0 || s->atom_type[j] >= nt)
             return set_err(ctx, HSDLA_ERR_ARG, "atom_type[%d]=%d out of range", j, s->atom_type[j]);
@@ -333,26 +337,7 @@ int validate(hsdla_context *ctx, const hsdla_system *s, const hsdla_kpoint *kpts
             if (s->type_dE_u_norm[tl] < 0.0)
                 return set_err(ctx, HSDLA_ERR_INPUT, "negative ||udot||^2 for type %d, l=%d", t, l);
         }
-        const hsdla_cx *T3[3] = {s->type_t_aa + (int64_t)t * L * L, s->type_t_ab + (int64_t)t * L * L,
-                                 s->type_t_bb + (int64_t)t * L * L};
-        for (int q = 0; q < 3; ++q)
-            if (!finite_all(reinterpret_cast<const double *>(T3[q]), 2 * (int64_t)L * L))
-                return set_err(ctx, HSDLA_ERR_INPUT, "T block %d of type %d not finite", q, t);
-        // T_AA and T_BB must be Hermitian (AtomData.cpp:138-139 asserts it): squared magnitudes over
-        // the lower triangle (its mirror element is the pair's other half)
-        for (int q = 0; q < 3; q += 2) {
-            double mx2 = 0.0, dev2 = 0.0;
-            for (int c = 0; c < L; ++c)
-                for (int r = c; r < L; ++r) {
-                    const hsdla_cx a = T3[q][r + (int64_t)L * c], b = T3[q][c + (int64_t)L * r];
-                    mx2 = std::max(mx2, std::max(a.re * a.re + a.im * a.im, b.re * b.re + b.im * b.im));
-                    const double dr = a.re - b.re, di = a.im + b.im;
-                    dev2 = std::max(dev2, dr * dr + di * di);
-                }
-            if (dev2 > 1e-24 * std::max(mx2, 1e-300))
-                return set_err(ctx, HSDLA_ERR_INPUT, "T_%s of type %d is not Hermitian (|T-T^H| = %.3g)",
-                               q == 0 ? "AA" : "BB", t, std::sqrt(dev2));
-        }
+        // the T blocks are checked on the device as they are assembled (check_tmats)
     }
     if (nk < 0 || (nk > 0 && !kpts)) return set_err(ctx, HSDLA_ERR_ARG, "bad k-point list");
     for (int i = 0; i < nk; ++i) {
@@ -364,27 +349,23 @@ int validate(hsdla_context *ctx, const hsdla_system *s, const hsdla_kpoint *kpts
     return HSDLA_OK;
 }
 
-// Hermitian full 2L x 2L block of one type from the lower triangles of T_AA/T_BB
-// (zhemm 'L' semantics, h_and_s_stripped_v2.cpp:202,345) and the full T_AB.
-// The Hermitian 2L x 2L block [[T_AA, T_AB], [T_AB^H, T_BB]] of type t (column-major, ld 2L) into
-// out, from the lower triangles of T_AA and T_BB and all of T_AB.
-void build_tfull(const hsdla_system *s, int t, int L, std::complex<double> *out) {
-    const int64_t LL = (int64_t)L * L, n = 2 * L;
-    const auto *aa = reinterpret_cast<const std::complex<double> *>(s->type_t_aa) + t * LL;
-    const auto *ab = reinterpret_cast<const std::complex<double> *>(s->type_t_ab) + t * LL;
-    const auto *bb = reinterpret_cast<const std::complex<double> *>(s->type_t_bb) + t * LL;
-    for (int c = 0; c < n; ++c) {
-        std::complex<double> *o = out + (size_t)n * c;
-        if (c < L) {
-            for (int r = 0; r < c; ++r) o[r] = std::conj(aa[c + L * r]);
-            for (int r = c; r < L; ++r) o[r] = aa[r + L * c];
-            for (int r = L; r < n; ++r) o[r] = std::conj(ab[c + L * (r - L)]);
-        } else {
-            for (int r = 0; r < L; ++r) o[r] = ab[r + L * (c - L)];
-            for (int r = L; r < c; ++r) o[r] = std::conj(bb[(c - L) + L * (r - L)]);
-            for (int r = c; r < n; ++r) o[r] = bb[(r - L) + L * (c - L)];
+// The T blocks' checks, made on the device while they were assembled (launch_tfull): finite
+// values, and T_AA and T_BB Hermitian (AtomData.cpp:138-139 asserts it), |T - T^H|^2 against
+// |T|^2 over the lower triangle (its mirror element is the pair's other half).
+int check_tmats(hsdla_context *ctx, const std::vector<unsigned long long> &st, int nt) {
+    auto as_double = [](unsigned long long b) { double d; memcpy(&d, &b, sizeof(d)); return d; };
+    for (int t = 0; t < nt; ++t) {
+        const unsigned long long fl = st[5 * (size_t)t];
+        for (int q = 0; q < 3; ++q)
+            if (fl & (1ull << q)) return set_err(ctx, HSDLA_ERR_INPUT, "T block %d of type %d not finite", q, t);
+        for (int q = 0; q < 2; ++q) {
+            const double mx2 = as_double(st[5 * (size_t)t + 1 + 2 * q]), dev2 = as_double(st[5 * (size_t)t + 2 + 2 * q]);
+            if (dev2 > 1e-24 * std::max(mx2, 1e-300))
+                return set_err(ctx, HSDLA_ERR_INPUT, "T_%s of type %d is not Hermitian (|T-T^H| = %.3g)",
+                               q == 0 ? "AA" : "BB", t, std::sqrt(dev2));
         }
     }
+    return HSDLA_OK;
 }
 
 template <typename T>
@@ -577,6 +558,7 @@ void hsdla_context_destroy(hsdla_context *ctx) {
     if (ctx->ws) ctx_free(ctx, ctx->ws, ctx->ws_bytes);
     if (ctx->hout) ctx_free(ctx, ctx->hout, ctx->hout_bytes);
     ctx_cache_release(ctx);
+    if (ctx->staging) cudaFreeHost(ctx->staging);
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
     if (ctx->ev_copy) cudaEventDestroy(ctx->ev_copy);
     if (ctx->copy_stream) cudaStreamDestroy(ctx->copy_stream);
@@ -676,15 +658,16 @@ int hsdla_plan_create(hsdla_context *ctx, const hsdla_system *s, const hsdla_kpo
             }
     }
     const size_t tf_elems = (size_t)nt * 4 * L * L;
+    const int64_t LLnt = (int64_t)nt * L * L;
 
-    // ---- one device block for all tables
+    // ---- one device block for all tables: the uploaded part, then what the device fills
     int64_t bytes = 0;
     auto add = [&](int64_t b) { bytes += (b + 255) & ~int64_t(255); };
     add(sizeof(int32_t) * na); add(sizeof(double) * 3 * na); add(s->atom_rotmat ? sizeof(double) * 9 * na : 0);
     add(sizeof(double) * nt); add(sizeof(int32_t) * nt);
     for (int q = 0; q < 5; ++q) add(sizeof(double) * nt * nl);
     add(sizeof(double) * L);
-    add(sizeof(double2) * tf_elems);
+    for (int q = 0; q < 3; ++q) add(sizeof(double2) * LLnt);     // T_AA, T_AB, T_BB as given
     add(sizeof(double) * pl->twoLa); add(sizeof(double) * pl->twoLa);
     for (int i = 0; i < nk; ++i) add(sizeof(int32_t) * 3 * kpts[i].n_g);
     // structure-factor form: per-type weights, per-atom phase factors along each axis, the atoms
@@ -698,18 +681,34 @@ int hsdla_plan_create(hsdla_context *ctx, const hsdla_system *s, const hsdla_kpo
                 for (int c = 0; c < 3; ++c) half[c] = std::max(half[c], 2 * std::abs(kpts[i].g[3 * q + c]));
         for (int c = 0; c < 3; ++c) ext[c] = 2 * half[c] + 1;
         add(sizeof(double) * 2 * L * nt);
-        add(sizeof(double2) * (int64_t)na * (ext[0] + ext[1] + ext[2]));
         add(sizeof(int32_t) * (na + nt + 1));
     }
-    // the structure-factor table comes last: it is filled on the device, not uploaded
     const int64_t upload_bytes = bytes;
-    if (pl->sf) add(sizeof(double2) * (int64_t)nt * ext[0] * ext[1] * ext[2]);
+    // filled on the device: the assembled T blocks and their checks; the structure-factor form's
+    // per-atom phase factors and its table
+    add(sizeof(double2) * tf_elems);
+    add(sizeof(unsigned long long) * 5 * nt);
+    if (pl->sf) {
+        add(sizeof(double2) * (int64_t)na * (ext[0] + ext[1] + ext[2]));
+        add(sizeof(double2) * (int64_t)nt * ext[0] * ext[1] * ext[2]);
+    }
     rc = ctx_malloc(ctx, &pl->tables, bytes);
     if (rc) { delete pl; return rc; }
     pl->tables_bytes = bytes;
-    // staging of the uploaded part (left uninitialised: every byte that matters is written)
-    std::unique_ptr<char[]> host(new char[std::max<int64_t>(upload_bytes, 1)]);
-    char *hp = host.get();
+    // staging of the uploaded part, page-locked and kept by the context (pageable if pinning
+    // fails); left uninitialised: every byte that matters is written
+    if (ctx->staging_bytes < upload_bytes) {
+        if (ctx->staging) cudaFreeHost(ctx->staging);
+        ctx->staging = nullptr;
+        ctx->staging_bytes = 0;
+        const int64_t want = std::max<int64_t>(upload_bytes, (int64_t)1 << 20);
+        if (cudaHostAlloc(&ctx->staging, (size_t)want, cudaHostAllocDefault) == cudaSuccess) ctx->staging_bytes = want;
+        else { cudaGetLastError(); ctx->staging = nullptr; }
+    }
+    std::unique_ptr<char[]> pageable;
+    char *stage = reinterpret_cast<char *>(ctx->staging);
+    if (!stage) { pageable.reset(new char[std::max<int64_t>(upload_bytes, 1)]); stage = pageable.get(); }
+    char *hp = stage;
     char *dp = reinterpret_cast<char *>(pl->tables);
     auto put = [&](const void *src, int64_t b) -> void * {
         void *d = dp;
@@ -733,9 +732,9 @@ int hsdla_plan_create(hsdla_context *ctx, const hsdla_system *s, const hsdla_kpo
     D.dE_u_dr = (const double *)put(s->type_dE_u_dr, sizeof(double) * nt * nl);
     D.inv_w = (const double *)put(inv_w.data(), sizeof(double) * nt * nl);
     D.ynorm = (const double *)put(yn.data(), sizeof(double) * L);
-    for (int t = 0; t < nt; ++t)
-        build_tfull(s, t, L, reinterpret_cast<std::complex<double> *>(hp) + (size_t)t * 4 * L * L);
-    pl->Tfull = (double2 *)put(nullptr, sizeof(double2) * tf_elems);
+    const double2 *d_taa = (const double2 *)put(s->type_t_aa, sizeof(double2) * LLnt);
+    const double2 *d_tab = (const double2 *)put(s->type_t_ab, sizeof(double2) * LLnt);
+    const double2 *d_tbb = (const double2 *)put(s->type_t_bb, sizeof(double2) * LLnt);
     pl->w = (double *)put(w.data(), sizeof(double) * pl->twoLa);
     pl->wsqrt = (double *)put(wsq.data(), sizeof(double) * pl->twoLa);
     for (int i = 0; i < nk; ++i) {
@@ -748,7 +747,7 @@ int hsdla_plan_create(hsdla_context *ctx, const hsdla_system *s, const hsdla_kpo
         const double G = (double)kpts[i].n_g;
         pl->flop += 20.0 * G * G * L * na + 24.0 * (double)L * L * na * G;
     }
-    const double2 *d_ex = nullptr;
+    double2 *d_ex = nullptr;
     const int32_t *d_order = nullptr;
     if (pl->sf) {
         std::vector<double> wt((size_t)2 * L * nt);
@@ -759,15 +758,6 @@ int hsdla_plan_create(hsdla_context *ctx, const hsdla_system *s, const hsdla_kpo
                     wt[(size_t)2 * L * t + L + lm] = (l <= s->type_lmax[t]) ? s->type_dE_u_norm[t * nl + l] : 0.0;
                 }
         pl->wt = (double *)put(wt.data(), sizeof(double) * wt.size());
-        std::vector<double2> ph((size_t)na * (ext[0] + ext[1] + ext[2]));
-        size_t o = 0;
-        for (int c = 0; c < 3; ++c)
-            for (int j = 0; j < na; ++j)
-                for (int i = 0; i < ext[c]; ++i) {
-                    const double ang = 2 * kPi * (double)(i - half[c]) * s->atom_pos[3 * j + c];
-                    ph[o++] = make_double2(std::cos(ang), std::sin(ang));
-                }
-        d_ex = (const double2 *)put(ph.data(), sizeof(double2) * ph.size());
         std::vector<int32_t> ord;
         std::vector<int32_t> tb(nt + 1, 0);
         for (int t = 0; t < nt; ++t) {
@@ -778,21 +768,41 @@ int hsdla_plan_create(hsdla_context *ctx, const hsdla_system *s, const hsdla_kpo
         tb[nt] = (int32_t)ord.size();
         ord.insert(ord.end(), tb.begin(), tb.end());
         d_order = (const int32_t *)put(ord.data(), sizeof(int32_t) * ord.size());
-        pl->sf_tab = (double2 *)dp;   // past the uploaded part
         SfTab &dm = pl->sf_dims;
         dm.dx = half[0]; dm.dy = half[1]; dm.dz = half[2];
         dm.ny = ext[1]; dm.nz = ext[2];
         dm.box = (int64_t)ext[0] * ext[1] * ext[2];
     }
-    cudaError_t e = cudaMemcpyAsync(pl->tables, host.get(), upload_bytes, cudaMemcpyHostToDevice, ctx->stream);
+    // past the uploaded part: what the device fills
+    auto dev_only = [&](int64_t b) -> void * {
+        void *d = dp;
+        dp += (b + 255) & ~int64_t(255);
+        return d;
+    };
+    pl->Tfull = (double2 *)dev_only(sizeof(double2) * tf_elems);
+    unsigned long long *d_stats = (unsigned long long *)dev_only(sizeof(unsigned long long) * 5 * nt);
+    if (pl->sf) {
+        d_ex = (double2 *)dev_only(sizeof(double2) * (int64_t)na * (ext[0] + ext[1] + ext[2]));
+        pl->sf_tab = (double2 *)dev_only(sizeof(double2) * (int64_t)nt * ext[0] * ext[1] * ext[2]);
+    }
+    std::vector<unsigned long long> tstats((size_t)5 * nt, 0);
+    cudaError_t e = cudaMemcpyAsync(pl->tables, stage, upload_bytes, cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(d_stats, 0, sizeof(unsigned long long) * 5 * nt, ctx->stream);
+    if (e == cudaSuccess) e = launch_tfull(d_taa, d_tab, d_tbb, nt, L, pl->Tfull, d_stats, ctx->stream);
+    if (e == cudaSuccess && pl->sf) e = launch_sf_phases(D.atom_pos, na, half, ext, d_ex, ctx->stream);
     if (e == cudaSuccess && pl->sf)
         e = launch_sf_table(d_ex, d_ex + (size_t)na * ext[0], d_ex + (size_t)na * (ext[0] + ext[1]), d_order,
                             d_order + na, nt, ext[0], ext[1], ext[2], pl->sf_tab, ctx->stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(tstats.data(), d_stats, sizeof(unsigned long long) * 5 * nt, cudaMemcpyDeviceToHost,
+                            ctx->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
     if (e != cudaSuccess) {
         hsdla_plan_destroy(pl);
         return set_err(ctx, HSDLA_ERR_CUDA, "table upload failed: %s", cudaGetErrorString(e));
     }
+    rc = check_tmats(ctx, tstats, nt);
+    if (rc) { hsdla_plan_destroy(pl); return rc; }
     if (pl->opts.precision == HSDLA_PREC_OZAKI_FP8) {
         pl->autotune = pl->opts.num_slices == 0;
         rc = ozaki_plan_init(pl->oz, pl->opts.num_slices, pl->opts.target_rel_err);
