@@ -20,26 +20,42 @@ __device__ __forceinline__ double2 cmul_d(double2 a, double2 b) {
 
 
 // sf[t][(ix ny + iy) nz + iz] = sum over the atoms of type t of ex[a][ix] ey[a][iy] ez[a][iz],
-// the atoms listed type by type (order[type_begin[t] .. type_begin[t+1])).
-__global__ void sf_table_kernel(const double2 *__restrict__ ex, const double2 *__restrict__ ey,
-                                const double2 *__restrict__ ez, const int32_t *__restrict__ order,
-                                const int32_t *__restrict__ type_begin, int nt, int nx, int ny, int nz,
-                                double2 *__restrict__ sf) {
-    const int64_t box = (int64_t)nx * ny * nz;
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < box * nt; i += (int64_t)gridDim.x * blockDim.x) {
-        const int t = (int)(i / box);
-        const int64_t e = i - (int64_t)t * box;
-        const int ix = (int)(e / ((int64_t)ny * nz));
-        const int iy = (int)((e / nz) % ny);
-        const int iz = (int)(e % nz);
+// the atoms listed type by type (order[type_begin[t] .. type_begin[t+1])).  One CTA per (ix, t):
+// the products ex ey of a chunk of atoms go to shared memory once per block of entries, and each
+// entry then costs one complex FMA per atom (FP64, the pipe that bounds this table).
+constexpr int kSfChunk = 16, kSfTabThreads = 256, kSfSmem = 48 * 1024;
+__global__ void __launch_bounds__(kSfTabThreads) sf_table_kernel(const double2 *__restrict__ ex,
+                                                                 const double2 *__restrict__ ey,
+                                                                 const double2 *__restrict__ ez,
+                                                                 const int32_t *__restrict__ order,
+                                                                 const int32_t *__restrict__ type_begin, int nx,
+                                                                 int ny, int nz, int chunk, double2 *__restrict__ sf) {
+    extern __shared__ double2 pxy[];            // [chunk][ny]
+    const int ix = blockIdx.x, t = blockIdx.y;
+    const int64_t nyz = (int64_t)ny * nz;
+    const int a0 = type_begin[t], a1 = type_begin[t + 1];
+    double2 *out = sf + ((int64_t)t * nx + ix) * nyz;
+    for (int64_t e0 = 0; e0 < nyz; e0 += blockDim.x) {
+        const int64_t e = e0 + threadIdx.x;
+        const int iy = (int)(e / nz), iz = (int)(e % nz);
         double2 acc = make_double2(0.0, 0.0);
-        for (int q = type_begin[t]; q < type_begin[t + 1]; ++q) {
-            const int a = order[q];
-            const double2 v = cmul_d(cmul_d(ex[(int64_t)a * nx + ix], ey[(int64_t)a * ny + iy]), ez[(int64_t)a * nz + iz]);
-            acc.x += v.x;
-            acc.y += v.y;
+        for (int c0 = a0; c0 < a1; c0 += chunk) {
+            const int nc = min(chunk, a1 - c0);
+            __syncthreads();
+            for (int w = threadIdx.x; w < nc * ny; w += blockDim.x) {
+                const int k = w / ny, y = w - k * ny;
+                const int a = order[c0 + k];
+                pxy[k * ny + y] = cmul_d(ex[(int64_t)a * nx + ix], ey[(int64_t)a * ny + y]);
+            }
+            __syncthreads();
+            if (e < nyz)
+                for (int k = 0; k < nc; ++k) {
+                    const double2 p = pxy[k * ny + iy], z = ez[(int64_t)order[c0 + k] * nz + iz];
+                    acc.x = fma(p.x, z.x, fma(-p.y, z.y, acc.x));
+                    acc.y = fma(p.x, z.y, fma(p.y, z.x, acc.y));
+                }
         }
-        sf[i] = acc;
+        if (e < nyz) out[e] = acc;
     }
 }
 
@@ -108,8 +124,12 @@ cudaError_t launch_sf_table(const double2 *ex, const double2 *ey, const double2 
                             const int32_t *type_begin, int nt, int nx, int ny, int nz, double2 *sf, cudaStream_t st) {
     const int64_t n = (int64_t)nx * ny * nz * nt;
     if (n <= 0) return cudaSuccess;
-    const int64_t blocks = std::min<int64_t>((n + 255) / 256, 65535);
-    sf_table_kernel<<<(unsigned)blocks, 256, 0, st>>>(ex, ey, ez, order, type_begin, nt, nx, ny, nz, sf);
+    // atoms per shared-memory chunk: kSfChunk, fewer for a long y extent
+    const int chunk = std::min<int>(kSfChunk, kSfSmem / (int)sizeof(double2) / std::max(ny, 1));
+    if (nx > 65535 || nt > 65535 || chunk < 1) return cudaErrorInvalidValue;
+    const size_t smem = sizeof(double2) * (size_t)chunk * ny;
+    sf_table_kernel<<<dim3((unsigned)nx, (unsigned)nt), kSfTabThreads, smem, st>>>(ex, ey, ez, order, type_begin, nx,
+                                                                                 ny, nz, chunk, sf);
     return cudaGetLastError();
 }
 
