@@ -142,6 +142,25 @@ def test_rejects_non_hermitian_taa(ctx):
     assert e.value.code == -4
 
 
+def test_rejects_non_hermitian_tbb_and_nonfinite_tab(ctx):
+    """The T blocks are checked on the device as they are assembled: T_BB not Hermitian, or a
+    non-finite value in T_AB, is an input error naming the block, and the context stays usable."""
+    s = synth.make_system("t0")
+    base = oracle.prepare_tmats(s)
+    tm = [x.copy() for x in base]
+    tm[2][1, 3, 1] += 0.25j
+    with pytest.raises(api.HsdlaError) as e:
+        ctx.create_hs(s, tmats=tuple(tm))
+    assert e.value.code == -4 and "T_BB of type 1 is not Hermitian" in str(e.value)
+    tm = [x.copy() for x in base]
+    tm[1][0, 2, 3] = np.nan
+    with pytest.raises(api.HsdlaError) as e:
+        ctx.create_hs(s, tmats=tuple(tm))
+    assert e.value.code == -4 and "T block 1 of type 0 not finite" in str(e.value)
+    res, _ = ctx.create_hs(s, tmats=base)
+    assert np.isfinite(res[0][0]).all()
+
+
 def test_memory_cap_reports_nomem(ctx):
     s = synth.make_system("c0")
     ctx.set_mem_cap(1 << 16)
