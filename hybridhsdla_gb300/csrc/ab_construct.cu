@@ -297,6 +297,99 @@ __global__ void __launch_bounds__(kThreads) construct_ab_kernel(DevSystem sys, c
     }
 }
 
+// Per-type rows M only (atoms sharing their type's rotation, no per-atom rows), kRowCols G columns
+// per CTA.  The per-column scalar work -- the Bessel recursions per type and the Y_lm sets, FP64
+// code with data-dependent loops -- runs one column per lane, as work items (column, type) and
+// (column, m), instead of on a few lanes of one warp per column: GB300 issues an FP64 warp
+// instruction in 16 cycles however few of its lanes are active.  The same formulas in the same
+// order as construct_ab_kernel, so M is the same to the bit.
+constexpr int kRowCols = 16;
+__global__ void __launch_bounds__(kThreads) construct_rows_kernel(DevSystem sys, const __grid_constant__ KTable tab) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int L = sys.L, nl = sys.max_lmax + 1, nt = sys.num_types, twoL = 2 * L, tnl = nt * nl;
+    double2 *ylm = reinterpret_cast<double2 *>(smem_raw);          // [kRowCols][L]
+    double *au = reinterpret_cast<double *>(ylm + kRowCols * L);    // [kRowCols][nt nl]
+    double *bu = au + kRowCols * tnl;                               // [kRowCols][nt nl]
+    double *cf = bu + kRowCols * tnl;                               // [nt nl] 4 pi / sqrt(Omega) / W
+    double *kv = cf + tnl;                                          // [kRowCols][4]: K, |bmat K|
+    unsigned char *l_of = reinterpret_cast<unsigned char *>(kv + 4 * kRowCols);   // [L]
+    for (int lm = threadIdx.x; lm < L; lm += blockDim.x) {
+        int l = (int)sqrt((double)lm);
+        while (l * l > lm) --l;
+        while ((l + 1) * (l + 1) <= lm) ++l;
+        l_of[lm] = (unsigned char)l;
+    }
+    for (int i = threadIdx.x; i < tnl; i += blockDim.x) cf[i] = sys.vol_prefac * sys.inv_w[i];
+    const int64_t ldm = tab.ldm;
+    for (int64_t col0 = blockIdx.x * (int64_t)kRowCols; col0 < tab.total_cols; col0 += (int64_t)gridDim.x * kRowCols) {
+        const int ncols = (int)(tab.total_cols - col0 < kRowCols ? tab.total_cols - col0 : kRowCols);
+        __syncthreads();
+        if (threadIdx.x < ncols) {
+            const int64_t gc = col0 + threadIdx.x;
+            const KEntry &ent = tab.e[entry_of(tab, gc)];
+            const int32_t *gv = ent.kp.g + 3 * (gc - ent.col_begin);
+            const double K[3] = {ent.kp.k[0] + gv[0], ent.kp.k[1] + gv[1], ent.kp.k[2] + gv[2]};
+            double s = 0.0;
+            for (int r = 0; r < 3; ++r) {
+                const double t = sys.bmat[3 * r] * K[0] + sys.bmat[3 * r + 1] * K[1] + sys.bmat[3 * r + 2] * K[2];
+                s += t * t;
+            }
+            double *k4 = kv + 4 * threadIdx.x;
+            k4[0] = K[0]; k4[1] = K[1]; k4[2] = K[2]; k4[3] = sqrt(s);
+        }
+        __syncthreads();
+        // the columns' Bessel values per type, then their Y_lm sets (one warp per kind, mostly)
+        const int nb = ncols * nt, ny = ncols * nl;
+        for (int w = threadIdx.x; w < nb + ny; w += blockDim.x) {
+            if (w < nb) {
+                const int c = w / nt, t = w - c * nt;
+                const double kn = kv[4 * c + 3];
+                double fj[kMaxLmax + 1], dfj[kMaxLmax + 1];
+                const double x = sys.type_rmt[t] * kn;
+                sphbes_dev(sys.max_lmax, x, fj);
+                dsphbs_dev(sys.max_lmax, x, fj, dfj);
+                for (int l = 0; l < nl; ++l) {
+                    const int tl = t * nl + l;
+                    au[c * tnl + tl] = sys.dE_u[tl] * kn * dfj[l] - sys.dE_u_dr[tl] * fj[l];
+                    bu[c * tnl + tl] = -sys.u[tl] * kn * dfj[l] + sys.u_dr[tl] * fj[l];
+                }
+            } else {
+                const int q = w - nb, c = q / nl, m = q - c * nl;
+                const double *k4 = kv + 4 * c;
+                double v[3];
+                for (int d = 0; d < 3; ++d) v[d] = sys.bmat[d] * k4[0] + sys.bmat[3 + d] * k4[1] + sys.bmat[6 + d] * k4[2];
+                const double nrm = sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+                if (nrm > 0.0) { v[0] /= nrm; v[1] /= nrm; v[2] /= nrm; }
+                ylm_column_dev(sys.max_lmax, m, v, sys.ynorm, ylm + c * L);
+            }
+        }
+        __syncthreads();
+        // the rows M_t = [A_t; B_t] / e^{i 2pi K.tau} of each column
+        for (int c = 0; c < ncols; ++c) {
+            const int64_t gc = col0 + c;
+            const KEntry &ent = tab.e[entry_of(tab, gc)];
+            if (!ent.M) continue;
+            double2 *mcol = ent.M + ldm * (gc - ent.col_begin);
+            for (int idx = threadIdx.x; idx < twoL * nt; idx += blockDim.x) {
+                const int t = idx / twoL;
+                const int r = idx - t * twoL;
+                const bool isB = r >= L;
+                const int lm = isB ? r - L : r;
+                const int l = l_of[lm];
+                double2 out = make_double2(0.0, 0.0);
+                if (l <= sys.type_lmax[t]) {
+                    const int tl = t * nl + l;
+                    const double cc = cf[tl];
+                    const double2 y = ylm[c * L + lm];
+                    const double f = isB ? bu[c * tnl + tl] : au[c * tnl + tl];
+                    out = make_double2((y.x * cc) * f, (-y.y * cc) * f);
+                }
+                mcol[idx] = out;
+            }
+        }
+    }
+}
+
 }  // namespace
 
 // X[2L a + r, g] = e^{i 2pi (k+g).tau_a} Z[2L t(a) + r, g]: the per-atom T application rebuilt
@@ -460,9 +553,22 @@ cudaError_t launch_construct_ab(const DevSystem &sys, const DevKpoint &kp, doubl
 
 cudaError_t launch_construct_ab_multi(const DevSystem &sys, const KTable &tab, cudaStream_t st) {
     if (tab.total_cols <= 0) return cudaSuccess;
-    bool anyM = false;
-    for (int k = 0; k < tab.nk; ++k) anyM = anyM || tab.e[k].M;
+    bool anyM = false, anyC = false;
+    for (int k = 0; k < tab.nk; ++k) { anyM = anyM || tab.e[k].M; anyC = anyC || tab.e[k].C; }
     const bool rot = sys.atom_rotmat != nullptr;
+    const int nl_ = sys.max_lmax + 1, tnl_ = sys.num_types * nl_;
+    size_t smem_rows = sizeof(double2) * kRowCols * sys.L +
+                       sizeof(double) * (2 * kRowCols * tnl_ + tnl_ + 4 * kRowCols) + sys.L + 16;
+    smem_rows = (smem_rows + 15) & ~size_t(15);
+    // (the column-per-CTA kernel below for many types at a high lmax, whose tables do not fit)
+    if (!rot && anyM && !anyC && smem_rows <= 160 * 1024) {
+        const size_t smem = smem_rows;
+        cudaError_t e = cudaFuncSetAttribute(construct_rows_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        const int64_t grid = std::min<int64_t>((tab.total_cols + kRowCols - 1) / kRowCols, (int64_t)sm_count() * 4);
+        construct_rows_kernel<<<(unsigned)grid, kThreads, smem, st>>>(sys, tab);
+        return cudaGetLastError();
+    }
     const int nl = sys.max_lmax + 1;
     size_t smem = sizeof(double) * 2 * sys.num_types * nl + sizeof(double2) * sys.num_atoms +
                   sizeof(double2) * (rot ? kRotChunk : 1) * sys.L + sys.L + 16;
