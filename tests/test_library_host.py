@@ -40,6 +40,23 @@ def test_struct_layouts_match_header():
     assert ctypes.sizeof(api.ReportStruct) == 10 * 8 + 8 * 4
 
 
+def _header_fields(struct_name):
+    txt = open(os.path.join(ROOT, "include", "hsdla.h")).read()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    body = re.search(r"typedef struct %s \{(.*?)\}" % struct_name, txt, flags=re.S).group(1)
+    names = []
+    for decl in body.split(";"):
+        decl = decl.strip()
+        if decl:
+            names += [re.sub(r"\[.*\]", "", v).strip(" *") for v in decl.split(None, 1)[1].split(",")]
+    return names
+
+
+def test_report_fields_match_header():
+    """The report's fields in the header's order (the Python mirror reads them by position)."""
+    assert [f for f, _ in api.ReportStruct._fields_] == _header_fields("hsdla_report")
+
+
 @pytest.mark.parametrize("cfg", ["t0", "t1", "c0"])
 def test_prepare_tmat_matches_oracle(cfg):
     s = synth.make_system(cfg)
