@@ -330,7 +330,7 @@ def run_ours(args):
                 "config": {"workload": WORKLOAD_TEXT.get(args.workload, args.workload),
                            "precision": f"ozaki-fp8 e4m3, {rep['num_slices']} digit slices",
                            "kpoints_per_rank": len(kps), "ms_per_kpoint": ms / len(kps),
-                           "l2": "inputs larger than L2 (c2: 1.6 GB of digit planes, 16 GB of per-type products)",
+                           "l2": "inputs larger than L2 (digit planes and per-type products: GBs per k-point; c2 1.6 GB and 16 GB)",
                            "parallelism": f"replicas{ws}"},
                 "e2e": {"value": ws * e2e_flop / e2e_s / 1e12, "unit": UNIT, "ms_per_kpoint": e2e_s * 1e3,
                         "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
