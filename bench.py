@@ -145,16 +145,31 @@ def shard_kpoints(kpoints, rank: int, world: int):
     return list(kpoints)[rank::world]
 
 
+def rank_kpoints(kpoints, rank: int, world: int):
+    """A batched workload's k-points are split over the replicas; a single-k-point workload runs
+    one full copy per replica (weak scaling)."""
+    return shard_kpoints(kpoints, rank, world) if len(kpoints) > 1 else list(kpoints)
+
+
+def bench_config(workload: str, ws: int, kpoints_per_rank: int) -> dict:
+    """The workload both arms report (the reference arm prints the same dict)."""
+    return {"workload": WORKLOAD_TEXT.get(workload, workload), "kpoints_per_rank": kpoints_per_rank,
+            "l2": "inputs larger than L2 (digit planes and per-type products: GBs per k-point; c2 1.6 GB and 16 GB)",
+            "parallelism": f"replicas{ws}"}
+
+
 def cpu_reference_step(sys_, n_g_sample: int, threads: int):
-    """One bounded sample of the reference CPU path: the c2 system with the basis
-    truncated to its first n_g_sample G-vectors.  Returns (seconds, flop)."""
+    """The reference CPU path (construct_AB + the create_HS2_stripped_v2 BLAS sequence) on the
+    workload's first k-point with its basis truncated to the first n_g_sample G-vectors (all of
+    them when n_g_sample >= n_G).  Returns (seconds, flop)."""
     import oracle
     from hybridhsdla_gb300 import synth
     kp = sys_.kpoints[0]
-    sub = synth.KPoint(k=kp.k, g=kp.g[:n_g_sample])
+    n = min(n_g_sample, kp.n_g)
+    sub = kp if n == kp.n_g else synth.KPoint(k=kp.k, g=kp.g[:n])
     t0 = time.perf_counter()
     oracle.reference_hs(sys_, sub, nthreads=threads)
-    return time.perf_counter() - t0, sys_.flop_per_kpoint(n_g_sample)
+    return time.perf_counter() - t0, sys_.flop_per_kpoint(n)
 
 
 def run_reference(args):
@@ -165,7 +180,7 @@ def run_reference(args):
     import oracle
     from hybridhsdla_gb300 import synth
     threads = oracle.nthreads_default()
-    sys_ = synth.make_system(WORKLOAD)
+    sys_ = synth.make_system(args.workload)
     ng = args.ref_sample_ng
     for _ in range(args.warmup):
         cpu_reference_step(sys_, ng, threads)
@@ -175,12 +190,15 @@ def run_reference(args):
         tot_s += s
         tot_f += f
     v = tot_f / tot_s / 1e12
-    sample = f"c2 system (128 atoms, lmax 10) with the basis truncated to its first {ng} of 8000 G-vectors"
+    kp0 = sys_.kpoints[0]
+    sample = (f"each step: the workload's first k-point with its basis truncated to the first "
+              f"{min(ng, kp0.n_g)} of its {kp0.n_g} G-vectors (full contraction length, {sys_.num_atoms} atoms, "
+              f"lmax {sys_.max_lmax}); rate = canonical flops of the sample / its time")
     line = {"metric": METRIC, "value": v, "unit": UNIT, "impl": "reference", "n_gpus": ws,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tot_s / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic (seeded)", "config": {"workload": "c2 sample", "n_g_sample": ng,
-                                                      "atoms": 128, "lmax": 10},
+            "data": "synthetic (seeded generators, no dataset)",
+            "config": bench_config(args.workload, ws, len(rank_kpoints(sys_.kpoints, 0, ws))),
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -204,7 +222,7 @@ def run_ours(args):
     batched = len(sys_.kpoints) > 1
     # replicas over k-points: rank r takes k-points r, r + N, ... of a batched workload (weak
     # scaling keeps one full copy of a single-k-point workload per rank)
-    kps = shard_kpoints(sys_.kpoints, rank, ws) if batched else sys_.kpoints
+    kps = rank_kpoints(sys_.kpoints, rank, ws)
     kp = kps[0]
     G = kp.n_g
     flop = sum(sys_.flop_per_kpoint(k.n_g) for k in kps)
@@ -244,14 +262,15 @@ def run_ours(args):
     tmats = api.prepare_tmats(sys_)
     ctx.create_hs(sys_, kpoints=[kp], precision="ozaki", num_slices=args.slices, tmats=tmats, out=outs_h)  # warm
     torch.cuda.synchronize()
-    e2e_steps = max(1, min(args.steps, 5))
-    e2e_calls = []
+    e2e_steps = max(1, min(args.steps, args.e2e_calls))
+    e2e_calls, e2e_dev = [], []
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
         tc = time.perf_counter()
         _, rep_e = ctx.create_hs(sys_, kpoints=[kp], precision="ozaki", num_slices=args.slices, tmats=tmats,
                                  out=outs_h)
         e2e_calls.append((time.perf_counter() - tc) * 1e3)
+        e2e_dev.append(rep_e["ms_total"])
     e2e_s = (time.perf_counter() - t0) / e2e_steps
     e2e_s = _max_over_ranks(ws, e2e_s)
     e2e_flop = sys_.flop_per_kpoint(G)
@@ -266,11 +285,13 @@ def run_ours(args):
 
     # ---- plain FP64 path on the first k-point, and the Ozaki error against it
     fp64 = None
+    S64 = H64 = None
     if not args.skip_fp64 and rank == 0:
         pl64 = ctx.plan(sys_, kpoints=[kp], precision="fp64")
         o64 = pl64.alloc_outputs()
         r64 = pl64.execute(o64)
         torch.cuda.synchronize()
+        H64, S64 = o64[0][0], o64[0][1]
 
         def errs(X, R):
             Xl = torch.tril(X.transpose(0, 1))
@@ -286,20 +307,36 @@ def run_ours(args):
         pl64.close()
         del o64
 
-    # ---- oracle check of the first k-point's top-left N x N block: A and B columns depend on their
-    # own G-vector only, so the oracle on the first N G-vectors gives exactly that block of H and S
+    # ---- oracle checks of the first k-point at its full contraction length: an H or S element
+    # depends only on the A and B columns of its own two G-vectors, so the oracle run on a subset
+    # of the G-vectors gives exactly the sub-matrix H[sub, sub], S[sub, sub] (sub in ascending
+    # order keeps the lower triangle lower).  Two subsets: the leading block and a seeded random one.
     block = None
     if args.oracle_block > 0 and rank == 0:
         import oracle
         nb = min(args.oracle_block, G)
-        sub = synth.KPoint(k=kp.k, g=kp.g[:nb])
-        Hr, Sr = oracle.reference_hs(sys_, sub)
-        Hb = np.tril(H_oz[:nb, :nb].cpu().numpy().T)
-        Sb = np.tril(S_oz[:nb, :nb].cpu().numpy().T)
-        block = {"n": nb}
-        for nm, X, R in (("H", Hb, Hr), ("S", Sb, Sr)):
-            fro, mx = oracle.lower_errors(X, R)
-            block[nm + "_fro"], block[nm + "_max"] = fro, mx
+        rng = np.random.default_rng(1234)
+        subsets = {"leading": np.arange(nb), "random": np.sort(rng.choice(G, nb, replace=False))}
+        block = {"n": nb, "note": "relative Frobenius / max-norm error of the lower triangle of H[sub, sub] and "
+                                  "S[sub, sub] against the oracle run on those G-vectors (full contraction length)"}
+        for sname, idx in subsets.items():
+            sub = synth.KPoint(k=kp.k, g=kp.g[idx])
+            t_or = time.perf_counter()
+            Hr, Sr = oracle.reference_hs(sys_, sub)
+            t_or = time.perf_counter() - t_or
+            ti = torch.from_numpy(idx).to(H_oz.device)
+            for prec, Hd, Sd in (("ozaki", H_oz, S_oz), ("fp64", H64, S64)):
+                if Hd is None:
+                    continue
+                ent = block.setdefault(prec, {}).setdefault(sname, {})
+                for nm, Xd, R in (("H", Hd, Hr), ("S", Sd, Sr)):
+                    X = np.tril(Xd.index_select(0, ti).index_select(1, ti).cpu().numpy().T)
+                    fro, mx = oracle.lower_errors(X, R)
+                    ent[nm + "_fro"], ent[nm + "_max"] = fro, mx
+            block.setdefault("oracle_s", {})[sname] = round(t_or, 2)
+        worst = max(v for p in ("ozaki", "fp64") for e in block.get(p, {}).values() for v in e.values())
+        block["max_err"] = worst
+        block["within_1e-13"] = worst <= 1e-13
 
     peaks, src = _peaks()
     fp8_peak = 2.0 * peaks["bf16_tflops"]
@@ -319,22 +356,31 @@ def run_ours(args):
         threads = oracle.nthreads_default()
         cpu_reference_step(sys_, args.ref_sample_ng, threads)       # warm
         s_, f_ = cpu_reference_step(sys_, args.ref_sample_ng, threads)
-        cpu = {"value": f_ / s_ / 1e12, "unit": UNIT, "cores": threads, "kind": "port",
-               "sample": f"c2 system with the basis truncated to its first {args.ref_sample_ng} G-vectors, "
-                         f"{s_:.1f} s"}
+        samp = {"value": f_ / s_ / 1e12, "seconds": round(s_, 2),
+                "sample": f"first k-point with its basis truncated to the first {min(args.ref_sample_ng, G)} "
+                          f"G-vectors (the reference arm's step)"}
+        if args.cpu_full:
+            sf_, ff_ = cpu_reference_step(sys_, G, threads)
+            cpu = {"value": ff_ / sf_ / 1e12, "unit": UNIT, "cores": threads, "kind": "port",
+                   "sample": f"one full k-point of the workload (n_G {G}, all {sys_.num_atoms} atoms, lmax "
+                             f"{sys_.max_lmax}): {sf_:.1f} s", "ms_per_kpoint": sf_ * 1e3,
+                   "truncated_sample": samp}
+        else:
+            cpu = {"value": samp["value"], "unit": UNIT, "cores": threads, "kind": "port",
+                   "sample": samp["sample"] + f", {s_:.1f} s"}
 
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded generators, no dataset)",
-                "config": {"workload": WORKLOAD_TEXT.get(args.workload, args.workload),
-                           "precision": f"ozaki-fp8 e4m3, {rep['num_slices']} digit slices",
-                           "kpoints_per_rank": len(kps), "ms_per_kpoint": ms / len(kps),
-                           "l2": "inputs larger than L2 (digit planes and per-type products: GBs per k-point; c2 1.6 GB and 16 GB)",
-                           "parallelism": f"replicas{ws}"},
+                "config": bench_config(args.workload, ws, len(kps)),
+                "precision": f"ozaki-fp8 e4m3, {rep['num_slices']} digit slices",
+                "ms_per_kpoint": ms / len(kps),
                 "e2e": {"value": ws * e2e_flop / e2e_s / 1e12, "unit": UNIT, "ms_per_kpoint": e2e_s * 1e3,
                         "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                         "calls_ms": [round(x, 2) for x in e2e_calls],
+                        "calls_device_ms": [round(x, 2) for x in e2e_dev],
+                        "median_ms": float(np.median(e2e_calls)),
                         "outputs": "written in place by the last combine" if rep_e["outputs_in_place"]
                         else "downloaded by the copy engine",
                         "note": "hsdla_create_hs on the rank's first k-point, pinned host buffers; "
@@ -362,8 +408,12 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--slices", type=int, default=0, help="Ozaki digit slices (0 = default)")
     ap.add_argument("--ref-sample-ng", type=int, default=3200)   # ~11 s of CPU work per step
-    ap.add_argument("--oracle-block", type=int, default=0,
-                    help="compare the first k-point's top-left N x N block of H and S with the oracle")
+    ap.add_argument("--oracle-block", type=int, default=1024,
+                    help="compare N x N sub-matrices of the first k-point's H and S (the leading block and a "
+                         "seeded random subset of G-vectors) with the oracle; 0 = off")
+    ap.add_argument("--cpu-full", type=int, default=1,
+                    help="1: time the reference CPU path on one full k-point of the workload once")
+    ap.add_argument("--e2e-calls", type=int, default=8, help="end-to-end calls through hsdla_create_hs")
     ap.add_argument("--skip-fp64", action="store_true")
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--workload", default=WORKLOAD, choices=sorted(WORKLOAD_TEXT),

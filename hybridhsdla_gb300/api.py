@@ -356,7 +356,7 @@ def zherkx_lower_noalloc(P, Q=None, w=None, num_slices=0, out=None, stream=None)
                                        ctypes.c_void_p(w.data_ptr()) if w is not None else None,
                                        ctypes.c_void_p(out.data_ptr()), n, st)
     if rc != 0:
-        raise HsdlaError(rc, "hsdla_zherkx_lower_noalloc failed")
+        raise HsdlaError(rc, L_.hsdla_last_error(None).decode())
     return out
 
 

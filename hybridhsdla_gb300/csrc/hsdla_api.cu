@@ -12,6 +12,7 @@
 // codes with a message in the context (the reference prints and exits,
 // h_and_s.cpp:712-723).
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <complex>
 #include <cstdarg>
@@ -101,6 +102,8 @@ struct hsdla_plan {
         // event pairs around the S/H product launches (one pair, or one per type in the
         // structure-factor form; recorded under graph capture too)
         std::vector<cudaEvent_t> ev_dom;
+        // event pairs around the T-application launches (un-graphed runs; the report's ms_tapply)
+        std::vector<cudaEvent_t> ev_t;
         SfTab sft{};                     // structure-factor combine of this group (outputs per run)
     };
     std::vector<Group> groups;
@@ -568,7 +571,9 @@ void hsdla_context_destroy(hsdla_context *ctx) {
     delete ctx;
 }
 
-const char *hsdla_last_error(const hsdla_context *ctx) { return ctx ? ctx->err.c_str() : "no context"; }
+// With a context: its last message.  Without one: the calling thread's last message of an entry
+// point that takes no context (hsdla_zherkx_lower_noalloc).
+const char *hsdla_last_error(const hsdla_context *ctx) { return ctx ? ctx->err.c_str() : ozaki_last_error(); }
 
 int hsdla_set_mem_cap(hsdla_context *ctx, int64_t bytes) {
     if (!ctx || bytes < 0) return HSDLA_ERR_ARG;
@@ -934,6 +939,8 @@ void release_groups(hsdla_plan *pl) {
         if (g.persist) ctx_free(pl->ctx, g.persist, g.persist_bytes);
         for (auto &e : g.ev_dom) if (e) cudaEventDestroy(e);
         g.ev_dom.clear();
+        for (auto &e : g.ev_t) if (e) cudaEventDestroy(e);
+        g.ev_t.clear();
         g.oz = nullptr;
         g.h_jobs_sh = nullptr;
         g.persist = nullptr;
@@ -1014,7 +1021,11 @@ int prepare_groups(hsdla_plan *pl, void *ws, cudaStream_t st) {
             char *oz_ws = reinterpret_cast<char *>((reinterpret_cast<uintptr_t>(p) + 1023) & ~uintptr_t(1023));
             int rc = ozaki_group_prepare(pl->oz, d, kb, oz_ws, g.persist, st, &g.oz);
             if (rc) return set_err(ctx, rc, "group set-up failed: %s", ozaki_last_error());
+            g.ev_t.assign(2 * ozaki_group_tapply_events(g.oz), nullptr);
+            for (auto &e : g.ev_t) CUDA_TRY(ctx, cudaEventCreate(&e));
         } else {
+            g.ev_t.assign(2, nullptr);
+            for (auto &e : g.ev_t) CUDA_TRY(ctx, cudaEventCreate(&e));
             std::vector<Fp64Job> jt, jsh;
             for (int q = 0; q < kt.nk; ++q) {
                 const KEntry &e = kt.e[q];
@@ -1221,7 +1232,7 @@ int combine_last(hsdla_plan *pl, hsdla_plan::Group &g, int t0, int ntypes, cudaS
 }
 
 // Enqueue every group's launches (no host synchronisation: capturable in a CUDA graph).
-int run_groups(hsdla_plan *pl, cudaStream_t st, bool timed, float *ms_ab, float *ms_dom, double *dom_flop) {
+int run_groups(hsdla_plan *pl, cudaStream_t st, bool timed, float *ms_ab, float *ms_tap, double *dom_flop) {
     hsdla_context *ctx = pl->ctx;
     pl->launches = 0;
     if (dom_flop) *dom_flop = 0.0;
@@ -1245,8 +1256,8 @@ int run_groups(hsdla_plan *pl, cudaStream_t st, bool timed, float *ms_ab, float 
         }
         if (g.oz) {
             int nl = 0;
-            const int rc =
-                ozaki_group_run(g.oz, pl->dsys, g.ktab, st, g.ev_dom.data(), (int)g.ev_dom.size(), &nl, defer);
+            const int rc = ozaki_group_run(g.oz, pl->dsys, g.ktab, st, g.ev_dom.data(), (int)g.ev_dom.size(), &nl,
+                                           defer, timed ? g.ev_t.data() : nullptr, timed ? (int)g.ev_t.size() : 0);
             if (rc) return set_err(ctx, rc, "Ozaki group failed: %s", ozaki_last_error());
             pl->launches += nl;
             if (defer) {
@@ -1255,7 +1266,9 @@ int run_groups(hsdla_plan *pl, cudaStream_t st, bool timed, float *ms_ab, float 
                 if (rcc) return rcc;
             }
         } else if (pl->sf) {
+            if (timed) CUDA_TRY(ctx, cudaEventRecord(g.ev_t[0], st));
             CUDA_TRY(ctx, launch_fp64_jobs(g.d_jobs_t, g.n_jobs_t, g.tiles_t, st));
+            if (timed) CUDA_TRY(ctx, cudaEventRecord(g.ev_t[1], st));
             pl->launches++;
             const int nj = 2 * g.ktab.nk;
             for (int t = 0; t < pl->nt; ++t) {
@@ -1278,7 +1291,9 @@ int run_groups(hsdla_plan *pl, cudaStream_t st, bool timed, float *ms_ab, float 
                 }
             }
         } else {
+            if (timed) CUDA_TRY(ctx, cudaEventRecord(g.ev_t[0], st));
             CUDA_TRY(ctx, launch_fp64_jobs(g.d_jobs_t, g.n_jobs_t, g.tiles_t, st));
+            if (timed) CUDA_TRY(ctx, cudaEventRecord(g.ev_t[1], st));
             pl->launches++;
             if (pl->hoist) {
                 CUDA_TRY(ctx, launch_apply_phase_multi(pl->dsys, g.ktab, st));
@@ -1297,6 +1312,11 @@ int run_groups(hsdla_plan *pl, cudaStream_t st, bool timed, float *ms_ab, float 
             float a = 0;
             cudaEventElapsedTime(&a, ctx->evs[0], ctx->evs[1]);
             *ms_ab += a;
+            for (size_t i = 0; ms_tap && i + 1 < g.ev_t.size(); i += 2) {
+                float b = 0;
+                if (cudaEventElapsedTime(&b, g.ev_t[i], g.ev_t[i + 1]) == cudaSuccess) *ms_tap += b;
+            }
+            cudaGetLastError();
         }
     }
     return HSDLA_OK;
@@ -1373,7 +1393,7 @@ int hsdla_plan_execute(hsdla_plan *pl, hsdla_cx *const *dH, hsdla_cx *const *dS,
         if (rc) { release_groups(pl); return rc; }
     }
     set_outputs(pl, dH, dS, ld);
-    float ms_ab = 0.f, ms_dom = 0.f;
+    float ms_ab = 0.f, ms_tap = 0.f;
     double dom_flop = 0.0;
     const bool want_graph = pl->opts.use_graph != 0 && !pl->graph_failed;
     cudaStream_t run_st = want_graph && st == nullptr ? ctx->stream : st;   // the legacy stream cannot capture
@@ -1413,11 +1433,11 @@ int hsdla_plan_execute(hsdla_plan *pl, hsdla_cx *const *dH, hsdla_cx *const *dS,
             CUDA_TRY(ctx, cudaGraphLaunch(pl->graph, run_st));
             if (dom_flop == 0.0) run_groups_flop(pl, &dom_flop);
         } else {
-            rc = run_groups(pl, run_st, true, &ms_ab, &ms_dom, &dom_flop);
+            rc = run_groups(pl, run_st, true, &ms_ab, &ms_tap, &dom_flop);
             if (rc) return rc;
         }
     } else {
-        rc = run_groups(pl, run_st, true, &ms_ab, &ms_dom, &dom_flop);
+        rc = run_groups(pl, run_st, true, &ms_ab, &ms_tap, &dom_flop);
         if (rc) return rc;
     }
     CUDA_TRY(ctx, cudaEventRecord(ctx->evs[3], run_st));
@@ -1438,7 +1458,8 @@ int hsdla_plan_execute(hsdla_plan *pl, hsdla_cx *const *dH, hsdla_cx *const *dS,
         rep->flop = pl->flop;
         rep->eff_tflops = ms > 0 ? pl->flop / (ms * 1e-3) / 1e12 : 0.0;
         rep->ms_construct_ab = ms_ab;
-        rep->ms_contract = ms - ms_ab;
+        rep->ms_tapply = ms_tap;
+        rep->ms_contract = ms - ms_ab - ms_tap;
         rep->ms_dominant = dominant_ms(pl);
         rep->dominant_flop = dom_flop;
         rep->num_slices = pl->opts.precision == HSDLA_PREC_OZAKI_FP8 ? pl->oz.num_slices : 0;
@@ -1573,9 +1594,9 @@ int hsdla_contract_ab(hsdla_context *ctx, int32_t L, int32_t a, int64_t G, const
                           cudaMemcpyHostToDevice, st) != cudaSuccess)
         return done(set_err(ctx, HSDLA_ERR_CUDA, "A/B upload failed"));
     set_outputs(pl, &dH, &dS, &ldd);
-    float ms_ab = 0.f, ms_dom = 0.f;
+    float ms_ab = 0.f, ms_tap = 0.f;
     double dom_flop = 0.0;
-    rc = run_groups(pl, st, true, &ms_ab, &ms_dom, &dom_flop);
+    rc = run_groups(pl, st, true, &ms_ab, &ms_tap, &dom_flop);
     if (rc) return done(rc);
     if (download_lower(H, ld, dH, G, st) != cudaSuccess || download_lower(S, ld, dS, G, st) != cudaSuccess)
         return done(set_err(ctx, HSDLA_ERR_CUDA, "H/S download failed"));
@@ -1592,6 +1613,7 @@ int hsdla_contract_ab(hsdla_context *ctx, int32_t L, int32_t a, int64_t G, const
         rep->num_kpoints = 1;
         rep->flop = pl->flop;
         rep->eff_tflops = ms > 0 ? pl->flop / (ms * 1e-3) / 1e12 : 0.0;
+        rep->ms_tapply = ms_tap;
         rep->ms_dominant = dominant_ms(pl);
         rep->dominant_flop = dom_flop;
         rep->num_slices = pl->opts.precision == HSDLA_PREC_OZAKI_FP8 ? pl->oz.num_slices : 0;
@@ -1610,12 +1632,19 @@ int hsdla_create_hs(hsdla_context *ctx, const hsdla_system *s, const hsdla_kpoin
         if (kpts && kpts[i].n_g > 0 && (!H[i] || !S[i] || ld[i] < kpts[i].n_g))
             return set_err(ctx, HSDLA_ERR_ARG, "k-point %d: bad output buffer or ld", i);
     CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+    // HSDLA_TRACE=1: host-side phase times of each call on stderr
+    const bool trace = env_flag("HSDLA_TRACE", false);
+    using clk = std::chrono::steady_clock;
+    const auto ms_since = [](clk::time_point a) { return std::chrono::duration<double, std::milli>(clk::now() - a).count(); };
+    const clk::time_point t_start = clk::now();
+    double t_plan = 0, t_setup = 0, t_exec = 0, t_sync = 0;
     cudaEvent_t e0, e1;
     CUDA_TRY(ctx, cudaEventCreate(&e0));
     CUDA_TRY(ctx, cudaEventCreate(&e1));
     cudaEventRecord(e0, ctx->stream);
     hsdla_plan *pl = nullptr;
     int rc = hsdla_plan_create(ctx, s, kpts, nk, opts, &pl);
+    t_plan = ms_since(t_start);
     if (rc) { cudaEventDestroy(e0); cudaEventDestroy(e1); return rc; }
     // device outputs: one buffer of the largest size, reused per k-point group
     std::vector<int64_t> ng(nk);
@@ -1661,10 +1690,12 @@ int hsdla_create_hs(hsdla_context *ctx, const hsdla_system *s, const hsdla_kpoin
             }
         }
     }
+    t_setup = ms_since(t_start) - t_plan;
     if (e == cudaSuccess) {
         pl->dl = &dl;
         rc = hsdla_plan_execute(pl, dH.data(), dS.data(), dld.data(), ctx->stream, rep);
         pl->dl = nullptr;
+        t_exec = ms_since(t_start) - t_plan - t_setup;
     } else {
         rc = set_err(ctx, HSDLA_ERR_CUDA, "memset failed: %s", cudaGetErrorString(e));
     }
@@ -1682,18 +1713,26 @@ int hsdla_create_hs(hsdla_context *ctx, const hsdla_system *s, const hsdla_kpoin
     }
     cudaEventRecord(e1, ctx->stream);
     cudaError_t es = cudaStreamSynchronize(ctx->stream);
+    t_sync = ms_since(t_start) - t_plan - t_setup - t_exec;
+    float ms_dev = 0.f;
+    if (es == cudaSuccess) cudaEventElapsedTime(&ms_dev, e0, e1);
     if (rc == HSDLA_OK && es != cudaSuccess) rc = set_err(ctx, HSDLA_ERR_CUDA, "sync failed: %s", cudaGetErrorString(es));
     if (rc == HSDLA_OK && rep) {
-        float ms = 0.f;
-        cudaEventElapsedTime(&ms, e0, e1);
-        rep->ms_total = ms;   // end-to-end: upload, compute, download
-        rep->ms_per_kpoint = nk ? ms / nk : 0.0;
-        rep->eff_tflops = ms > 0 ? pl->flop / (ms * 1e-3) / 1e12 : 0.0;
+        rep->ms_total = ms_dev;   // end-to-end: upload, compute, download
+        rep->ms_per_kpoint = nk ? ms_dev / nk : 0.0;
+        rep->eff_tflops = ms_dev > 0 ? pl->flop / (ms_dev * 1e-3) / 1e12 : 0.0;
         rep->outputs_in_place = dl.in_place ? 1 : 0;
     }
+    const clk::time_point t_destroy = clk::now();
     hsdla_plan_destroy(pl);
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
+    if (trace)
+        fprintf(stderr,
+                "hsdla_create_hs: plan %.2f ms, set-up %.2f ms, execute %.2f ms, sync %.2f ms, destroy %.2f ms; "
+                "device %.2f ms; in place %d; context holds %lld B (%lld B kept for reuse)\n",
+                t_plan, t_setup, t_exec, t_sync, ms_since(t_destroy), ms_dev, dl.in_place ? 1 : 0,
+                (long long)ctx->mem_used, (long long)ctx->cached_bytes);
     return rc;
 }
 

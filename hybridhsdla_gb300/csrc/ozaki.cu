@@ -45,7 +45,9 @@
 
 namespace hsdla {
 
-static const char *g_oz_err = "";
+// Message of the last failed Ozaki call, per host thread: contexts driven from different threads
+// never see each other's messages (each context copies it into its own message at once).
+static thread_local const char *g_oz_err = "";
 const char *ozaki_last_error() { return g_oz_err; }
 
 namespace {
@@ -1623,7 +1625,7 @@ int ozaki_check_device_error(OzakiPlan &oz) {
     if (cudaMemcpy(w, oz.d_error, sizeof(w), cudaMemcpyDeviceToHost) != cudaSuccess) return HSDLA_ERR_CUDA;
     const int h = w[0];
     if (h != 0) {
-        static char buf[192];
+        static thread_local char buf[192];
         snprintf(buf, sizeof(buf),
                  "device wait expired (code %d, role %d; block %d rank %d stage %d phase %d count %d)", h / 16,
                  h % 16, w[1], w[2], w[3], w[4], w[5]);
@@ -2283,18 +2285,24 @@ static cudaError_t record(cudaEvent_t ev, cudaStream_t st) {
 // T application (or phase expansion), X digits, the S/H products (accumulating after the first
 // panel).  With several panels the events span the panels' S/H launches and the slicing between
 // them.
+int ozaki_group_tapply_events(const OzGroup *g) { return (g->sf || g->hoist) ? 1 : g->panels; }
+
 int ozaki_group_run(OzGroup *g, const DevSystem &sys, const KTable &ktab, cudaStream_t st, const cudaEvent_t *ev,
-                    int nev, int *launches, bool defer_last_combine) {
+                    int nev, int *launches, bool defer_last_combine, const cudaEvent_t *ev_t, int nev_t) {
     const cudaEvent_t ev0 = nev >= 2 ? ev[0] : nullptr, ev1 = nev >= 2 ? ev[nev - 1] : nullptr;
+    // T-application events: pair q around the q-th T launch (when the caller gave enough of them)
+    const bool tev = ev_t && nev_t >= 2 * ozaki_group_tapply_events(g);
     int nl = 0;
     cudaError_t e = cudaSuccess;
     if (g->sf) {
         e = slice_launch(g->tM, st);                      // M and M diag(w_t)
+        if (e == cudaSuccess && tev) e = cudaEventRecord(ev_t[0], st);
         if (e == cudaSuccess)
             e = g->pair ? launch_pair(g->maps_t, g->s, g->d_err, g->d_jobs_t, g->n_jobs_t, g->tiles_t, g->d_list_t,
                                       nullptr, st, g->units_t, g->halves)
                         : launch_prepared(g->maps_t, g->s, g->d_err, g->d_jobs_t, g->n_jobs_t, g->tiles_t,
                                           g->d_list_t, nullptr, st);
+        if (e == cudaSuccess && tev) e = cudaEventRecord(ev_t[1], st);
         if (e == cudaSuccess) e = slice_launch(g->pan[0].tX, st);    // Z
         nl += 3;
         for (int t = 0; t < g->nt && e == cudaSuccess; ++t) {
@@ -2356,9 +2364,11 @@ int ozaki_group_run(OzGroup *g, const DevSystem &sys, const KTable &ktab, cudaSt
     }
     if (g->hoist) {
         e = slice_launch(g->tM, st);
+        if (e == cudaSuccess && tev) e = cudaEventRecord(ev_t[0], st);
         if (e == cudaSuccess)
             e = launch_prepared(g->maps_t, g->s, g->d_err, g->d_jobs_t, g->n_jobs_t, g->tiles_t, g->d_list_t, nullptr,
                                 st);
+        if (e == cudaSuccess && tev) e = cudaEventRecord(ev_t[1], st);
         nl += 2;
     }
     // the S/H job tables travel from pinned memory in stream order (a graph replays the copy)
@@ -2376,8 +2386,11 @@ int ozaki_group_run(OzGroup *g, const DevSystem &sys, const KTable &ktab, cudaSt
                 kt.a1 = (int)p.a1;
                 e = launch_apply_phase_multi(sys, kt, st);
             } else {
-                e = launch_prepared(g->maps_t, g->s, g->d_err, g->d_jobs_t + p.jt_off, p.n_jobs_t, p.tiles_t,
-                                    g->d_list_t + p.lt_off, nullptr, st);
+                if (tev) e = cudaEventRecord(ev_t[2 * pi], st);
+                if (e == cudaSuccess)
+                    e = launch_prepared(g->maps_t, g->s, g->d_err, g->d_jobs_t + p.jt_off, p.n_jobs_t, p.tiles_t,
+                                        g->d_list_t + p.lt_off, nullptr, st);
+                if (e == cudaSuccess && tev) e = cudaEventRecord(ev_t[2 * pi + 1], st);
             }
             nl += 1;
         }
@@ -2475,7 +2488,15 @@ unsigned char *g_noalloc_ptr[kNoAllocMaxDevices] = {};
 
 int noalloc_scratch(unsigned char **out) {
     int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kNoAllocMaxDevices) return HSDLA_ERR_DEVICE;
+    if (cudaGetDevice(&dev) != cudaSuccess) {
+        cudaGetLastError();
+        g_oz_err = "no current CUDA device";
+        return HSDLA_ERR_DEVICE;
+    }
+    if (dev < 0 || dev >= kNoAllocMaxDevices) {
+        g_oz_err = "device index beyond the 64 devices the static scratch table covers";
+        return HSDLA_ERR_DEVICE;
+    }
     std::lock_guard<std::mutex> lock(g_noalloc_mu);
     if (!g_noalloc_ptr[dev]) {
         void *p = nullptr;
@@ -2504,8 +2525,16 @@ extern "C" int hsdla_zherkx_lower_noalloc(int32_t num_slices, int64_t n, int64_t
                                           int64_t ldo, void *stream) {
     using namespace hsdla;
     const int s = num_slices == 0 ? kOzDefaultSlices : num_slices;
-    if (s < 2 || s > kOzMaxSlices || n < 0 || k < 0 || !dP || !dQ || !dOut || ldp < k || ldq < k || ldo < n)
+    if (s < 2 || s > kOzMaxSlices) {
+        g_oz_err = "num_slices outside [2, 12] (0 selects 11)";
         return HSDLA_ERR_ARG;
+    }
+    if (n < 0 || k < 0 || !dP || !dQ || !dOut || ldp < k || ldq < k || ldo < n) {
+        g_oz_err = "bad arguments: n or k negative, a NULL buffer, or a leading dimension below k (inputs) or n "
+                   "(output)";
+        return HSDLA_ERR_ARG;
+    }
+    g_oz_err = "";
     if (n == 0) return HSDLA_OK;
     const int64_t Kpad = round_up(std::max<int64_t>(k, 1), kKBlock);
     if (noalloc_bytes(s, n, Kpad) > kNoAllocScratchBytes) {
@@ -2557,6 +2586,14 @@ extern "C" int hsdla_zherkx_lower_noalloc(int32_t num_slices, int64_t n, int64_t
     if (e == cudaSuccess) e = cudaMemcpyAsync(&herr, d_err, sizeof(int), cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) { g_oz_err = cudaGetErrorString(e); return HSDLA_ERR_CUDA; }
-    if (herr != 0) { g_oz_err = "device wait expired"; return HSDLA_ERR_TIMEOUT; }
+    if (herr != 0) {
+        // the error word: code * 16 + the role whose bounded wait expired (1 TMA producer, 2 MMA
+        // issuer waiting for a drained accumulator, 3 MMA issuer waiting for operands, 4 epilogue)
+        static thread_local char buf[160];
+        snprintf(buf, sizeof(buf), "device wait expired in hsdla_zherkx_lower_noalloc (code %d, role %d)", herr / 16,
+                 herr % 16);
+        g_oz_err = buf;
+        return herr / 16 == kDevBadInput ? HSDLA_ERR_CUDA : HSDLA_ERR_TIMEOUT;
+    }
     return HSDLA_OK;
 }

@@ -79,9 +79,14 @@ int ozaki_group_last_combine(const OzGroup *g);
 // Enqueues the group's launches (slices, T application, phases, S/H products); no host sync.
 // ev: event pairs recorded around the S/H product launches (one pair, or one per type in the
 // structure-factor form; nev events, may be 0).  defer_last_combine: the structure-factor form's
-// last combine batch is left to the caller.
+// last combine batch is left to the caller.  ev_t: event pairs recorded around the T-application
+// launches (one pair, or one per atom panel when each panel applies T itself; nev_t events, may
+// be 0; plain records, so not for a run under graph capture).
 int ozaki_group_run(OzGroup *g, const DevSystem &sys, const KTable &ktab, cudaStream_t st, const cudaEvent_t *ev,
-                    int nev, int *launches, bool defer_last_combine = false);
+                    int nev, int *launches, bool defer_last_combine = false, const cudaEvent_t *ev_t = nullptr,
+                    int nev_t = 0);
+// Event pairs ozaki_group_run records around the group's T application (see ev_t).
+int ozaki_group_tapply_events(const OzGroup *g);
 void ozaki_group_destroy(OzGroup *g);
 
 int ozaki_plan_init(OzakiPlan &oz, int num_slices, double target);

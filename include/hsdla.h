@@ -113,9 +113,9 @@ typedef struct hsdla_report {
     double ms_per_kpoint;
     double flop;                 /* canonical 20 G^2 La + 24 L^2 a G, summed over k-points */
     double eff_tflops;           /* flop / ms_total */
-    double ms_construct_ab;      /* stage times of the last un-graphed run (0 under a graph) */
-    double ms_tapply;
-    double ms_contract;
+    double ms_construct_ab;      /* stage times of the last un-graphed run (0 under a graph): kernel (a), */
+    double ms_tapply;            /* the T-application launches (X = T C, or Z_t = T_t M_t per type), */
+    double ms_contract;          /* and the rest (slicing, S/H products, combine) */
     double ms_dominant;          /* device time of the dominant launch: the S/H contraction of the last k-point */
     double dominant_flop;        /* algorithmic flops of that launch (FP8 digit products for Ozaki, FP64 for plain) */
     double est_rel_err;          /* Ozaki: relative error predicted by the slice autotuner (0 if not tuned) */
@@ -134,6 +134,8 @@ typedef struct hsdla_plan hsdla_plan;
 int hsdla_context_create(int device, hsdla_context **ctx);
 /* Destroys the context and every plan still alive in it (plan handles become invalid). */
 void hsdla_context_destroy(hsdla_context *ctx);
+/* The context's last error message.  With ctx = NULL: the calling thread's last message of the
+ * entry point that takes no context, hsdla_zherkx_lower_noalloc ("" after a call that succeeded). */
 const char *hsdla_last_error(const hsdla_context *ctx);
 /* Cap on device bytes the context may allocate (0 = no cap); exceeding it returns HSDLA_ERR_NOMEM. */
 int hsdla_set_mem_cap(hsdla_context *ctx, int64_t bytes);
@@ -226,7 +228,8 @@ int hsdla_selftest_wait_timeout(hsdla_context *ctx, int32_t which, int64_t budge
  * array's device address (cudaGetSymbolAddress) with that device current; make that first
  * call before any stream capture.  Every call shares the one array, so calls that overlap on
  * the GPU (other streams, other host threads) race: serialise them.  The call returns after
- * the work on `stream` (NULL = default stream) has completed. */
+ * the work on `stream` (NULL = default stream) has completed.  Its error messages are read with
+ * hsdla_last_error(NULL) on the calling thread. */
 int hsdla_zherkx_lower_noalloc(int32_t num_slices, int64_t n, int64_t k, const hsdla_cx *dP, int64_t ldp,
                                const hsdla_cx *dQ, int64_t ldq, const double *dw, hsdla_cx *dOut,
                                int64_t ldo, void *stream);

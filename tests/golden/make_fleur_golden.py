@@ -9,9 +9,10 @@ packing as ``flapw_opt/tests/flapw_verify.py:68-82`` unpacks them).
 There is no HDF5 library in this image, so this script carries a minimal read-only parser for
 what the file uses: superblock version 0 with 8-byte offsets, version-1 object headers,
 symbol-table groups (v1 B-tree + local heap), contiguous layouts, committed (shared) compound
-datatypes.  Run it where the reference tree is present:
+datatypes.  Run it where the reference tree is present, naming the dump (as an argument, or
+in the environment variable HSDLA_FLEUR_DUMP):
 
-    python tests/golden/make_fleur_golden.py [path/to/fleur_dump.h5]
+    python tests/golden/make_fleur_golden.py <reference>/flapw_opt/tests/sample_input/two_atoms/fleur_dump.h5
 
 The fixture keeps the quantities as the dump stores them (Fortran column-major arrays
 reinterpreted the way FleurData.cpp reads them); T matrices keep their lower triangles, the
@@ -23,7 +24,6 @@ import sys
 
 import numpy as np
 
-DEFAULT = "/root/reference/flapw_opt/tests/sample_input/two_atoms/fleur_dump.h5"
 OUT = os.path.join(os.path.dirname(os.path.abspath(__file__)), "fleur_two_atoms.npz")
 
 
@@ -160,7 +160,10 @@ def field(info, name):
     raise KeyError(name)
 
 
-def main(path=DEFAULT):
+def main(path=None):
+    path = path or os.environ.get("HSDLA_FLEUR_DUMP")
+    if not path:
+        sys.exit("usage: make_fleur_golden.py <fleur_dump.h5> (or set HSDLA_FLEUR_DUMP)")
     f = H5(path)
     f64 = lambda p: f.dataset(p)["raw"].view("<f8")
     i32 = lambda p: f.dataset(p)["raw"].view("<i4")

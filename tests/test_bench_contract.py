@@ -26,3 +26,5 @@ def test_reference_arm_json_line():
     e2e = line["e2e"]
     assert e2e["value"] == line["value"] and e2e["unit"] == line["unit"]
     assert e2e["h2d_bytes_per_step"] == 0 and e2e["d2h_bytes_per_step"] == 0
+    # the same workload description as the GPU arm prints, so the two lines compare like for like
+    assert line["config"] == bench.bench_config("c2", 1, 1)

@@ -87,3 +87,15 @@ def test_context_without_gpu_reports_device_error():
     with pytest.raises(api.HsdlaError) as e:
         api.Context()
     assert e.value.code == -7
+
+
+def test_noalloc_argument_errors_carry_a_message():
+    """The entry point without a context reports through hsdla_last_error(NULL) on the calling
+    thread; argument checks run before any device call, so this needs no GPU."""
+    L = api.load()
+    rc = L.hsdla_zherkx_lower_noalloc(99, 4, 4, None, 4, None, 4, None, None, 4, None)
+    assert rc == -1
+    assert b"num_slices" in L.hsdla_last_error(None)
+    rc = L.hsdla_zherkx_lower_noalloc(11, 4, 8, None, 4, None, 4, None, None, 4, None)
+    assert rc == -1
+    assert b"leading dimension" in L.hsdla_last_error(None)
