@@ -82,7 +82,9 @@ EXPORTS = ["hsdla_context_create", "hsdla_context_destroy", "hsdla_last_error", 
            "hsdla_prepare_tmat", "hsdla_create_hs", "hsdla_plan_create", "hsdla_plan_execute",
            "hsdla_plan_workspace_bytes", "hsdla_plan_destroy", "hsdla_plan_construct_ab",
            "hsdla_zherkx_lower", "hsdla_zherkx_lower_noalloc", "hsdla_contract_ab", "hsdla_pack_lower",
-           "hsdla_selftest_wait_timeout"]
+           "hsdla_selftest_wait_timeout", "hsdla_zherk", "hsdla_zher2k", "hsdla_zherkx", "hsdla_dev_init",
+           "hsdla_dev_finalize", "hsdla_dev_context", "hsdla_dev_status", "hsdla_dev_zherk_", "hsdla_dev_zher2k_",
+           "hsdla_dev_zherkx_"]
 
 _lib = None
 
@@ -134,6 +136,23 @@ def load(build_if_missing: bool = True):
     L.hsdla_selftest_wait_timeout.argtypes = [vp, ctypes.c_int32, ctypes.c_int64]
     L.hsdla_zherkx_lower_noalloc.argtypes = [ctypes.c_int32, ctypes.c_int64, ctypes.c_int64, vp, ctypes.c_int64, vp,
                                              ctypes.c_int64, vp, vp, ctypes.c_int64, vp]
+    i32, i64, ch, dbl = ctypes.c_int32, ctypes.c_int64, ctypes.c_char, ctypes.c_double
+    L.hsdla_zherk.argtypes = [vp, i32, i32, ch, ch, i64, i64, dbl, vp, i64, dbl, vp, i64, vp]
+    L.hsdla_zher2k.argtypes = [vp, i32, i32, ch, ch, i64, i64, Cx, vp, i64, vp, i64, dbl, vp, i64, vp]
+    L.hsdla_zherkx.argtypes = [vp, i32, i32, ch, ch, i64, i64, Cx, vp, i64, vp, i64, dbl, vp, i64, vp]
+    L.hsdla_dev_init.argtypes = [i32, i32, i32]
+    L.hsdla_dev_finalize.argtypes = []
+    L.hsdla_dev_context.argtypes = []
+    L.hsdla_dev_context.restype = vp
+    L.hsdla_dev_status.argtypes = []
+    ip = ctypes.POINTER(ctypes.c_int)
+    cp = ctypes.c_char_p
+    L.hsdla_dev_zherk_.argtypes = [cp, cp, ip, ip, _dp, vp, ip, _dp, vp, ip]
+    L.hsdla_dev_zherk_.restype = None
+    L.hsdla_dev_zher2k_.argtypes = [cp, cp, ip, ip, _cxp, vp, ip, vp, ip, _dp, vp, ip]
+    L.hsdla_dev_zher2k_.restype = None
+    L.hsdla_dev_zherkx_.argtypes = [cp, cp, ip, ip, _cxp, vp, ip, vp, ip, _dp, vp, ip]
+    L.hsdla_dev_zherkx_.restype = None
     _lib = L
     return L
 
@@ -141,6 +160,26 @@ def load(build_if_missing: bool = True):
 # ------------------------------------------------------------------ helpers
 def _c(a, dtype):
     return np.ascontiguousarray(a, dtype=dtype)
+
+
+def _addr(x):
+    """Address of a numpy array or a torch tensor (host or device), or None."""
+    if x is None:
+        return None
+    if hasattr(x, "data_ptr"):
+        return ctypes.c_void_p(x.data_ptr())
+    return ctypes.c_void_p(x.ctypes.data)
+
+
+def _stream(stream):
+    if stream is None:
+        return None
+    return ctypes.c_void_p(stream.cuda_stream if hasattr(stream, "cuda_stream") else int(stream))
+
+
+def _cx(z) -> Cx:
+    z = complex(z)
+    return Cx(z.real, z.imag)
 
 
 def prepare_tmats(sys_) -> Tuple[np.ndarray, np.ndarray, np.ndarray]:
@@ -338,6 +377,81 @@ class Context:
         return out
 
 
+# ------------------------------------------------- BLAS-shaped contraction plugin
+# Argument order and meaning of dev_zherk_ / dev_zher2k_ / dev_zherkx_
+# (flapw_opt/src/include/acc/wrappers.h:19-28): column-major matrices given as numpy arrays or torch
+# tensors (host or device memory) with explicit leading dimensions.
+def _plugin_methods():
+    def zherk(self, uplo, trans, n, k, alpha, A, lda, beta, C, ldc, precision="fp64", num_slices=0, stream=None):
+        """C = alpha op(A) op(A)^H + beta C on C's uplo triangle (``hsdla_zherk``)."""
+        self.check(self.lib.hsdla_zherk(self.h, _PREC[precision], int(num_slices), uplo.encode(), trans.encode(),
+                                        int(n), int(k), float(alpha), _addr(A), int(lda), float(beta), _addr(C),
+                                        int(ldc), _stream(stream)))
+
+    def zher2k(self, uplo, trans, n, k, alpha, A, lda, B, ldb, beta, C, ldc, precision="fp64", num_slices=0,
+               stream=None):
+        """C = alpha op(A) op(B)^H + conj(alpha) op(B) op(A)^H + beta C (``hsdla_zher2k``)."""
+        self.check(self.lib.hsdla_zher2k(self.h, _PREC[precision], int(num_slices), uplo.encode(), trans.encode(),
+                                         int(n), int(k), _cx(alpha), _addr(A), int(lda), _addr(B), int(ldb),
+                                         float(beta), _addr(C), int(ldc), _stream(stream)))
+
+    def zherkx(self, uplo, trans, n, k, alpha, A, lda, B, ldb, beta, C, ldc, precision="fp64", num_slices=0,
+               stream=None):
+        """C = alpha op(A) op(B)^H + beta C, Hermitian result assumed (``hsdla_zherkx``)."""
+        self.check(self.lib.hsdla_zherkx(self.h, _PREC[precision], int(num_slices), uplo.encode(), trans.encode(),
+                                         int(n), int(k), _cx(alpha), _addr(A), int(lda), _addr(B), int(ldb),
+                                         float(beta), _addr(C), int(ldc), _stream(stream)))
+    return zherk, zher2k, zherkx
+
+
+def dev_init(device: int = 0, precision="fp64", num_slices: int = 0):
+    """``hsdla_dev_init``: the library-owned context of the Fortran-style entry points."""
+    L_ = load()
+    rc = L_.hsdla_dev_init(int(device), _PREC[precision] if isinstance(precision, str) else int(precision),
+                           int(num_slices))
+    if rc != 0:
+        raise HsdlaError(rc, "hsdla_dev_init failed")
+
+
+def dev_finalize():
+    load().hsdla_dev_finalize()
+
+
+def _dev_check():
+    L_ = load()
+    rc = L_.hsdla_dev_status()
+    if rc != 0:
+        c = L_.hsdla_dev_context()
+        raise HsdlaError(rc, L_.hsdla_last_error(c).decode() if c else "no context")
+
+
+def _iref(v):
+    return ctypes.byref(ctypes.c_int(int(v)))
+
+
+def dev_zherk_(uplo, trans, n, k, alpha, A, lda, beta, C, ldc):
+    """The reference's ``dev_zherk_`` argument list (every argument by reference)."""
+    load().hsdla_dev_zherk_(uplo.encode(), trans.encode(), _iref(n), _iref(k), ctypes.byref(ctypes.c_double(alpha)),
+                            _addr(A), _iref(lda), ctypes.byref(ctypes.c_double(beta)), _addr(C), _iref(ldc))
+    _dev_check()
+
+
+def dev_zher2k_(uplo, trans, n, k, alpha, A, lda, B, ldb, beta, C, ldc):
+    """The reference's ``dev_zher2k_`` argument list."""
+    load().hsdla_dev_zher2k_(uplo.encode(), trans.encode(), _iref(n), _iref(k), ctypes.byref(_cx(alpha)), _addr(A),
+                             _iref(lda), _addr(B), _iref(ldb), ctypes.byref(ctypes.c_double(beta)), _addr(C),
+                             _iref(ldc))
+    _dev_check()
+
+
+def dev_zherkx_(uplo, trans, n, k, alpha, A, lda, B, ldb, beta, C, ldc):
+    """The reference's ``dev_zherkx_`` argument list."""
+    load().hsdla_dev_zherkx_(uplo.encode(), trans.encode(), _iref(n), _iref(k), ctypes.byref(_cx(alpha)), _addr(A),
+                             _iref(lda), _addr(B), _iref(ldb), ctypes.byref(ctypes.c_double(beta)), _addr(C),
+                             _iref(ldc))
+    _dev_check()
+
+
 def zherkx_lower_noalloc(P, Q=None, w=None, num_slices=0, out=None, stream=None):
     """Allocation-free Ozaki contraction (``hsdla_zherkx_lower_noalloc``): lower
     triangle of P^H diag(w) Q for device complex128 K x n matrices given as torch
@@ -445,3 +559,6 @@ def create_HS2(kpt, kmax, bmat, g_mesh, ad, method="fp64", ctx: Optional[Context
         raise ValueError("bmat differs from the system's reciprocal basis")
     (res,), rep = ctx.create_hs(ad, [kp], precision=method)
     return res[0], res[1], rep["ms_total"]
+
+
+Context.zherk, Context.zher2k, Context.zherkx = _plugin_methods()

@@ -131,6 +131,16 @@ cudaError_t launch_sf_table(const double2 *ex, const double2 *ey, const double2 
 // but for the end).
 cudaError_t launch_sf_combine(const SfTab &tab, const double2 *sf, bool first, cudaStream_t st);
 
+// BLAS-shaped plugin (blas_plugin.cu).  Operand in the 'C' layout: dst rows [r0, r0 + k) of every
+// column c < n (ld ldd) = s * src[r, c] (src k x n, transpose false) or s * conj(src[c, r]) (src
+// n x k, transpose true).
+cudaError_t launch_plugin_operand(const double2 *src, int64_t lds, bool transpose, int64_t k, int64_t n, double2 s,
+                                  double2 *dst, int64_t ldd, int64_t r0, cudaStream_t st);
+// On C's uplo triangle: C = a T(R) + beta C, T(R)[i, j] = R[i, j] (lower) or conj(R[j, i]) (upper),
+// R's lower triangle read (R may be NULL: C = beta C); herm: real diagonal.
+cudaError_t launch_plugin_epilogue(const double2 *R, int64_t ldr, double2 *C, int64_t ldc, int64_t n, double2 a,
+                                   double beta, bool upper, bool herm, cudaStream_t st);
+
 // Fleur's packed lower triangle (row by row) of a column-major n x n matrix (device buffers).
 cudaError_t launch_pack_lower(const double2 *M, int64_t ld, int64_t n, double2 *P, cudaStream_t st);
 

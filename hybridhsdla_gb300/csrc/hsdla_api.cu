@@ -20,6 +20,7 @@
 #include <cstring>
 #include <map>
 #include <memory>
+#include <mutex>
 #include <set>
 #include <string>
 #include <tuple>
@@ -60,6 +61,8 @@ struct hsdla_context {
     std::set<hsdla_plan *> plans;   // live plans, destroyed with the context
     // slice autotuner results: (L, atoms, types, n_G bucket, target) -> (slices, predicted error)
     std::map<std::tuple<int, int, int, int64_t, double>, std::pair<int, double>> tune_cache;
+    // the BLAS-shaped plugin's Ozaki state (its device error word), set up on first use
+    OzakiPlan plugin_oz{};
 };
 
 struct PlanKpoint {
@@ -560,6 +563,7 @@ void hsdla_context_destroy(hsdla_context *ctx) {
     while (!ctx->plans.empty()) hsdla_plan_destroy(*ctx->plans.begin());
     if (ctx->ws) ctx_free(ctx, ctx->ws, ctx->ws_bytes);
     if (ctx->hout) ctx_free(ctx, ctx->hout, ctx->hout_bytes);
+    ozaki_plan_release(ctx->plugin_oz);
     ctx_cache_release(ctx);
     if (ctx->staging) cudaFreeHost(ctx->staging);
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
@@ -1806,6 +1810,268 @@ int hsdla_zherkx_lower(hsdla_context *ctx, int32_t precision, int32_t num_slices
         return HSDLA_OK;
     }
     return set_err(ctx, HSDLA_ERR_ARG, "unknown precision %d", precision);
+}
+
+}  // extern "C"
+
+// =====================================================================================
+// BLAS-shaped contraction plugin: the reference's dev_zherk_ / dev_zher2k_ / dev_zherkx_
+// (flapw_opt/src/include/acc/wrappers.h:19-28, flapw_opt/src/wrappers.cpp:171-257) with their
+// full argument semantics, on this library's lower-triangle contraction R = lower(P^H Q).
+namespace {
+
+enum PluginKind { kPluginHerk = 0, kPluginHer2k = 1, kPluginHerkx = 2 };
+
+// True when p is host memory (pageable or page-locked): such operands are staged through device
+// memory, as the reference's cuBLASXt backend does with the page-locked buffers of create_HS2.
+bool host_memory(const void *p) {
+    cudaPointerAttributes a{};
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return true;
+    }
+    return a.type == cudaMemoryTypeHost || a.type == cudaMemoryTypeUnregistered;
+}
+
+int64_t r1k(int64_t b) { return (b + 1023) / 1024 * 1024; }
+
+//   zherk : C = alpha op(A) op(A)^H + beta C                       (alpha, beta real)
+//   zher2k: C = alpha op(A) op(B)^H + conj(alpha) op(B) op(A)^H + beta C
+//   zherkx: C = alpha op(A) op(B)^H + beta C (the product taken as Hermitian; no diagonal rule)
+// with op(X) = X (trans 'N', X n x k) or X^H (trans 'C', X k x n), on C's uplo triangle only.
+// With the k x n operands X_A = op(A)^H (A itself for 'C', its conjugate transpose for 'N') and
+// X_B likewise, op(A) op(B)^H = X_A^H X_B, so every product is lower(P^H Q):
+//   zherk : P = Q = X_A,  zherkx: P = X_A, Q = X_B,  zher2k: P = [X_A; X_B], Q = [alpha X_B; conj(alpha) X_A].
+// uplo 'U' swaps P and Q: the upper triangle of P^H Q is the conjugate transpose of the lower
+// triangle of Q^H P.
+int plugin_contract(hsdla_context *ctx, int kind, int32_t precision, int32_t num_slices, char uplo, char trans,
+                    int64_t n, int64_t k, double2 alpha, const double2 *A, int64_t lda, const double2 *B, int64_t ldb,
+                    double beta, double2 *C, int64_t ldc, cudaStream_t st) {
+    static const char *names[3] = {"zherk", "zher2k", "zherkx"};
+    const char *nm = names[kind];
+    const char u = (char)toupper((unsigned char)uplo), tr = (char)toupper((unsigned char)trans);
+    if (u != 'L' && u != 'U') return set_err(ctx, HSDLA_ERR_ARG, "%s: uplo must be 'L' or 'U'", nm);
+    if (tr != 'N' && tr != 'C') return set_err(ctx, HSDLA_ERR_ARG, "%s: trans must be 'N' or 'C'", nm);
+    if (precision != HSDLA_PREC_FP64 && precision != HSDLA_PREC_OZAKI_FP8)
+        return set_err(ctx, HSDLA_ERR_ARG, "%s: unknown precision %d", nm, precision);
+    if (n < 0 || k < 0) return set_err(ctx, HSDLA_ERR_ARG, "%s: n or k negative", nm);
+    const bool two = kind != kPluginHerk;
+    const int64_t rows = tr == 'N' ? n : k, cols = tr == 'N' ? k : n;   // stored shape of A (and B)
+    if (lda < std::max<int64_t>(1, rows) || (two && ldb < std::max<int64_t>(1, rows)) || ldc < std::max<int64_t>(1, n))
+        return set_err(ctx, HSDLA_ERR_ARG, "%s: leading dimension too small (lda, ldb >= %s, ldc >= n)", nm,
+                       tr == 'N' ? "n" : "k");
+    if (n == 0) return HSDLA_OK;
+    const bool product = k > 0 && (alpha.x != 0.0 || alpha.y != 0.0);
+    if (!C || (product && (!A || (two && !B)))) return set_err(ctx, HSDLA_ERR_ARG, "%s: NULL matrix", nm);
+    CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+    const bool upper = u == 'U', herm = kind != kPluginHerkx;
+    const bool hA = product && host_memory(A), hB = product && two && host_memory(B), hC = host_memory(C);
+    const int64_t K = kind == kPluginHer2k ? 2 * k : k;
+    // operands in place when A (and B) are already K x n: trans 'C', not zher2k
+    const bool build = product && (tr == 'N' || kind == kPluginHer2k);
+    // R straight into C's lower triangle when nothing is left to scale or add
+    const bool direct = !upper && beta == 0.0 && (kind == kPluginHer2k || (alpha.x == 1.0 && alpha.y == 0.0));
+    const int s = precision == HSDLA_PREC_OZAKI_FP8 ? (num_slices == 0 ? kOzDefaultSlices : num_slices) : 0;
+    if (precision == HSDLA_PREC_OZAKI_FP8 && (s < 2 || s > kOzMaxSlices))
+        return set_err(ctx, HSDLA_ERR_ARG, "%s: num_slices outside [2, 12]", nm);
+    // ---- workspace: staged host operands, built operands, R, the contraction's own scratch
+    const int64_t e16 = (int64_t)sizeof(double2);
+    int64_t off = 0;
+    auto slot = [&](bool need, int64_t bytes) { const int64_t o = off; if (need) off += r1k(bytes); return o; };
+    const int64_t oA = slot(hA, rows * cols * e16), oB = slot(hB, rows * cols * e16), oC = slot(hC, n * n * e16);
+    const int64_t oP = slot(build, K * n * e16), oQ = slot(build && kind != kPluginHerk, K * n * e16);
+    const int64_t oR = slot(product && !direct, n * n * e16);
+    const int64_t oJ = slot(product && precision == HSDLA_PREC_FP64, sizeof(Fp64Job));
+    const int64_t oZ = slot(product && precision == HSDLA_PREC_OZAKI_FP8, s ? ozaki_herkx_workspace(s, K, n) : 0);
+    void *wsv = nullptr;
+    int rc = ctx_workspace(ctx, std::max<int64_t>(off, 1024), &wsv);
+    if (rc) return rc;
+    char *ws = reinterpret_cast<char *>(wsv);
+    // ---- stage host memory
+    const double2 *dA = A, *dB = B;
+    double2 *dC = C;
+    int64_t dlda = lda, dldb = ldb, dldc = ldc;
+    if (hA) {
+        CUDA_TRY(ctx, cudaMemcpy2DAsync(ws + oA, rows * e16, A, lda * e16, rows * e16, cols, cudaMemcpyHostToDevice, st));
+        dA = reinterpret_cast<const double2 *>(ws + oA);
+        dlda = rows;
+    }
+    if (hB) {
+        CUDA_TRY(ctx, cudaMemcpy2DAsync(ws + oB, rows * e16, B, ldb * e16, rows * e16, cols, cudaMemcpyHostToDevice, st));
+        dB = reinterpret_cast<const double2 *>(ws + oB);
+        dldb = rows;
+    }
+    if (hC) {
+        // the whole n x n block travels (the other triangle comes back as it went)
+        CUDA_TRY(ctx, cudaMemcpy2DAsync(ws + oC, n * e16, C, ldc * e16, n * e16, n, cudaMemcpyHostToDevice, st));
+        dC = reinterpret_cast<double2 *>(ws + oC);
+        dldc = n;
+    }
+    // ---- operands and product
+    const double2 one = make_double2(1.0, 0.0), calpha = make_double2(alpha.x, -alpha.y);
+    double2 *R = direct ? dC : reinterpret_cast<double2 *>(ws + oR);
+    const int64_t ldr = direct ? dldc : n;
+    if (product) {
+        const double2 *P = dA, *Q = two ? dB : dA;
+        int64_t ldp = dlda, ldq = two ? dldb : dlda;
+        if (build) {
+            double2 *bP = reinterpret_cast<double2 *>(ws + oP);
+            double2 *bQ = kind == kPluginHerk ? bP : reinterpret_cast<double2 *>(ws + oQ);
+            const bool t = tr == 'N';
+            cudaError_t e = launch_plugin_operand(dA, dlda, t, k, n, one, bP, K, 0, st);
+            if (kind == kPluginHer2k) {
+                if (e == cudaSuccess) e = launch_plugin_operand(dB, dldb, t, k, n, one, bP, K, k, st);
+                if (e == cudaSuccess) e = launch_plugin_operand(dB, dldb, t, k, n, alpha, bQ, K, 0, st);
+                if (e == cudaSuccess) e = launch_plugin_operand(dA, dlda, t, k, n, calpha, bQ, K, k, st);
+            } else if (kind == kPluginHerkx) {
+                if (e == cudaSuccess) e = launch_plugin_operand(dB, dldb, t, k, n, one, bQ, K, 0, st);
+            }
+            if (e != cudaSuccess) return set_err(ctx, HSDLA_ERR_CUDA, "%s: operand build: %s", nm, cudaGetErrorString(e));
+            P = bP; Q = bQ; ldp = ldq = K;
+        }
+        if (upper) { std::swap(P, Q); std::swap(ldp, ldq); }
+        if (precision == HSDLA_PREC_FP64) {
+            std::vector<Fp64Job> jobs(1);
+            Fp64Job &j = jobs[0];
+            j.P = P; j.ldp = ldp; j.Q = Q; j.ldq = ldq; j.w = nullptr;
+            j.out = R; j.ldo = ldr; j.m = n; j.n = n; j.k = K; j.lower = 1;
+            const int64_t tiles = assign_tiles(jobs, 0);
+            Fp64Job *dj = reinterpret_cast<Fp64Job *>(ws + oJ);
+            CUDA_TRY(ctx, cudaMemcpyAsync(dj, jobs.data(), sizeof(Fp64Job), cudaMemcpyHostToDevice, st));
+            CUDA_TRY(ctx, launch_fp64_jobs(dj, 1, tiles, st));
+        } else {
+            rc = ozaki_plan_init(ctx->plugin_oz, s, 1e-13);
+            if (rc) return set_err(ctx, rc, "%s: %s", nm, ozaki_last_error());
+            int nl = 0;
+            rc = ozaki_herkx(ctx->plugin_oz, P, ldp, Q, ldq, nullptr, K, n, R, ldr, ws + oZ, st, &nl);
+            if (rc) return set_err(ctx, rc, "%s: %s", nm, ozaki_last_error());
+        }
+    }
+    // ---- epilogue on C's triangle (in place for the direct form: only the real diagonal)
+    if (!direct || herm) {
+        const double2 a = kind == kPluginHer2k ? one : alpha;
+        CUDA_TRY(ctx, launch_plugin_epilogue(product ? R : nullptr, ldr, dC, dldc, n, a, beta, upper, herm, st));
+    }
+    if (hC) CUDA_TRY(ctx, cudaMemcpy2DAsync(C, ldc * e16, dC, n * e16, n * e16, n, cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(ctx, cudaStreamSynchronize(st));
+    if (product && precision == HSDLA_PREC_OZAKI_FP8) {
+        rc = ozaki_check_device_error(ctx->plugin_oz);
+        if (rc) return set_err(ctx, rc, "%s: device-side error: %s", nm, ozaki_last_error());
+    }
+    return HSDLA_OK;
+}
+
+// The Fortran-style entry points' library-owned context and settings (hsdla_dev_init).
+std::mutex g_dev_mu;
+hsdla_context *g_dev_ctx = nullptr;
+int32_t g_dev_prec = HSDLA_PREC_FP64, g_dev_slices = 0;
+thread_local int g_dev_status = HSDLA_OK;
+
+hsdla_context *dev_ctx() {
+    std::lock_guard<std::mutex> lock(g_dev_mu);
+    if (!g_dev_ctx) {
+        int dev = 0;
+        if (const char *v = getenv("HSDLA_DEVICE")) dev = (int)strtol(v, nullptr, 10);
+        if (hsdla_context_create(dev, &g_dev_ctx) != HSDLA_OK) g_dev_ctx = nullptr;
+    }
+    return g_dev_ctx;
+}
+
+void dev_call(int kind, const char *uplo, const char *trans, const int *n, const int *k, double2 alpha,
+              const hsdla_cx *A, const int *lda, const hsdla_cx *B, const int *ldb, const double *beta, hsdla_cx *C,
+              const int *ldc) {
+    hsdla_context *ctx = dev_ctx();
+    if (!ctx) { g_dev_status = HSDLA_ERR_DEVICE; return; }
+    if (!uplo || !trans || !n || !k || !lda || !beta || !ldc || (kind != kPluginHerk && !ldb)) {
+        g_dev_status = set_err(ctx, HSDLA_ERR_ARG, "NULL scalar argument");
+        return;
+    }
+    std::lock_guard<std::mutex> lock(g_dev_mu);   // one context: calls are serialised
+    g_dev_status = plugin_contract(ctx, kind, g_dev_prec, g_dev_slices, *uplo, *trans, *n, *k, alpha,
+                                   reinterpret_cast<const double2 *>(A), *lda, reinterpret_cast<const double2 *>(B),
+                                   ldb ? *ldb : 0, *beta, reinterpret_cast<double2 *>(C), *ldc, ctx->stream);
+}
+
+}  // namespace
+
+extern "C" {
+
+int hsdla_zherk(hsdla_context *ctx, int32_t precision, int32_t num_slices, char uplo, char trans, int64_t n, int64_t k,
+                double alpha, const hsdla_cx *A, int64_t lda, double beta, hsdla_cx *C, int64_t ldc, void *stream) {
+    if (!ctx) return HSDLA_ERR_ARG;
+    return plugin_contract(ctx, kPluginHerk, precision, num_slices, uplo, trans, n, k, make_double2(alpha, 0.0),
+                           reinterpret_cast<const double2 *>(A), lda, nullptr, 0, beta, reinterpret_cast<double2 *>(C),
+                           ldc, (cudaStream_t)stream);
+}
+
+int hsdla_zher2k(hsdla_context *ctx, int32_t precision, int32_t num_slices, char uplo, char trans, int64_t n,
+                 int64_t k, hsdla_cx alpha, const hsdla_cx *A, int64_t lda, const hsdla_cx *B, int64_t ldb, double beta,
+                 hsdla_cx *C, int64_t ldc, void *stream) {
+    if (!ctx) return HSDLA_ERR_ARG;
+    return plugin_contract(ctx, kPluginHer2k, precision, num_slices, uplo, trans, n, k, make_double2(alpha.re, alpha.im),
+                           reinterpret_cast<const double2 *>(A), lda, reinterpret_cast<const double2 *>(B), ldb, beta,
+                           reinterpret_cast<double2 *>(C), ldc, (cudaStream_t)stream);
+}
+
+int hsdla_zherkx(hsdla_context *ctx, int32_t precision, int32_t num_slices, char uplo, char trans, int64_t n,
+                 int64_t k, hsdla_cx alpha, const hsdla_cx *A, int64_t lda, const hsdla_cx *B, int64_t ldb, double beta,
+                 hsdla_cx *C, int64_t ldc, void *stream) {
+    if (!ctx) return HSDLA_ERR_ARG;
+    return plugin_contract(ctx, kPluginHerkx, precision, num_slices, uplo, trans, n, k, make_double2(alpha.re, alpha.im),
+                           reinterpret_cast<const double2 *>(A), lda, reinterpret_cast<const double2 *>(B), ldb, beta,
+                           reinterpret_cast<double2 *>(C), ldc, (cudaStream_t)stream);
+}
+
+int hsdla_dev_init(int32_t device, int32_t precision, int32_t num_slices) {
+    if (precision != HSDLA_PREC_FP64 && precision != HSDLA_PREC_OZAKI_FP8) return HSDLA_ERR_ARG;
+    if (precision == HSDLA_PREC_OZAKI_FP8 && num_slices != 0 && (num_slices < 2 || num_slices > kOzMaxSlices))
+        return HSDLA_ERR_ARG;
+    std::lock_guard<std::mutex> lock(g_dev_mu);
+    if (g_dev_ctx && g_dev_ctx->device != device) {
+        hsdla_context_destroy(g_dev_ctx);
+        g_dev_ctx = nullptr;
+    }
+    if (!g_dev_ctx) {
+        const int rc = hsdla_context_create(device, &g_dev_ctx);
+        if (rc) { g_dev_ctx = nullptr; return rc; }
+    }
+    g_dev_prec = precision;
+    g_dev_slices = num_slices;
+    return HSDLA_OK;
+}
+
+int hsdla_dev_finalize(void) {
+    std::lock_guard<std::mutex> lock(g_dev_mu);
+    if (g_dev_ctx) hsdla_context_destroy(g_dev_ctx);
+    g_dev_ctx = nullptr;
+    return HSDLA_OK;
+}
+
+const hsdla_context *hsdla_dev_context(void) {
+    std::lock_guard<std::mutex> lock(g_dev_mu);
+    return g_dev_ctx;
+}
+
+int hsdla_dev_status(void) { return g_dev_status; }
+
+void hsdla_dev_zherk_(const char *uplo, const char *trans, const int *n, const int *k, const double *alpha,
+                      const hsdla_cx *A, const int *lda, const double *beta, hsdla_cx *C, const int *ldc) {
+    if (!alpha) { g_dev_status = HSDLA_ERR_ARG; return; }
+    dev_call(kPluginHerk, uplo, trans, n, k, make_double2(*alpha, 0.0), A, lda, nullptr, nullptr, beta, C, ldc);
+}
+
+void hsdla_dev_zher2k_(const char *uplo, const char *trans, const int *n, const int *k, const hsdla_cx *alpha,
+                       const hsdla_cx *A, const int *lda, const hsdla_cx *B, const int *ldb, const double *beta,
+                       hsdla_cx *C, const int *ldc) {
+    if (!alpha) { g_dev_status = HSDLA_ERR_ARG; return; }
+    dev_call(kPluginHer2k, uplo, trans, n, k, make_double2(alpha->re, alpha->im), A, lda, B, ldb, beta, C, ldc);
+}
+
+void hsdla_dev_zherkx_(const char *uplo, const char *trans, const int *n, const int *k, const hsdla_cx *alpha,
+                       const hsdla_cx *A, const int *lda, const hsdla_cx *B, const int *ldb, const double *beta,
+                       hsdla_cx *C, const int *ldc) {
+    if (!alpha) { g_dev_status = HSDLA_ERR_ARG; return; }
+    dev_call(kPluginHerkx, uplo, trans, n, k, make_double2(alpha->re, alpha->im), A, lda, B, ldb, beta, C, ldc);
 }
 
 }  // extern "C"

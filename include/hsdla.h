@@ -197,6 +197,51 @@ int hsdla_zherkx_lower(hsdla_context *ctx, int32_t precision, int32_t num_slices
                        const hsdla_cx *dP, int64_t ldp, const hsdla_cx *dQ, int64_t ldq,
                        const double *dw, hsdla_cx *dOut, int64_t ldo, void *stream);
 
+/* ---- BLAS-shaped contraction plugin: the reference's backend dev_zherk_, dev_zher2k_, dev_zherkx_
+ * (flapw_opt/src/include/acc/wrappers.h:19-28, flapw_opt/src/wrappers.cpp:171-257), which
+ * create_HS2_stripped_v2 calls for S = A^H A, S += W^H W, H = B^H X + X^H B and H += A^H X'
+ * (flapw_opt/src/h_and_s_stripped_v2.cpp:158, 177, 300, 362).  Fortran BLAS / cuBLAS semantics,
+ * column-major, on the uplo triangle of C only (the other triangle is not touched):
+ *   zherk : C = alpha op(A) op(A)^H + beta C                         (alpha, beta real)
+ *   zher2k: C = alpha op(A) op(B)^H + conj(alpha) op(B) op(A)^H + beta C   (beta real)
+ *   zherkx: C = alpha op(A) op(B)^H + beta C, the product taken as Hermitian (cuBLAS's herkx; MKL's
+ *           zgemmt in the reference's CPU build)                     (beta real)
+ * op(X) = X for trans 'N' (X n x k, ld >= n), X^H for trans 'C' (X k x n, ld >= k); uplo 'L' or 'U'
+ * (either case).  zherk and zher2k leave a real diagonal (its imaginary part set to zero, as BLAS
+ * does); beta = 0 never reads C.  A, B, C may be device or host memory (host matrices are staged
+ * through device memory, as the reference's cuBLASXt backend does with its page-locked buffers).
+ * precision: HSDLA_PREC_FP64 (DMMA) or HSDLA_PREC_OZAKI_FP8 with num_slices (0 = 11) digit slices.
+ * Asynchronous work runs on `stream` (NULL = the legacy default stream); the call returns after it
+ * completed. */
+int hsdla_zherk(hsdla_context *ctx, int32_t precision, int32_t num_slices, char uplo, char trans, int64_t n, int64_t k,
+                double alpha, const hsdla_cx *A, int64_t lda, double beta, hsdla_cx *C, int64_t ldc, void *stream);
+int hsdla_zher2k(hsdla_context *ctx, int32_t precision, int32_t num_slices, char uplo, char trans, int64_t n,
+                 int64_t k, hsdla_cx alpha, const hsdla_cx *A, int64_t lda, const hsdla_cx *B, int64_t ldb, double beta,
+                 hsdla_cx *C, int64_t ldc, void *stream);
+int hsdla_zherkx(hsdla_context *ctx, int32_t precision, int32_t num_slices, char uplo, char trans, int64_t n,
+                 int64_t k, hsdla_cx alpha, const hsdla_cx *A, int64_t lda, const hsdla_cx *B, int64_t ldb, double beta,
+                 hsdla_cx *C, int64_t ldc, void *stream);
+
+/* The same three with the reference's own argument lists (Fortran style: every argument by pointer,
+ * void return), for a wrappers.cpp whose dev_zherk_ / dev_zher2k_ / dev_zherkx_ forward to them
+ * one to one, and hsdla_dev_init / hsdla_dev_finalize in place of dev_init / dev_finalize
+ * (flapw_opt/src/wrappers.cpp:111-169).  They run on a context the library owns (created by
+ * hsdla_dev_init, or on first use on device HSDLA_DEVICE, default 0, in FP64), one call at a time,
+ * and return after the result is in C.  hsdla_dev_status() is the status of the calling thread's
+ * last hsdla_dev_* call; its message is hsdla_last_error(hsdla_dev_context()). */
+int hsdla_dev_init(int32_t device, int32_t precision, int32_t num_slices);
+int hsdla_dev_finalize(void);
+const hsdla_context *hsdla_dev_context(void);
+int hsdla_dev_status(void);
+void hsdla_dev_zherk_(const char *uplo, const char *trans, const int *n, const int *k, const double *alpha,
+                      const hsdla_cx *A, const int *lda, const double *beta, hsdla_cx *C, const int *ldc);
+void hsdla_dev_zher2k_(const char *uplo, const char *trans, const int *n, const int *k, const hsdla_cx *alpha,
+                       const hsdla_cx *A, const int *lda, const hsdla_cx *B, const int *ldb, const double *beta,
+                       hsdla_cx *C, const int *ldc);
+void hsdla_dev_zherkx_(const char *uplo, const char *trans, const int *n, const int *k, const hsdla_cx *alpha,
+                       const hsdla_cx *A, const int *lda, const hsdla_cx *B, const int *ldb, const double *beta,
+                       hsdla_cx *C, const int *ldc);
+
 /* Hand-off to an eigensolver in Fleur's packed form: the lower triangle of the column-major
  * n x n DEVICE matrix M (leading dimension ld >= n, e.g. H or S from hsdla_plan_execute) written
  * row by row into the DEVICE array packed of n (n + 1) / 2 elements, element (r, c), c <= r, at
