@@ -46,6 +46,7 @@ WORKLOAD_TEXT = {
     "c3": "c3: 17.6x17.6x25.2 bohr, 64 atoms / 4 types, lmax 8, 64 k-points (4x4x4), n_G 6000-6600, CUDA graph",
     "c4": "c4: cubic a=40 bohr, 512 atoms / 16 types, lmax 10, 4 k-points, n_G 19800-20700, CUDA graph",
     "c2t1": "c2t1: c2's cell and n_G 8000 with 16 atoms of one type (one per-type S/H launch of c2's shape)",
+    "c2r": "c2r: c2 with per-atom rotations, the atoms of each type in two rotation classes (16 classes)",
 }
 PROFILE_SUMMARY = os.path.join(ROOT, "profiles", "oz_pair_c2.md")
 

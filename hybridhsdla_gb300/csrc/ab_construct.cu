@@ -338,53 +338,62 @@ __global__ void __launch_bounds__(kThreads) construct_rows_kernel(DevSystem sys,
             k4[0] = K[0]; k4[1] = K[1]; k4[2] = K[2]; k4[3] = sqrt(s);
         }
         __syncthreads();
-        // the columns' Bessel values per type, then their Y_lm sets (one warp per kind, mostly)
-        const int nb = ncols * nt, ny = ncols * nl;
-        for (int w = threadIdx.x; w < nb + ny; w += blockDim.x) {
-            if (w < nb) {
-                const int c = w / nt, t = w - c * nt;
-                const double kn = kv[4 * c + 3];
-                double fj[kMaxLmax + 1], dfj[kMaxLmax + 1];
-                const double x = sys.type_rmt[t] * kn;
-                sphbes_dev(sys.max_lmax, x, fj);
-                dsphbs_dev(sys.max_lmax, x, fj, dfj);
-                for (int l = 0; l < nl; ++l) {
-                    const int tl = t * nl + l;
-                    au[c * tnl + tl] = sys.dE_u[tl] * kn * dfj[l] - sys.dE_u_dr[tl] * fj[l];
-                    bu[c * tnl + tl] = -sys.u[tl] * kn * dfj[l] + sys.u_dr[tl] * fj[l];
+        // the columns' Bessel values per type, then their Y_lm sets (one warp per kind, mostly);
+        // with (type, rotation) classes the Y_lm sets come once per rotation, each followed by the
+        // rows of the types (classes) that carry it
+        const int nrot = sys.num_rots > 0 ? sys.num_rots : 1;
+        for (int rho = 0; rho < nrot; ++rho) {
+            // R^T K with R = mrot bmat of this rotation (tensor_AB_match.cpp:97), bmat without one
+            const double *R = sys.num_rots > 0 ? sys.rots + 9 * rho : sys.bmat;
+            const int nb = rho == 0 ? ncols * nt : 0, ny = ncols * nl;
+            if (rho > 0) __syncthreads();     // the previous rotation's rows have read ylm
+            for (int w = threadIdx.x; w < nb + ny; w += blockDim.x) {
+                if (w < nb) {
+                    const int c = w / nt, t = w - c * nt;
+                    const double kn = kv[4 * c + 3];
+                    double fj[kMaxLmax + 1], dfj[kMaxLmax + 1];
+                    const double x = sys.type_rmt[t] * kn;
+                    sphbes_dev(sys.max_lmax, x, fj);
+                    dsphbs_dev(sys.max_lmax, x, fj, dfj);
+                    for (int l = 0; l < nl; ++l) {
+                        const int tl = t * nl + l;
+                        au[c * tnl + tl] = sys.dE_u[tl] * kn * dfj[l] - sys.dE_u_dr[tl] * fj[l];
+                        bu[c * tnl + tl] = -sys.u[tl] * kn * dfj[l] + sys.u_dr[tl] * fj[l];
+                    }
+                } else {
+                    const int q = w - nb, c = q / nl, m = q - c * nl;
+                    const double *k4 = kv + 4 * c;
+                    double v[3];
+                    for (int d = 0; d < 3; ++d) v[d] = R[d] * k4[0] + R[3 + d] * k4[1] + R[6 + d] * k4[2];
+                    const double nrm = sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+                    if (nrm > 0.0) { v[0] /= nrm; v[1] /= nrm; v[2] /= nrm; }
+                    ylm_column_dev(sys.max_lmax, m, v, sys.ynorm, ylm + c * L);
                 }
-            } else {
-                const int q = w - nb, c = q / nl, m = q - c * nl;
-                const double *k4 = kv + 4 * c;
-                double v[3];
-                for (int d = 0; d < 3; ++d) v[d] = sys.bmat[d] * k4[0] + sys.bmat[3 + d] * k4[1] + sys.bmat[6 + d] * k4[2];
-                const double nrm = sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
-                if (nrm > 0.0) { v[0] /= nrm; v[1] /= nrm; v[2] /= nrm; }
-                ylm_column_dev(sys.max_lmax, m, v, sys.ynorm, ylm + c * L);
             }
-        }
-        __syncthreads();
-        // the rows M_t = [A_t; B_t] / e^{i 2pi K.tau} of each column
-        for (int c = 0; c < ncols; ++c) {
-            const int64_t gc = col0 + c;
-            const KEntry &ent = tab.e[entry_of(tab, gc)];
-            if (!ent.M) continue;
-            double2 *mcol = ent.M + ldm * (gc - ent.col_begin);
-            for (int idx = threadIdx.x; idx < twoL * nt; idx += blockDim.x) {
-                const int t = idx / twoL;
-                const int r = idx - t * twoL;
-                const bool isB = r >= L;
-                const int lm = isB ? r - L : r;
-                const int l = l_of[lm];
-                double2 out = make_double2(0.0, 0.0);
-                if (l <= sys.type_lmax[t]) {
-                    const int tl = t * nl + l;
-                    const double cc = cf[tl];
-                    const double2 y = ylm[c * L + lm];
-                    const double f = isB ? bu[c * tnl + tl] : au[c * tnl + tl];
-                    out = make_double2((y.x * cc) * f, (-y.y * cc) * f);
+            __syncthreads();
+            // the rows M_t = [A_t; B_t] / e^{i 2pi K.tau} of each column (types with this rotation)
+            for (int c = 0; c < ncols; ++c) {
+                const int64_t gc = col0 + c;
+                const KEntry &ent = tab.e[entry_of(tab, gc)];
+                if (!ent.M) continue;
+                double2 *mcol = ent.M + ldm * (gc - ent.col_begin);
+                for (int idx = threadIdx.x; idx < twoL * nt; idx += blockDim.x) {
+                    const int t = idx / twoL;
+                    if (sys.num_rots > 0 && sys.type_rot[t] != rho) continue;
+                    const int r = idx - t * twoL;
+                    const bool isB = r >= L;
+                    const int lm = isB ? r - L : r;
+                    const int l = l_of[lm];
+                    double2 out = make_double2(0.0, 0.0);
+                    if (l <= sys.type_lmax[t]) {
+                        const int tl = t * nl + l;
+                        const double cc = cf[tl];
+                        const double2 y = ylm[c * L + lm];
+                        const double f = isB ? bu[c * tnl + tl] : au[c * tnl + tl];
+                        out = make_double2((y.x * cc) * f, (-y.y * cc) * f);
+                    }
+                    mcol[idx] = out;
                 }
-                mcol[idx] = out;
             }
         }
     }
@@ -556,12 +565,10 @@ cudaError_t launch_construct_ab_multi(const DevSystem &sys, const KTable &tab, c
     bool anyM = false, anyC = false;
     for (int k = 0; k < tab.nk; ++k) { anyM = anyM || tab.e[k].M; anyC = anyC || tab.e[k].C; }
     const bool rot = sys.atom_rotmat != nullptr;
-    const int nl_ = sys.max_lmax + 1, tnl_ = sys.num_types * nl_;
-    size_t smem_rows = sizeof(double2) * kRowCols * sys.L +
-                       sizeof(double) * (2 * kRowCols * tnl_ + tnl_ + 4 * kRowCols) + sys.L + 16;
-    smem_rows = (smem_rows + 15) & ~size_t(15);
-    // (the column-per-CTA kernel below for many types at a high lmax, whose tables do not fit)
-    if (!rot && anyM && !anyC && smem_rows <= 160 * 1024) {
+    const size_t smem_rows = rows_kernel_smem(sys.L, sys.max_lmax, sys.num_types);
+    // (the column-per-CTA kernel below for many types at a high lmax, whose tables do not fit;
+    // per-type rows of (type, rotation) classes come only from this kernel)
+    if ((!rot || sys.num_rots > 0) && anyM && !anyC && smem_rows <= kRowsKernelSmemMax) {
         const size_t smem = smem_rows;
         cudaError_t e = cudaFuncSetAttribute(construct_rows_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;

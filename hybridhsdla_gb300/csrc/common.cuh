@@ -35,7 +35,22 @@ struct DevSystem {
     const double *u, *u_dr, *dE_u, *dE_u_dr;
     const double *inv_w;        // 1 / (udot u' - u udot')
     const double *ynorm;        // [L] Y_lm normalisation (ylm4.f:111-137)
+    // Per-type rows of (type, rotation) classes: the types are the classes, type t's atoms share
+    // the rotation rots[9 type_rot[t] ..] (row-major mrot bmat).  num_rots = 0: every type's rows
+    // use R = bmat (no atom carries its own rotation).
+    int num_rots;
+    const double *rots;         // [num_rots][9]
+    const int32_t *type_rot;    // [t]
 };
+
+// Shared memory of the per-type rows kernel (construct_rows_kernel) for L lm, lmax max_lmax and
+// nt types; the kernel runs only where it fits (160 KB).
+inline size_t rows_kernel_smem(int L, int max_lmax, int nt) {
+    const int kRowCols = 16, nl = max_lmax + 1, tnl = nt * nl;
+    size_t b = sizeof(double) * 2 * kRowCols * L + sizeof(double) * (2 * kRowCols * tnl + tnl + 4 * kRowCols) + L + 16;
+    return (b + 15) & ~size_t(15);
+}
+constexpr size_t kRowsKernelSmemMax = 160 * 1024;
 
 struct DevKpoint {
     double k[3];

@@ -123,6 +123,7 @@ struct hsdla_plan {
     // structure-factor form (atoms share their type's rotation): per-type S weights [nt][2L] and
     // the structure factors SF_t over the box of G-vector differences
     bool sf = false;
+    int classes = 0;                 // (type, rotation) classes the structure-factor form runs over (0: types)
     double *wt = nullptr;
     double2 *sf_tab = nullptr;
     SfTab sf_dims{};                 // box extents and offsets (entries filled per group)
@@ -355,20 +356,93 @@ int validate(hsdla_context *ctx, const hsdla_system *s, const hsdla_kpoint *kpts
     return HSDLA_OK;
 }
 
+// (type, rotation) classes.  The reference gives every atom its own rotation mrot bmat
+// (FleurData.cpp:52-62, 453-455) and builds its rows with it (tensor_AB_match.cpp:97) while its
+// type supplies the radial data and T blocks.  Atoms of one type whose rotations are equal have
+// the same rows up to their structure phase, so the structure-factor form runs per class instead
+// of per type: a derived system whose types are the classes (each with its type's tables) and
+// whose rows carry the class's rotation.
+struct ClassSystem {
+    hsdla_system sys{};
+    int n = 0;                            // classes
+    std::vector<int32_t> atom_class, class_type, class_rot, lmax;
+    std::vector<double> rots, rmt, u, u_dr, dE_u, dE_u_dr, dE_u_norm;
+    std::vector<hsdla_cx> taa, tab, tbb;
+};
+
+// Builds the class system when it shrinks the work: the classes' rows (2L per class) are few
+// enough against the per-atom rows (2L per atom) to pay for the structure-factor combine, and
+// their table fits the per-type rows kernel.  Returns false otherwise (per-atom form).
+bool make_classes(const hsdla_system *s, ClassSystem &cs) {
+    if (!s->atom_rotmat) return false;
+    const int na = s->num_atoms, nt = s->num_types, nl = s->max_lmax + 1, L = nl * nl;
+    std::map<std::vector<uint64_t>, int> rot_id;
+    std::map<std::pair<int, int>, int> cls;
+    cs.atom_class.resize(na);
+    for (int j = 0; j < na; ++j) {
+        std::vector<uint64_t> bits(9);
+        memcpy(bits.data(), s->atom_rotmat + 9 * (size_t)j, 9 * sizeof(double));
+        auto r = rot_id.find(bits);
+        if (r == rot_id.end()) {
+            r = rot_id.emplace(bits, (int)rot_id.size()).first;
+            cs.rots.insert(cs.rots.end(), s->atom_rotmat + 9 * (size_t)j, s->atom_rotmat + 9 * (size_t)j + 9);
+        }
+        const auto key = std::make_pair((int)s->atom_type[j], r->second);
+        auto c = cls.find(key);
+        if (c == cls.end()) {
+            c = cls.emplace(key, (int)cls.size()).first;
+            cs.class_type.push_back(key.first);
+            cs.class_rot.push_back(key.second);
+        }
+        cs.atom_class[j] = c->second;
+    }
+    cs.n = (int)cls.size();
+    if (4 * cs.n > 3 * na || cs.n > kMaxTypes || rows_kernel_smem(L, s->max_lmax, cs.n) > kRowsKernelSmemMax)
+        return false;
+    const int n = cs.n;
+    cs.rmt.resize(n); cs.lmax.resize(n);
+    for (auto *v : {&cs.u, &cs.u_dr, &cs.dE_u, &cs.dE_u_dr, &cs.dE_u_norm}) v->resize((size_t)n * nl);
+    for (auto *v : {&cs.taa, &cs.tab, &cs.tbb}) v->resize((size_t)n * L * L);
+    for (int c = 0; c < n; ++c) {
+        const int t = cs.class_type[c];
+        cs.rmt[c] = s->type_rmt[t];
+        cs.lmax[c] = s->type_lmax[t];
+        const double *src[5] = {s->type_u, s->type_u_dr, s->type_dE_u, s->type_dE_u_dr, s->type_dE_u_norm};
+        std::vector<double> *dst[5] = {&cs.u, &cs.u_dr, &cs.dE_u, &cs.dE_u_dr, &cs.dE_u_norm};
+        for (int q = 0; q < 5; ++q) memcpy(dst[q]->data() + (size_t)c * nl, src[q] + (size_t)t * nl, nl * sizeof(double));
+        const hsdla_cx *tsrc[3] = {s->type_t_aa, s->type_t_ab, s->type_t_bb};
+        std::vector<hsdla_cx> *tdst[3] = {&cs.taa, &cs.tab, &cs.tbb};
+        for (int q = 0; q < 3; ++q)
+            memcpy(tdst[q]->data() + (size_t)c * L * L, tsrc[q] + (size_t)t * L * L, (size_t)L * L * sizeof(hsdla_cx));
+    }
+    hsdla_system &d = cs.sys;
+    d = *s;
+    d.num_types = n;
+    d.atom_type = cs.atom_class.data();
+    d.type_rmt = cs.rmt.data();
+    d.type_lmax = cs.lmax.data();
+    d.type_u = cs.u.data(); d.type_u_dr = cs.u_dr.data(); d.type_dE_u = cs.dE_u.data();
+    d.type_dE_u_dr = cs.dE_u_dr.data(); d.type_dE_u_norm = cs.dE_u_norm.data();
+    d.type_t_aa = cs.taa.data(); d.type_t_ab = cs.tab.data(); d.type_t_bb = cs.tbb.data();
+    return true;
+}
+
 // The T blocks' checks, made on the device while they were assembled (launch_tfull): finite
 // values, and T_AA and T_BB Hermitian (AtomData.cpp:138-139 asserts it), |T - T^H|^2 against
 // |T|^2 over the lower triangle (its mirror element is the pair's other half).
-int check_tmats(hsdla_context *ctx, const std::vector<unsigned long long> &st, int nt) {
+int check_tmats(hsdla_context *ctx, const std::vector<unsigned long long> &st, int nt,
+                const std::vector<int32_t> *class_type = nullptr) {
     auto as_double = [](unsigned long long b) { double d; memcpy(&d, &b, sizeof(d)); return d; };
     for (int t = 0; t < nt; ++t) {
+        const int ty = class_type ? (*class_type)[t] : t;    // the caller's type of a class
         const unsigned long long fl = st[5 * (size_t)t];
         for (int q = 0; q < 3; ++q)
-            if (fl & (1ull << q)) return set_err(ctx, HSDLA_ERR_INPUT, "T block %d of type %d not finite", q, t);
+            if (fl & (1ull << q)) return set_err(ctx, HSDLA_ERR_INPUT, "T block %d of type %d not finite", q, ty);
         for (int q = 0; q < 2; ++q) {
             const double mx2 = as_double(st[5 * (size_t)t + 1 + 2 * q]), dev2 = as_double(st[5 * (size_t)t + 2 + 2 * q]);
             if (dev2 > 1e-24 * std::max(mx2, 1e-300))
                 return set_err(ctx, HSDLA_ERR_INPUT, "T_%s of type %d is not Hermitian (|T-T^H| = %.3g)",
-                               q == 0 ? "AA" : "BB", t, std::sqrt(dev2));
+                               q == 0 ? "AA" : "BB", ty, std::sqrt(dev2));
         }
     }
     return HSDLA_OK;
@@ -633,8 +707,16 @@ int hsdla_plan_create(hsdla_context *ctx, const hsdla_system *s, const hsdla_kpo
     CUDA_TRY(ctx, cudaSetDevice(ctx->device));
     int rc = validate(ctx, s, kpts, nk);
     if (rc) return rc;
+    // atoms with rotations: (type, rotation) classes keep the structure-factor form where they
+    // shrink the work (HSDLA_SF=0 or HSDLA_CLASSES=0 keeps the per-atom form)
+    const char *sf_env0 = getenv("HSDLA_SF");
+    ClassSystem cls;
+    const bool use_classes = s->atom_rotmat && !(sf_env0 && strtol(sf_env0, nullptr, 10) == 0) &&
+                             env_flag("HSDLA_CLASSES", true) && make_classes(s, cls);
+    if (use_classes) s = &cls.sys;
     auto *pl = new hsdla_plan();
     pl->ctx = ctx;
+    pl->classes = use_classes ? cls.n : 0;
     if (opts) pl->opts = *opts;
     if (pl->opts.precision != HSDLA_PREC_FP64 && pl->opts.precision != HSDLA_PREC_OZAKI_FP8) {
         delete pl;
@@ -643,7 +725,7 @@ int hsdla_plan_create(hsdla_context *ctx, const hsdla_system *s, const hsdla_kpo
     if (pl->opts.target_rel_err <= 0.0) pl->opts.target_rel_err = 1e-13;
     const int na = s->num_atoms, nt = s->num_types, nl = s->max_lmax + 1, L = nl * nl;
     pl->L = L; pl->na = na; pl->nt = nt; pl->max_lmax = s->max_lmax;
-    pl->hoist = s->atom_rotmat == nullptr;
+    pl->hoist = s->atom_rotmat == nullptr || use_classes;
     pl->twoLa = 2 * (int64_t)L * na;
     pl->atom_type.assign(s->atom_type, s->atom_type + na);
 
@@ -673,6 +755,7 @@ int hsdla_plan_create(hsdla_context *ctx, const hsdla_system *s, const hsdla_kpo
     int64_t bytes = 0;
     auto add = [&](int64_t b) { bytes += (b + 255) & ~int64_t(255); };
     add(sizeof(int32_t) * na); add(sizeof(double) * 3 * na); add(s->atom_rotmat ? sizeof(double) * 9 * na : 0);
+    add(use_classes ? sizeof(double) * cls.rots.size() : 0); add(use_classes ? sizeof(int32_t) * nt : 0);
     add(sizeof(double) * nt); add(sizeof(int32_t) * nt);
     for (int q = 0; q < 5; ++q) add(sizeof(double) * nt * nl);
     add(sizeof(double) * L);
@@ -733,6 +816,11 @@ int hsdla_plan_create(hsdla_context *ctx, const hsdla_system *s, const hsdla_kpo
     D.atom_type = (const int32_t *)put(s->atom_type, sizeof(int32_t) * na);
     D.atom_pos = (const double *)put(s->atom_pos, sizeof(double) * 3 * na);
     D.atom_rotmat = s->atom_rotmat ? (const double *)put(s->atom_rotmat, sizeof(double) * 9 * na) : nullptr;
+    if (use_classes) {
+        D.num_rots = (int)(cls.rots.size() / 9);
+        D.rots = (const double *)put(cls.rots.data(), sizeof(double) * cls.rots.size());
+        D.type_rot = (const int32_t *)put(cls.class_rot.data(), sizeof(int32_t) * nt);
+    }
     D.type_rmt = (const double *)put(s->type_rmt, sizeof(double) * nt);
     D.type_lmax = (const int32_t *)put(s->type_lmax, sizeof(int32_t) * nt);
     D.u = (const double *)put(s->type_u, sizeof(double) * nt * nl);
@@ -810,7 +898,7 @@ int hsdla_plan_create(hsdla_context *ctx, const hsdla_system *s, const hsdla_kpo
         hsdla_plan_destroy(pl);
         return set_err(ctx, HSDLA_ERR_CUDA, "table upload failed: %s", cudaGetErrorString(e));
     }
-    rc = check_tmats(ctx, tstats, nt);
+    rc = check_tmats(ctx, tstats, nt, use_classes ? &cls.class_type : nullptr);
     if (rc) { hsdla_plan_destroy(pl); return rc; }
     if (pl->opts.precision == HSDLA_PREC_OZAKI_FP8) {
         pl->autotune = pl->opts.num_slices == 0;
@@ -1470,6 +1558,8 @@ int hsdla_plan_execute(hsdla_plan *pl, hsdla_cx *const *dH, hsdla_cx *const *dS,
         rep->est_rel_err = pl->est_err;
         rep->kernel_launches = pl->launches;
         rep->num_panels = pl->opts.precision == HSDLA_PREC_OZAKI_FP8 ? pl->panels : 0;
+        rep->num_row_sets = pl->sf ? pl->nt : 0;
+        rep->rotation_classes = pl->classes > 0 ? 1 : 0;
     }
     return HSDLA_OK;
 }

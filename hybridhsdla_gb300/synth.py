@@ -126,6 +126,10 @@ CONFIGS: Dict[str, dict] = {
     # few GB of device memory (the case profiled in full)
     "c2t1": dict(cell=(24.0, 24.0, 24.0), atoms=16, types=1, rmt=2.0, min_sep=4.0,
                  lmax=10, kpts=[(0.1, 0.2, 0.3)], n_g=8000, seed=1002),
+    # c2 with rotations, as a Fleur dump gives them: the atoms of each type in two rotation
+    # classes (one the identity), 16 (type, rotation) classes
+    "c2r": dict(cell=(24.0, 24.0, 24.0), atoms=128, types=8, rmt=2.0, min_sep=4.0,
+                lmax=10, kpts=[(0.1, 0.2, 0.3)], n_g=8000, seed=1002, rot_classes=2),
     # tiny cases for fast parity tests
     "t0": dict(cell=(9.0, 9.5, 10.0), atoms=3, types=2, rmt=2.0, min_sep=4.2,
                lmax=3, kpts=[(0.1, 0.2, 0.3)], n_g=37, seed=7),
@@ -269,11 +273,40 @@ def make_system(cfg: str | dict, *, n_kpoints: Optional[int] = None,
         kvec = np.asarray(kk, dtype=np.float64)
         kpoints.append(KPoint(k=kvec, g=g_vectors(bmat, kvec, target)))
 
-    return System(real_basis=real_basis, bmat=bmat, vol_cell=vol, atom_type=atom_type,
-                  atom_pos=atom_pos, atom_rotmat=None, type_rmt=type_rmt, type_lmax=type_lmax,
-                  type_lmax_nonsph=type_lmax_nonsph, u=u, u_dr=u_dr, dE_u=dE_u, dE_u_dr=dE_u_dr,
-                  dE_u_norm=dE_u_norm, energies=energies, taa_raw=taa, tbb_raw=tbb, tab_raw=tab,
-                  kpoints=kpoints, name=name)
+    out = System(real_basis=real_basis, bmat=bmat, vol_cell=vol, atom_type=atom_type,
+                 atom_pos=atom_pos, atom_rotmat=None, type_rmt=type_rmt, type_lmax=type_lmax,
+                 type_lmax_nonsph=type_lmax_nonsph, u=u, u_dr=u_dr, dE_u=dE_u, dE_u_dr=dE_u_dr,
+                 dE_u_norm=dE_u_norm, energies=energies, taa_raw=taa, tbb_raw=tbb, tab_raw=tab,
+                 kpoints=kpoints, name=name)
+    if c.get("rot_classes"):
+        out = with_class_rotations(out, per_type=int(c["rot_classes"]))
+    return out
+
+
+def _rotation(rng: np.random.Generator) -> np.ndarray:
+    q, r = np.linalg.qr(rng.standard_normal((3, 3)))
+    q = q * np.sign(np.diag(r))[None, :]
+    if np.linalg.det(q) < 0:
+        q[:, 0] = -q[:, 0]
+    return q
+
+
+def with_class_rotations(sys_: System, per_type: int = 2, seed: int = 77, identity_first: bool = True) -> System:
+    """Copy of ``sys_`` whose atoms carry rotations shared within classes: the atoms of each type
+    are dealt round-robin into ``per_type`` classes, each class with one seeded proper rotation
+    (the first the identity when ``identity_first``), stored as ``mrot @ bmat`` like
+    ``FleurData.cpp:453-455``.  This is the situation of a Fleur dump: one rotation per atom,
+    equal for the atoms a symmetry operation maps onto each other."""
+    rng = np.random.default_rng(seed)
+    rots = np.zeros((sys_.num_atoms, 3, 3))
+    for t in range(sys_.num_types):
+        atoms = np.flatnonzero(sys_.atom_type == t)
+        mats = [np.eye(3) if (identity_first and c == 0) else _rotation(rng) for c in range(per_type)]
+        for i, j in enumerate(atoms):
+            rots[j] = mats[i % per_type] @ sys_.bmat
+    out = dataclasses.replace(sys_)
+    out.atom_rotmat = rots
+    return out
 
 
 def with_rotations(sys_: System, seed: int = 99) -> System:

@@ -124,7 +124,10 @@ typedef struct hsdla_report {
     int32_t kernel_launches;     /* kernels launched per execution */
     int32_t num_panels;          /* Ozaki: atom panels the contraction was streamed in (1 = resident) */
     int32_t outputs_in_place;    /* hsdla_create_hs: 1 = the GPU wrote the page-locked host H, S itself */
-    int32_t reserved[3];
+    int32_t num_row_sets;        /* structure-factor form: the row sets contracted (types, or (type, rotation)
+                                    classes when atoms carry rotations); 0 = the per-atom form */
+    int32_t rotation_classes;    /* 1: the row sets are (type, rotation) classes */
+    int32_t reserved[1];
 } hsdla_report;
 
 typedef struct hsdla_context hsdla_context;
