@@ -1710,7 +1710,9 @@ struct OzGroup {
     bool pair = false;          // S/H on CTA-pair tiles
     PairUnits units{};          // their accumulation units
     PairUnits units_t{};        // the T application's (structure-factor form on pair tiles)
-    int halves = 1;             // 2: structure-factor launches on half-width pair tiles
+    int halves = 1;             // 2: structure-factor S/H launches on half-width pair tiles
+    int halves_t = 1;           // the same for the T application
+    bool merged = true;         // S/H units merge adjacent digit diagonals where exact
     bool sf = false;            // structure-factor form
     int tbatch = 1;             // its types per combine batch
     // with one batch: the first side_types types are combined on a side stream while the S/H
@@ -1983,11 +1985,13 @@ static int group_prepare_sf(OzakiPlan &oz, const OzGroupDesc &d, const std::vect
     if (!rc) rc = make_map(g->dW, s);
     if (!rc) rc = make_map(g->dX, s);
     if (!rc) rc = make_map(g->dT, g->pair ? 2 * s : s);
-    // half-width pair tiles (HSDLA_PAIR_HALVES=1: full width): the right operands' 64-row maps
+    // half-width pair tiles (HSDLA_PAIR_HALVES=1: full width; the tile tuner may switch the S/H
+    // launches): the right operands' 64-row maps, made for both shapes
     g->halves = g->pair && env_int("HSDLA_PAIR_HALVES", 2) == 2 ? 2 : 1;
-    if (!rc && g->halves == 2) rc = make_map(g->dM, 2 * s, kPairTile / 4, &g->dM.map64);
-    if (!rc && g->halves == 2) rc = make_map(g->dW, s, kPairTile / 4, &g->dW.map64);
-    if (!rc && g->halves == 2) rc = make_map(g->dX, s, kPairTile / 4, &g->dX.map64);
+    g->halves_t = g->halves;
+    if (!rc && g->pair) rc = make_map(g->dM, 2 * s, kPairTile / 4, &g->dM.map64);
+    if (!rc && g->pair) rc = make_map(g->dW, s, kPairTile / 4, &g->dW.map64);
+    if (!rc && g->pair) rc = make_map(g->dX, s, kPairTile / 4, &g->dX.map64);
     if (rc) return fail(rc);
     // T application per type: Z_t = T_t M_t
     std::vector<OzJob> jt;
@@ -2010,11 +2014,12 @@ static int group_prepare_sf(OzakiPlan &oz, const OzGroupDesc &d, const std::vect
     rc = upload_schedule(jt, g->d_jobs_t, g->d_list_t, g->tiles_t, g->pair ? kPairTile : kTileN);
     g->units_t = g->pair ? pair_units(s, tkb, env_int("HSDLA_MERGE", 1) != 0) : pair_units_plain(s);
     if (rc) return fail(rc);
-    g->maps_t[0] = g->halves == 2 ? g->dM.map64 : g->dM.map;    // right operand
+    g->maps_t[0] = g->halves_t == 2 ? g->dM.map64 : g->dM.map;  // right operand
     g->maps_t[1] = g->dM.map; g->maps_t[2] = g->dM.map; g->maps_t[3] = g->dT.map;
     // per type: S_t = M_t^H diag(w_t) M_t and H_t = M_t^H Z_t into the products; on pair tiles
     // with merged accumulation units (HSDLA_MERGE=0: one per diagonal)
-    g->units = g->pair ? pair_units(s, tkb, env_int("HSDLA_MERGE", 1) != 0) : pair_units_plain(s);
+    g->merged = env_int("HSDLA_MERGE", 1) != 0;
+    g->units = g->pair ? pair_units(s, tkb, g->merged) : pair_units_plain(s);
     const int64_t tile = g->pair ? kPairTile : kTileN;
     g->n_jobs_sh = 2 * g->nk;
     std::vector<OzJob> all;
@@ -2299,7 +2304,7 @@ int ozaki_group_run(OzGroup *g, const DevSystem &sys, const KTable &ktab, cudaSt
         if (e == cudaSuccess && tev) e = cudaEventRecord(ev_t[0], st);
         if (e == cudaSuccess)
             e = g->pair ? launch_pair(g->maps_t, g->s, g->d_err, g->d_jobs_t, g->n_jobs_t, g->tiles_t, g->d_list_t,
-                                      nullptr, st, g->units_t, g->halves)
+                                      nullptr, st, g->units_t, g->halves_t)
                         : launch_prepared(g->maps_t, g->s, g->d_err, g->d_jobs_t, g->n_jobs_t, g->tiles_t,
                                           g->d_list_t, nullptr, st);
         if (e == cudaSuccess && tev) e = cudaEventRecord(ev_t[1], st);
@@ -2407,6 +2412,72 @@ int ozaki_group_run(OzGroup *g, const DevSystem &sys, const KTable &ktab, cudaSt
     if (e == cudaSuccess && ev1) e = record(ev1, st);
     if (launches) *launches = nl;
     if (e != cudaSuccess) { g_oz_err = cudaGetErrorString(e); return HSDLA_ERR_CUDA; }
+    return HSDLA_OK;
+}
+
+// The structure-factor form's S/H tile configuration: tile shape (halves 1: 256 x 256
+// accumulators; 2: two 256 x 128 halves in alternating TMEM buffers) and accumulation split
+// (merged: adjacent digit diagonals share an exact FP32 unit; else one unit per diagonal).
+static void set_sh_tiles(OzGroup *g, int halves, bool merged) {
+    g->halves = halves;
+    g->merged = merged;
+    g->units = pair_units(g->s, g->bpad / kKBlock, merged);
+    g->maps_sh[1] = halves == 2 ? g->dW.map64 : g->dW.map;
+    g->maps_sh[2] = halves == 2 ? g->dX.map64 : g->dX.map;
+}
+
+bool ozaki_group_tunable(const OzGroup *g) { return g && g->sf && g->pair; }
+
+void ozaki_group_tiles(const OzGroup *g, int *halves, int *merged) {
+    *halves = g->halves;
+    *merged = g->merged ? 1 : 0;
+}
+
+void ozaki_group_set_tiles(OzGroup *g, int halves, int merged) {
+    if (ozaki_group_tunable(g)) set_sh_tiles(g, halves == 1 ? 1 : 2, merged != 0);
+}
+
+// Times the first type's S/H launch (every k-point of the group) in each configuration and keeps
+// the fastest.  The digit planes must hold a completed run's data (the launches only rewrite that
+// type's product slot, which the run has combined already).  Each configuration runs twice, the
+// second timed.
+int ozaki_group_tune_tiles(OzGroup *g, cudaStream_t st, float *ms_best) {
+    if (!ozaki_group_tunable(g)) return HSDLA_OK;
+    const int cfg[4][2] = {{2, 1}, {1, 1}, {2, 0}, {1, 0}};
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) {
+        if (e0) cudaEventDestroy(e0);
+        g_oz_err = "tile tuner: event creation failed";
+        return HSDLA_ERR_CUDA;
+    }
+    const int h0 = g->halves;
+    const bool m0 = g->merged;
+    float best = -1.f;
+    int bi = 0;
+    cudaError_t e = cudaSuccess;
+    for (int c = 0; c < 4 && e == cudaSuccess; ++c) {
+        set_sh_tiles(g, cfg[c][0], cfg[c][1] != 0);
+        for (int rep = 0; rep < 2 && e == cudaSuccess; ++rep) {
+            if (rep == 1) e = cudaEventRecord(e0, st);
+            if (e == cudaSuccess)
+                e = launch_pair(g->maps_sh, g->s, g->d_err, g->d_jobs_sh, g->n_jobs_sh, g->tiles_sh, g->d_list_sh,
+                                nullptr, st, g->units, g->halves);
+            if (e == cudaSuccess && rep == 1) e = cudaEventRecord(e1, st);
+        }
+        if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+        float ms = 0.f;
+        if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+        if (e == cudaSuccess && (best < 0.f || ms < best)) { best = ms; bi = c; }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (e != cudaSuccess) {
+        set_sh_tiles(g, h0, m0);
+        g_oz_err = cudaGetErrorString(e);
+        return HSDLA_ERR_CUDA;
+    }
+    set_sh_tiles(g, cfg[bi][0], cfg[bi][1] != 0);
+    if (ms_best) *ms_best = best;
     return HSDLA_OK;
 }
 

@@ -88,6 +88,15 @@ int ozaki_group_run(OzGroup *g, const DevSystem &sys, const KTable &ktab, cudaSt
 // Event pairs ozaki_group_run records around the group's T application (see ev_t).
 int ozaki_group_tapply_events(const OzGroup *g);
 void ozaki_group_destroy(OzGroup *g);
+// The structure-factor form's S/H tile configuration on CTA-pair tiles: halves 1 (256 x 256
+// accumulators) or 2 (two 256 x 128 halves), merged 1 (adjacent digit diagonals share exact
+// accumulation units) or 0.  Tunable: a structure-factor group on pair tiles.
+bool ozaki_group_tunable(const OzGroup *g);
+void ozaki_group_tiles(const OzGroup *g, int *halves, int *merged);
+void ozaki_group_set_tiles(OzGroup *g, int halves, int merged);
+// Times the first type's S/H launch in each configuration on the digit planes of a completed
+// run and keeps the fastest (ms_best: its time).
+int ozaki_group_tune_tiles(OzGroup *g, cudaStream_t st, float *ms_best);
 
 int ozaki_plan_init(OzakiPlan &oz, int num_slices, double target);
 void ozaki_plan_release(OzakiPlan &oz);
