@@ -205,6 +205,54 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def secondary_workload(ctx, name: str, steps: int, oracle_n: int) -> dict:
+    """One more workload on the same GPU: every k-point of it in one plan (k-point groups, one
+    launch per stage, captured in a CUDA graph), `steps` timed executions after one warm-up, and
+    the first k-point checked on a random subset of its G-vectors against the oracle."""
+    import numpy as np
+    import torch
+
+    from hybridhsdla_gb300 import synth
+    sys_ = synth.make_system(name)
+    t0 = time.perf_counter()
+    plan = ctx.plan(sys_, precision="ozaki", num_slices=0, use_graph=True)
+    outs = plan.alloc_outputs()
+    rep = plan.execute(outs)                         # slice autotune, tile tuning, graph capture
+    plan.execute(outs)
+    torch.cuda.synchronize()
+    setup_s = time.perf_counter() - t0
+    stream = torch.cuda.current_stream()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for _ in range(steps):
+        rep = plan.execute(outs)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    ms = ev0.elapsed_time(ev1) / steps
+    nk = len(sys_.kpoints)
+    flop = sys_.total_flop()
+    out = {"workload": WORKLOAD_TEXT.get(name, name), "kpoints": nk, "ms_total": ms, "ms_per_kpoint": ms / nk,
+           "value": flop / (ms * 1e-3) / 1e12, "unit": UNIT, "steps": steps, "num_slices": rep["num_slices"],
+           "tile_halves": rep["tile_halves"], "merged_units": rep["merged_units"],
+           "tile_tuned": rep["tile_tuned"], "kernel_launches": rep["kernel_launches"],
+           "setup_s": round(setup_s, 2), "graph": True}
+    if oracle_n > 0:
+        import oracle
+        kp = sys_.kpoints[0]
+        idx = np.sort(np.random.default_rng(77).choice(kp.n_g, min(oracle_n, kp.n_g), replace=False))
+        Hr, Sr = oracle.reference_hs(sys_, synth.KPoint(k=kp.k, g=kp.g[idx]))
+        ti = torch.from_numpy(idx).to(outs[0][0].device)
+        errs = {}
+        for nm, Xd, R in (("H", outs[0][0], Hr), ("S", outs[0][1], Sr)):
+            X = np.tril(Xd.index_select(0, ti).index_select(1, ti).cpu().numpy().T)
+            errs[nm + "_fro"], errs[nm + "_max"] = oracle.lower_errors(X, R)
+        out["oracle_random_subset"] = {"n": len(idx), "kpoint": 0, **errs}
+    plan.close()
+    del outs
+    torch.cuda.empty_cache()
+    return out
+
+
 def run_ours(args):
     import numpy as np
     import torch
@@ -370,6 +418,15 @@ def run_ours(args):
             cpu = {"value": samp["value"], "unit": UNIT, "cores": threads, "kind": "port",
                    "sample": samp["sample"] + f", {s_:.1f} s"}
 
+    # ---- the batching and large combined workloads on the same GPU (evidence beside the headline)
+    extra = {}
+    if rank == 0 and ws == 1:
+        for name in [w for w in args.also.split(",") if w]:
+            try:
+                extra[name] = secondary_workload(ctx, name, args.also_steps, args.also_oracle)
+            except Exception as exc:      # reported, not fatal: the headline line still prints
+                extra[name] = {"error": f"{type(exc).__name__}: {exc}"}
+
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
@@ -387,11 +444,16 @@ def run_ours(args):
                         "note": "hsdla_create_hs on the rank's first k-point, pinned host buffers; "
                                 "value = mean over calls_ms"},
                 "gpu_launches": launches,
+                "tiles": {"halves": rep["tile_halves"], "merged_units": rep["merged_units"],
+                          "tuned": rep["tile_tuned"], "row_sets": rep["num_row_sets"],
+                          "rotation_classes": rep["rotation_classes"]},
                 "stage_ms": {"construct_ab": rep["ms_construct_ab"], "tapply": rep["ms_tapply"],
                              "contract": rep["ms_contract"], "dominant": dom},
                 "fp64": fp64, "roofline": roof, "cpu_baseline": cpu, "clocks": clk.summary()}
         if block is not None:
             line["oracle_block"] = block
+        if extra:
+            line["workloads"] = extra
         if rep.get("num_panels", 1) > 1:
             line["config"]["atom_panels"] = rep["num_panels"]
         print(json.dumps(line), flush=True)
@@ -415,6 +477,11 @@ def main():
     ap.add_argument("--cpu-full", type=int, default=1,
                     help="1: time the reference CPU path on one full k-point of the workload once")
     ap.add_argument("--e2e-calls", type=int, default=8, help="end-to-end calls through hsdla_create_hs")
+    ap.add_argument("--also", default="c3,c4",
+                    help="further workloads timed after the headline (comma list; empty = none)")
+    ap.add_argument("--also-steps", type=int, default=2)
+    ap.add_argument("--also-oracle", type=int, default=256,
+                    help="random-subset size of the oracle check of each further workload's first k-point")
     ap.add_argument("--skip-fp64", action="store_true")
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--workload", default=WORKLOAD, choices=sorted(WORKLOAD_TEXT),

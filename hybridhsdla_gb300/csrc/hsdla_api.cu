@@ -63,6 +63,9 @@ struct hsdla_context {
     std::map<std::tuple<int, int, int, int64_t, double>, std::pair<int, double>> tune_cache;
     // the BLAS-shaped plugin's Ozaki state (its device error word), set up on first use
     OzakiPlan plugin_oz{};
+    // tile tuner results of the structure-factor form: (2L, row sets, k-points of the first group,
+    // its largest n_G bucket, slices) -> (halves, merged)
+    std::map<std::tuple<int, int, int, int64_t, int>, std::pair<int, int>> tile_cache;
 };
 
 struct PlanKpoint {
@@ -140,6 +143,9 @@ struct hsdla_plan {
     Download *dl = nullptr;
     double est_err = 0.0;            // autotuner's predicted relative error
     int launches = 0;
+    bool tiles_tuned = false;        // the S/H tile configuration came from the tile tuner
+    bool tiles_done = false;         // nothing (more) to tune
+    int tile_h = 0, tile_m = 0;      // the tuned configuration (re-applied when groups are re-prepared)
 };
 
 namespace {
@@ -1414,6 +1420,48 @@ int run_groups(hsdla_plan *pl, cudaStream_t st, bool timed, float *ms_ab, float 
     return HSDLA_OK;
 }
 
+// The tile tuner of the structure-factor form (after a plan's first completed run): the S/H
+// tile shape and accumulation split timed on this data, or taken from the context's cache for
+// this shape, then set on every group.  HSDLA_PAIR_HALVES or HSDLA_MERGE in the environment, or
+// HSDLA_TILE_TUNE=0, keep the configuration the groups were prepared with.
+int tune_tiles(hsdla_plan *pl, cudaStream_t st) {
+    hsdla_context *ctx = pl->ctx;
+    pl->tiles_done = true;
+    if (pl->groups.empty() || !pl->groups[0].oz || !ozaki_group_tunable(pl->groups[0].oz)) return HSDLA_OK;
+    if (getenv("HSDLA_PAIR_HALVES") || getenv("HSDLA_MERGE") || !env_flag("HSDLA_TILE_TUNE", true)) return HSDLA_OK;
+    const auto &g0 = pl->groups[0];
+    int64_t gmax = 0;
+    for (int i : g0.kidx) gmax = std::max(gmax, pl->kps[i].n_g);
+    const auto key = std::make_tuple(2 * pl->L, pl->nt, (int)g0.kidx.size(), (gmax + 511) / 512, pl->oz.num_slices);
+    int h = 0, m = 0;
+    auto hit = ctx->tile_cache.find(key);
+    if (hit != ctx->tile_cache.end()) {
+        h = hit->second.first;
+        m = hit->second.second;
+    } else {
+        float best = 0.f;
+        const int rc = ozaki_group_tune_tiles(g0.oz, st, &best);
+        if (rc) return set_err(ctx, rc, "tile tuner: %s", ozaki_last_error());
+        const int rce = ozaki_check_device_error(pl->oz);
+        if (rce) return set_err(ctx, rce, "tile tuner: device-side error: %s", ozaki_last_error());
+        ozaki_group_tiles(g0.oz, &h, &m);
+        ctx->tile_cache[key] = std::make_pair(h, m);
+    }
+    int h0 = 0, m0 = 0;
+    ozaki_group_tiles(g0.oz, &h0, &m0);
+    for (auto &g : pl->groups) ozaki_group_set_tiles(g.oz, h, m);
+    pl->tiles_tuned = true;
+    pl->tile_h = h;
+    pl->tile_m = m;
+    // a captured graph holds the old launch parameters
+    if ((h != h0 || m != m0) && pl->graph) {
+        cudaGraphExecDestroy(pl->graph);
+        pl->graph = nullptr;
+        pl->graph_outputs.clear();
+    }
+    return HSDLA_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -1483,6 +1531,8 @@ int hsdla_plan_execute(hsdla_plan *pl, hsdla_cx *const *dH, hsdla_cx *const *dS,
         release_groups(pl);
         rc = prepare_groups(pl, ws, st);
         if (rc) { release_groups(pl); return rc; }
+        if (pl->tiles_tuned)
+            for (auto &g : pl->groups) ozaki_group_set_tiles(g.oz, pl->tile_h, pl->tile_m);
     }
     set_outputs(pl, dH, dS, ld);
     float ms_ab = 0.f, ms_tap = 0.f;
@@ -1540,9 +1590,14 @@ int hsdla_plan_execute(hsdla_plan *pl, hsdla_cx *const *dH, hsdla_cx *const *dS,
     CUDA_TRY(ctx, cudaEventSynchronize(ctx->evs[3]));
     rc = ozaki_check_device_error(pl->oz);
     if (rc) return set_err(ctx, rc, "device-side error: %s", ozaki_last_error());
+    float ms_run = 0.f;
+    cudaEventElapsedTime(&ms_run, ctx->evs[2], ctx->evs[3]);
+    if (!pl->tiles_done) {
+        rc = tune_tiles(pl, run_st);
+        if (rc) return rc;
+    }
     if (rep) {
-        float ms = 0.f;
-        cudaEventElapsedTime(&ms, ctx->evs[2], ctx->evs[3]);
+        const float ms = ms_run;
         memset(rep, 0, sizeof(*rep));
         rep->ms_total = ms;
         rep->num_kpoints = nk;
@@ -1560,6 +1615,13 @@ int hsdla_plan_execute(hsdla_plan *pl, hsdla_cx *const *dH, hsdla_cx *const *dS,
         rep->num_panels = pl->opts.precision == HSDLA_PREC_OZAKI_FP8 ? pl->panels : 0;
         rep->num_row_sets = pl->sf ? pl->nt : 0;
         rep->rotation_classes = pl->classes > 0 ? 1 : 0;
+        if (!pl->groups.empty() && pl->groups[0].oz && ozaki_group_tunable(pl->groups[0].oz)) {
+            int h = 0, m = 0;
+            ozaki_group_tiles(pl->groups[0].oz, &h, &m);
+            rep->tile_halves = h;
+            rep->merged_units = m;
+            rep->tile_tuned = pl->tiles_tuned ? 1 : 0;
+        }
     }
     return HSDLA_OK;
 }

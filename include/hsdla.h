@@ -127,7 +127,11 @@ typedef struct hsdla_report {
     int32_t num_row_sets;        /* structure-factor form: the row sets contracted (types, or (type, rotation)
                                     classes when atoms carry rotations); 0 = the per-atom form */
     int32_t rotation_classes;    /* 1: the row sets are (type, rotation) classes */
-    int32_t reserved[1];
+    int32_t tile_halves;         /* Ozaki, structure-factor form: S/H tiles as 256 x 256 accumulators (1) or */
+                                 /* two 256 x 128 halves in alternating TMEM buffers (2); 0 otherwise */
+    int32_t merged_units;        /* the same launches: 1 = adjacent digit diagonals share exact accumulation units */
+    int32_t tile_tuned;          /* 1 = those two were chosen by timing on this plan's data (or a cached result) */
+    int32_t reserved[2];
 } hsdla_report;
 
 typedef struct hsdla_context hsdla_context;
