@@ -86,7 +86,7 @@ EXPORTS = ["hsdla_context_create", "hsdla_context_destroy", "hsdla_last_error", 
            "hsdla_zherkx_lower", "hsdla_zherkx_lower_noalloc", "hsdla_contract_ab", "hsdla_pack_lower",
            "hsdla_selftest_wait_timeout", "hsdla_zherk", "hsdla_zher2k", "hsdla_zherkx", "hsdla_dev_init",
            "hsdla_dev_finalize", "hsdla_dev_context", "hsdla_dev_status", "hsdla_dev_zherk_", "hsdla_dev_zher2k_",
-           "hsdla_dev_zherkx_"]
+           "hsdla_dev_zherkx_", "hsdla_radial_match"]
 
 _lib = None
 
@@ -155,6 +155,7 @@ def load(build_if_missing: bool = True):
     L.hsdla_dev_zher2k_.restype = None
     L.hsdla_dev_zherkx_.argtypes = [cp, cp, ip, ip, _cxp, vp, ip, vp, ip, _dp, vp, ip]
     L.hsdla_dev_zherkx_.restype = None
+    L.hsdla_radial_match.argtypes = [i32, dbl, _dp, i32, dbl, dbl, _dp]
     _lib = L
     return L
 

@@ -249,6 +249,16 @@ void hsdla_dev_zherkx_(const char *uplo, const char *trans, const int *n, const 
                        const hsdla_cx *A, const int *lda, const hsdla_cx *B, const int *ldb, const double *beta,
                        hsdla_cx *C, const int *ldc);
 
+/* Matching values of one (type, l): Fleur's scalar-relativistic radial solution u_l and its energy
+ * derivative udot_l at energy e for the potential r V(r) on Fleur's logarithmic mesh of n points
+ * (r_i = R_MT e^{(i - n) dx}, i = 1..n), evaluated at R_MT: out = {u(R), u'(R), udot(R),
+ * udot'(R), ||udot||^2}.  The quantities hsdla_system's type_u .. type_dE_u_norm hold; the
+ * reference computes them in AtomData::generate_matchdata (flapw_opt/src/AtomData.cpp:72-88)
+ * through radial_solve (flapw_opt/src/special_funcs.cpp:21-36) and Fleur's radfun
+ * (external/compat/fleur/radfun.f, radsra.f, radsrd.F, intgr.F).  Host only, once per run;
+ * n >= 7, 0 <= l <= 14. */
+int hsdla_radial_match(int32_t l, double e, const double *vr, int32_t n, double rmt, double dx, double *out);
+
 /* Hand-off to an eigensolver in Fleur's packed form: the lower triangle of the column-major
  * n x n DEVICE matrix M (leading dimension ld >= n, e.g. H or S from hsdla_plan_execute) written
  * row by row into the DEVICE array packed of n (n + 1) / 2 elements, element (r, c), c <= r, at
