@@ -2468,6 +2468,9 @@ int ozaki_group_tune_tiles(OzGroup *g, cudaStream_t st, float *ms_best) {
         float ms = 0.f;
         if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
         if (e == cudaSuccess && (best < 0.f || ms < best)) { best = ms; bi = c; }
+        if (e == cudaSuccess && env_int("HSDLA_TRACE", 0))
+            fprintf(stderr, "tile tuner: halves %d, %s units: %.3f ms\n", cfg[c][0], cfg[c][1] ? "merged" : "single-diagonal",
+                    ms);
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
