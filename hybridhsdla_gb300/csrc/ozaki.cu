@@ -2452,6 +2452,9 @@ int ozaki_group_tune_tiles(OzGroup *g, cudaStream_t st, float *ms_best) {
     }
     const int h0 = g->halves;
     const bool m0 = g->merged;
+    // a prefix of the tile list is enough to rank the configurations (a batched group's launch
+    // covers every k-point): at most 16 waves of pair tiles
+    const int64_t tiles = std::min<int64_t>(g->tiles_sh, 16 * 76);
     float best = -1.f;
     int bi = 0;
     cudaError_t e = cudaSuccess;
@@ -2460,8 +2463,8 @@ int ozaki_group_tune_tiles(OzGroup *g, cudaStream_t st, float *ms_best) {
         for (int rep = 0; rep < 2 && e == cudaSuccess; ++rep) {
             if (rep == 1) e = cudaEventRecord(e0, st);
             if (e == cudaSuccess)
-                e = launch_pair(g->maps_sh, g->s, g->d_err, g->d_jobs_sh, g->n_jobs_sh, g->tiles_sh, g->d_list_sh,
-                                nullptr, st, g->units, g->halves);
+                e = launch_pair(g->maps_sh, g->s, g->d_err, g->d_jobs_sh, g->n_jobs_sh, tiles, g->d_list_sh, nullptr,
+                                st, g->units, g->halves);
             if (e == cudaSuccess && rep == 1) e = cudaEventRecord(e1, st);
         }
         if (e == cudaSuccess) e = cudaEventSynchronize(e1);
