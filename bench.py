@@ -325,8 +325,14 @@ def run_ours(args):
     e2e_flop = sys_.flop_per_kpoint(G)
     h2d = sum(a.nbytes for a in (kp.g, tmats[0], tmats[1], tmats[2], sys_.u, sys_.u_dr, sys_.dE_u,
                                   sys_.dE_u_dr, sys_.dE_u_norm, sys_.atom_pos, sys_.atom_type, sys_.type_rmt))
+    # the end-to-end outputs against the device path's (lower triangles; the same launches, so the
+    # same bits), outside the timed region
+    il = np.tril_indices(G)
+    e2e_same = bool(np.array_equal(Hh.numpy().T[il], H_oz.cpu().numpy().T[il]) and
+                    np.array_equal(Sh.numpy().T[il], S_oz.cpu().numpy().T[il]))
+    del il
     if rep_e["outputs_in_place"]:
-        # the last combine wrote the lower triangles of H and S into the page-locked buffers
+        # the combine wrote the lower triangles of H and S into the page-locked buffers
         d2h = 2 * 16 * G * (G + 1) // 2
     else:
         # the download copies each 512-column block of H and S from its first row down
@@ -439,8 +445,11 @@ def run_ours(args):
                         "calls_ms": [round(x, 2) for x in e2e_calls],
                         "calls_device_ms": [round(x, 2) for x in e2e_dev],
                         "median_ms": float(np.median(e2e_calls)),
-                        "outputs": "written in place by the last combine" if rep_e["outputs_in_place"]
+                        "outputs": ("written in place by the combine in %d column blocks while the products "
+                                    "of the next block ran" % rep_e["output_blocks"]) if rep_e["output_blocks"]
+                        else "written in place by the last combine" if rep_e["outputs_in_place"]
                         else "downloaded by the copy engine",
+                        "equal_to_device_path": e2e_same,
                         "note": "hsdla_create_hs on the rank's first k-point, pinned host buffers; "
                                 "value = mean over calls_ms"},
                 "gpu_launches": launches,

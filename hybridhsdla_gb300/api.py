@@ -73,7 +73,8 @@ class ReportStruct(ctypes.Structure):
                 ("kernel_launches", ctypes.c_int32), ("num_panels", ctypes.c_int32),
                 ("outputs_in_place", ctypes.c_int32), ("num_row_sets", ctypes.c_int32),
                 ("rotation_classes", ctypes.c_int32), ("tile_halves", ctypes.c_int32),
-                ("merged_units", ctypes.c_int32), ("tile_tuned", ctypes.c_int32), ("reserved", ctypes.c_int32 * 2)]
+                ("merged_units", ctypes.c_int32), ("tile_tuned", ctypes.c_int32), ("output_blocks", ctypes.c_int32),
+                ("reserved", ctypes.c_int32 * 1)]
 
     def as_dict(self) -> dict:
         return {f: getattr(self, f) for f, _ in self._fields_ if f != "reserved"}

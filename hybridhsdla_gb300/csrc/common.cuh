@@ -127,11 +127,15 @@ struct SfEntry {
     int64_t ldp = 0, ldo = 0, n = 0, pstride = 0, ldi = 0;
     const int32_t *g = nullptr;
     int64_t tile_begin = 0;
+    // where rows < SfTab::xrow1 go instead of S and H (NULL: nowhere else), leading dimension ldx
+    double2 *Sx = nullptr, *Hx = nullptr;
+    int64_t ldx = 0;
 };
 struct SfTab {
     int nk = 0, type = 0, ntypes = 1;             // the batch: types [type, type + ntypes) in slots
     int slot0 = 0;                                // slot0, slot0 + 1, ...
     int64_t col0 = 0, col1 = INT64_MAX;           // the columns combined (of every entry)
+    int64_t xrow1 = 0;                            // rows below it go to the entries' Sx, Hx when set
 
     int dx = 0, dy = 0, dz = 0, ny = 0, nz = 0;   // box offsets (half widths) and extents
     int64_t box = 0;                              // entries per type
@@ -143,7 +147,7 @@ cudaError_t launch_sf_table(const double2 *ex, const double2 *ey, const double2 
                             const int32_t *type_begin, int nt, int nx, int ny, int nz, double2 *sf, cudaStream_t st);
 // S (+)= sum_b SF_{type+b} (.) PS_b and H (+)= sum_b SF_{type+b} (.) PH_b over the lower triangles
 // of every entry, b over the batch's type slots, in columns [tab.col0, tab.col1) (multiples of 32
-// but for the end).
+// but for the end); rows below tab.xrow1 into Sx, Hx instead for entries that give them.
 cudaError_t launch_sf_combine(const SfTab &tab, const double2 *sf, bool first, cudaStream_t st);
 
 // BLAS-shaped plugin (blas_plugin.cu).  Operand in the 'C' layout: dst rows [r0, r0 + k) of every

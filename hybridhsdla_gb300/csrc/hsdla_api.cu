@@ -139,6 +139,7 @@ struct hsdla_plan {
         bool direct = false;   // every output is page-locked host memory the GPU can write
         bool done = false;
         bool in_place = false;   // the combine wrote the host outputs
+        int blocks = 0;          // ... in column blocks while the products of the next ran (0: after them)
     };
     Download *dl = nullptr;
     double est_err = 0.0;            // autotuner's predicted relative error
@@ -1268,6 +1269,22 @@ void run_groups_flop(const hsdla_plan *pl, double *dom_flop) {
     for (const auto &g : pl->groups) run_groups_flop_one(pl, g, dom_flop);
 }
 
+// The combine table of a group with the caller's page-locked host H and S as its outputs (the
+// device outputs become the sums of earlier batches, read when the batch is not the first).
+SfTab host_output_tab(const hsdla_plan *pl, const hsdla_plan::Group &g) {
+    SfTab tab = g.sft;
+    for (int q = 0; q < g.ktab.nk; ++q) {
+        const int i = g.kidx[q];
+        tab.e[q].Si = tab.e[q].S;
+        tab.e[q].Hi = tab.e[q].H;
+        tab.e[q].ldi = tab.e[q].ldo;
+        tab.e[q].H = reinterpret_cast<double2 *>(pl->dl->H[i]);
+        tab.e[q].S = reinterpret_cast<double2 *>(pl->dl->S[i]);
+        tab.e[q].ldo = pl->dl->ld[i];
+    }
+    return tab;
+}
+
 // The last combine batch of a group [t0, t0 + ntypes).  With a host download pending (and no graph
 // capture) it runs in column blocks of kDownBlock, and after each block the copy stream downloads
 // that block of every k-point's H and S lower triangle while the next block is combined.
@@ -1285,16 +1302,11 @@ int combine_last(hsdla_plan *pl, hsdla_plan::Group &g, int t0, int ntypes, cudaS
     if (pl->dl->direct) {
         // the combine writes the host outputs itself (page-locked memory, addressed over the
         // CPU-GPU link), adding to the device sums of the earlier batches: no download
-        for (int q = 0; q < g.ktab.nk; ++q) {
-            const int i = g.kidx[q];
-            tab.e[q].Si = tab.e[q].S;
-            tab.e[q].Hi = tab.e[q].H;
-            tab.e[q].ldi = tab.e[q].ldo;
-            tab.e[q].H = reinterpret_cast<double2 *>(pl->dl->H[i]);
-            tab.e[q].S = reinterpret_cast<double2 *>(pl->dl->S[i]);
-            tab.e[q].ldo = pl->dl->ld[i];
-        }
-        CUDA_TRY(ctx, launch_sf_combine(tab, pl->sf_tab, t0 == 0, st));
+        SfTab ht = host_output_tab(pl, g);
+        ht.type = tab.type;
+        ht.ntypes = tab.ntypes;
+        ht.slot0 = tab.slot0;
+        CUDA_TRY(ctx, launch_sf_combine(ht, pl->sf_tab, t0 == 0, st));
         pl->launches++;
         pl->dl->done = pl->dl->in_place = true;
         return HSDLA_OK;
@@ -1354,11 +1366,20 @@ int run_groups(hsdla_plan *pl, cudaStream_t st, bool timed, float *ms_ab, float 
         }
         if (g.oz) {
             int nl = 0;
+            // page-locked host outputs: written in column blocks while the products run, where the
+            // group allows it (every type in one combine batch)
+            const bool streamed = defer && pl->dl->direct && ozaki_group_streamable(g.oz);
+            SfTab host_tab{};
+            if (streamed) host_tab = host_output_tab(pl, g);
             const int rc = ozaki_group_run(g.oz, pl->dsys, g.ktab, st, g.ev_dom.data(), (int)g.ev_dom.size(), &nl,
-                                           defer, timed ? g.ev_t.data() : nullptr, timed ? (int)g.ev_t.size() : 0);
+                                           defer, timed ? g.ev_t.data() : nullptr, timed ? (int)g.ev_t.size() : 0,
+                                           streamed ? &host_tab : nullptr);
             if (rc) return set_err(ctx, rc, "Ozaki group failed: %s", ozaki_last_error());
             pl->launches += nl;
-            if (defer) {
+            if (streamed) {
+                pl->dl->done = pl->dl->in_place = true;
+                pl->dl->blocks = ozaki_group_output_blocks(g.oz);
+            } else if (defer) {
                 const int t0 = ozaki_group_last_combine(g.oz);
                 const int rcc = combine_last(pl, g, t0, pl->nt - t0, st, capturing);
                 if (rcc) return rcc;
@@ -1878,6 +1899,7 @@ int hsdla_create_hs(hsdla_context *ctx, const hsdla_system *s, const hsdla_kpoin
         rep->ms_per_kpoint = nk ? ms_dev / nk : 0.0;
         rep->eff_tflops = ms_dev > 0 ? pl->flop / (ms_dev * 1e-3) / 1e12 : 0.0;
         rep->outputs_in_place = dl.in_place ? 1 : 0;
+        rep->output_blocks = dl.blocks;
     }
     const clk::time_point t_destroy = clk::now();
     hsdla_plan_destroy(pl);

@@ -1481,6 +1481,12 @@ void build_schedule(const std::vector<OzJob> &jobs, std::vector<int4> &list, int
 }
 
 constexpr int kProgressCap = 1024;   // progress slots (>= SM count, multiple of 4)
+// Streamed host output: the S/H launches of all types are cut into at most kMaxOutBlocks launches
+// of whole waves of pair tiles; the tiles are ordered by kOutColumnBlocks column blocks (of about
+// equal tile counts), so that the columns a launch completes are combined and sent to the host
+// while the next launch runs.  Only the part completed by the last launch stays exposed.
+constexpr int kMaxOutBlocks = 8;
+constexpr int kOutColumnBlocks = 8;
 
 int launch_gemm(std::vector<OzJob> &jobs, const CUtensorMap *maps, int s, int *d_err, OzJob *d_jobs,
                 cudaStream_t st, cudaEvent_t ev0 = nullptr, cudaEvent_t ev1 = nullptr, int4 *d_list = nullptr,
@@ -1722,6 +1728,18 @@ struct OzGroup {
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     SfTab sft{};                // its combine table (outputs patched per run)
     const double2 *sf_tab = nullptr;
+    // Streamed host output (structure-factor form on pair tiles, every type in one combine batch):
+    // the S/H products of all types in column blocks, one launch per block, each block combined
+    // into the caller's page-locked outputs on blk_side while the next block's products run.
+    // Block b covers tile-list entries [blk_begin[b], blk_begin[b+1]) of d_list_blk and output
+    // columns [blk_col[b], blk_col[b+1]).
+    int nblk = 0;
+    int64_t blk_begin[kMaxOutBlocks + 1] = {};
+    int64_t blk_col[kMaxOutBlocks + 1] = {};
+    int4 *d_list_blk = nullptr;
+    cudaStream_t blk_side = nullptr;
+    cudaEvent_t ev_blk[kMaxOutBlocks] = {};
+    cudaEvent_t ev_blk_join = nullptr;
 };
 
 namespace {
@@ -1878,16 +1896,71 @@ int64_t ozaki_group_persist_bytes(int s, int64_t twoL, int64_t na, int64_t nt, c
                                   int panels) {
     const int64_t bpad = round_up(atom_stride(twoL), kKBlock);    // T operand: one atom's rows per plane row
     const int64_t nk = (int64_t)G.size();
-    int64_t tiles_t = 0, tiles_sh = 0;
+    int64_t tiles_t = 0, tiles_sh = 0, tiles_blk = 0;
     for (int64_t g : G) {
-        const int64_t T = (g + kTileN - 1) / kTileN;
+        const int64_t T = (g + kTileN - 1) / kTileN, Tp = (g + kPairTile - 1) / kPairTile;
         tiles_t += std::max(na, nt) * ((twoL + kTileM - 1) / kTileM) * T;
         tiles_sh += T * (T + 1);
+        tiles_blk += Tp * (Tp + 1);
     }
     return operand_bytes(s, nt * twoL, bpad, use_pair() ? 4 * s : 2 * s) +
            round_up(sizeof(OzJob) * nk * (std::max(na, nt) + 2), 1024) +
            round_up(sizeof(OzJob) * 2 * nk * panels, 1024) + round_up(sizeof(int4) * (tiles_t + panels), 1024) +
-           round_up(sizeof(int4) * (tiles_sh + 1), 1024) + round_up(sizeof(int) * kProgressCap, 1024) + 8192;
+           round_up(sizeof(int4) * (tiles_sh + 1), 1024) + round_up(sizeof(int) * kProgressCap, 1024) +
+           round_up(sizeof(int4) * (nt * tiles_blk + 1), 1024) + 8192;
+}
+
+// The streamed host output's launches (pair tiles).  The tile columns are split into
+// kOutColumnBlocks ranges of about equal lower-triangle tile counts; the tile list runs through
+// them in order, and within a range type by type, each type in the per-type schedule's order (so
+// that the pairs working at a time share few types' operands in L2).  The list is then cut into
+// launches of whole waves (one tile per cluster pair of the GPU); launch b leaves columns
+// [blk_col[b], blk_col[b+1]) complete (possibly none).  jobs0: the first type's S/H jobs.
+static int build_output_blocks(OzGroup *g, const std::vector<OzJob> &jobs0, int64_t tile) {
+    std::vector<int4> l0;
+    build_schedule(jobs0, l0, tile);
+    int64_t T = 0;
+    for (const auto &j : jobs0) T = std::max<int64_t>(T, (j.n + tile - 1) / tile);
+    g->nblk = 0;
+    if (T < 2) return HSDLA_OK;
+    const int C = (int)std::min<int64_t>(kOutColumnBlocks, T);
+    const int64_t total = T * (T + 1) / 2;
+    std::vector<int64_t> cb(C + 1, T);
+    cb[0] = 0;
+    int64_t acc = 0, c = 0;
+    for (int b = 1; b < C; ++b) {
+        while (c < T && acc < total * b / C) { acc += T - c; ++c; }
+        cb[b] = c;
+    }
+    std::vector<int4> lb;
+    lb.reserve(l0.size() * g->nt);
+    for (int b = 0; b < C; ++b)
+        for (int t = 0; t < g->nt; ++t)
+            for (const int4 &e : l0)
+                if (e.z >= cb[b] && e.z < cb[b + 1]) lb.push_back(make_int4(t * g->n_jobs_sh + e.x, e.y, e.z, 0));
+    const int64_t N = (int64_t)lb.size();
+    if (N != (int64_t)l0.size() * g->nt) { g_oz_err = "output block schedule size mismatch"; return HSDLA_ERR_ARG; }
+    // first incomplete tile column after list position i: suffix minimum of the tile columns
+    std::vector<int64_t> open(N + 1, T);
+    for (int64_t i = N - 1; i >= 0; --i) open[i] = std::min<int64_t>(open[i + 1], lb[i].z);
+    int dev = 0, nsm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    const int64_t wave = std::max(1, nsm / 2);
+    const int64_t waves = (N + wave - 1) / wave;
+    const int64_t per = std::max<int64_t>(1, (waves + kMaxOutBlocks - 1) / kMaxOutBlocks) * wave;
+    g->blk_begin[0] = 0;
+    g->blk_col[0] = 0;
+    for (int64_t i0 = 0; i0 < N && g->nblk < kMaxOutBlocks; ++g->nblk) {
+        const int64_t i1 = g->nblk + 1 == kMaxOutBlocks ? N : std::min(N, i0 + per);
+        g->blk_begin[g->nblk + 1] = i1;
+        g->blk_col[g->nblk + 1] = std::max(g->blk_col[g->nblk], open[i1] * tile);
+        i0 = i1;
+    }
+    g->blk_col[g->nblk] = T * tile;
+    const cudaError_t e = cudaMemcpy(g->d_list_blk, lb.data(), sizeof(int4) * N, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) { g_oz_err = cudaGetErrorString(e); return HSDLA_ERR_CUDA; }
+    return HSDLA_OK;
 }
 
 // Structure-factor form of a group: digit planes of M, M diag(w_t) and Z (2L rows per type, each
@@ -1958,6 +2031,12 @@ static int group_prepare_sf(OzakiPlan &oz, const OzGroupDesc &d, const std::vect
     g->d_list_t = keep.take<int4>(tiles_t + 1);
     g->d_list_sh = keep.take<int4>(tiles_sh + 1);
     g->d_progress = keep.take<int>(kProgressCap);
+    int64_t tiles_blk = 0;
+    for (int64_t x : G) {
+        const int64_t Tp = (x + kPairTile - 1) / kPairTile;
+        tiles_blk += Tp * (Tp + 1);
+    }
+    g->d_list_blk = keep.take<int4>(d.nt * tiles_blk + 1);
     auto fail = [&](int code) { ozaki_group_destroy(g); return code; };
     auto table = [&](const DigitOperand &o, int which) {
         SliceTab t;
@@ -2056,6 +2135,10 @@ static int group_prepare_sf(OzakiPlan &oz, const OzGroupDesc &d, const std::vect
     }
     e = cudaMemcpy(g->d_jobs_sh, all.data(), sizeof(OzJob) * all.size(), cudaMemcpyHostToDevice);
     if (e != cudaSuccess) { g_oz_err = cudaGetErrorString(e); return fail(HSDLA_ERR_CUDA); }
+    if (g->pair) {
+        rc = build_output_blocks(g, std::vector<OzJob>(all.begin(), all.begin() + g->n_jobs_sh), tile);
+        if (rc) return fail(rc);
+    }
     g->maps_sh[0] = g->dM.map;
     g->maps_sh[1] = g->halves == 2 ? g->dW.map64 : g->dW.map;   // right operands
     g->maps_sh[2] = g->halves == 2 ? g->dX.map64 : g->dX.map;
@@ -2292,8 +2375,91 @@ static cudaError_t record(cudaEvent_t ev, cudaStream_t st) {
 // them.
 int ozaki_group_tapply_events(const OzGroup *g) { return (g->sf || g->hoist) ? 1 : g->panels; }
 
+bool ozaki_group_streamable(const OzGroup *g) {
+    return g && g->sf && g->pair && g->nblk > 1 && g->tbatch >= g->nt && g->side_types == 0 &&
+           env_int("HSDLA_STREAM_OUTPUT", 1) != 0;
+}
+
+int ozaki_group_output_blocks(const OzGroup *g) { return g ? g->nblk : 0; }
+
+// The streamed host output's S/H part.  Per column block: one pair launch over every type's tiles
+// of the block, then the block's combine on the main stream, which writes the block's diagonal
+// square (rows < the block's end) into the caller's page-locked outputs in place and the rows
+// below it into the device outputs; the copy engine then downloads those rows (side stream)
+// while the next block's products run.  The last block's combine writes everything in place.
+// The main stream waits for the last download at the end.  No SM work runs beside the products.
+static cudaError_t run_sh_streamed(OzGroup *g, cudaStream_t st, const cudaEvent_t *ev, int nev, const SfTab &out,
+                                   int *nl) {
+    cudaError_t e = cudaSuccess;
+    if (!g->blk_side) {
+        e = cudaStreamCreateWithFlags(&g->blk_side, cudaStreamNonBlocking);
+        for (int b = 0; b < g->nblk && e == cudaSuccess; ++b)
+            e = cudaEventCreateWithFlags(&g->ev_blk[b], cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&g->ev_blk_join, cudaEventDisableTiming);
+        if (e != cudaSuccess) return e;
+    }
+    // the dominant-launch event pairs: pair b spans block b's S/H launch where there are enough of
+    // them (the rest, and a shortfall, span nothing)
+    const int npair = nev / 2;
+    for (int b = 0; b < g->nblk && e == cudaSuccess; ++b) {
+        const int64_t c0 = g->blk_col[b], c1 = g->blk_col[b + 1];
+        const bool last = b + 1 == g->nblk;
+        if (b < npair) e = record(ev[2 * b], st);
+        if (e == cudaSuccess)
+            e = launch_pair(g->maps_sh, g->s, g->d_err, g->d_jobs_sh, g->n_jobs_sh * g->nt,
+                            g->blk_begin[b + 1] - g->blk_begin[b], g->d_list_blk + g->blk_begin[b], nullptr, st,
+                            g->units, g->halves);
+        if (e == cudaSuccess && b < npair) e = record(ev[2 * b + 1], st);
+        SfTab tab = out;
+        tab.type = 0;
+        tab.ntypes = g->nt;
+        tab.slot0 = 0;
+        tab.col0 = c0;
+        tab.col1 = c1;
+        if (!last) {
+            // rows below the block's diagonal square into the device outputs (the sums Si, Hi of an
+            // earlier batch are the device outputs themselves; this is the only batch)
+            tab.xrow1 = c1;
+            for (int q = 0; q < tab.nk; ++q) {
+                SfEntry &E = tab.e[q];
+                E.Sx = E.S;
+                E.Hx = E.H;
+                E.ldx = E.ldo;
+                E.S = const_cast<double2 *>(E.Si);
+                E.H = const_cast<double2 *>(E.Hi);
+                E.ldo = E.ldi;
+            }
+        }
+        if (c1 <= c0) { *nl += 1; continue; }       // no column completed by this launch
+        if (e == cudaSuccess) e = launch_sf_combine(tab, g->sf_tab, true, st);
+        *nl += 2;
+        if (last || e != cudaSuccess) continue;
+        e = cudaEventRecord(g->ev_blk[b], st);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(g->blk_side, g->ev_blk[b], 0);
+        for (int q = 0; q < tab.nk && e == cudaSuccess; ++q) {
+            const SfEntry &E = tab.e[q];
+            if (c1 >= E.n) continue;
+            const int64_t w = std::min(c1, E.n) - c0;
+            for (int m = 0; m < 2 && e == cudaSuccess; ++m) {
+                double2 *host = (m == 0 ? E.Sx : E.Hx) + c1 + E.ldx * c0;
+                const double2 *dev = (m == 0 ? E.S : E.H) + c1 + E.ldo * c0;
+                e = cudaMemcpy2DAsync(host, E.ldx * sizeof(double2), dev, E.ldo * sizeof(double2),
+                                      (E.n - c1) * sizeof(double2), w, cudaMemcpyDeviceToHost, g->blk_side);
+            }
+        }
+    }
+    for (int p = g->nblk; p < npair && e == cudaSuccess; ++p) {
+        e = record(ev[2 * p], st);
+        if (e == cudaSuccess) e = record(ev[2 * p + 1], st);
+    }
+    if (e == cudaSuccess) e = cudaEventRecord(g->ev_blk_join, g->blk_side);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(st, g->ev_blk_join, 0);
+    return e;
+}
+
 int ozaki_group_run(OzGroup *g, const DevSystem &sys, const KTable &ktab, cudaStream_t st, const cudaEvent_t *ev,
-                    int nev, int *launches, bool defer_last_combine, const cudaEvent_t *ev_t, int nev_t) {
+                    int nev, int *launches, bool defer_last_combine, const cudaEvent_t *ev_t, int nev_t,
+                    const SfTab *host_out) {
     const cudaEvent_t ev0 = nev >= 2 ? ev[0] : nullptr, ev1 = nev >= 2 ? ev[nev - 1] : nullptr;
     // T-application events: pair q around the q-th T launch (when the caller gave enough of them)
     const bool tev = ev_t && nev_t >= 2 * ozaki_group_tapply_events(g);
@@ -2310,6 +2476,12 @@ int ozaki_group_run(OzGroup *g, const DevSystem &sys, const KTable &ktab, cudaSt
         if (e == cudaSuccess && tev) e = cudaEventRecord(ev_t[1], st);
         if (e == cudaSuccess) e = slice_launch(g->pan[0].tX, st);    // Z
         nl += 3;
+        if (host_out && ozaki_group_streamable(g)) {
+            if (e == cudaSuccess) e = run_sh_streamed(g, st, ev, nev, *host_out, &nl);
+            if (launches) *launches = nl;
+            if (e != cudaSuccess) { g_oz_err = cudaGetErrorString(e); return HSDLA_ERR_CUDA; }
+            return HSDLA_OK;
+        }
         for (int t = 0; t < g->nt && e == cudaSuccess; ++t) {
             const OzJob *jobs = g->d_jobs_sh + (int64_t)g->n_jobs_sh * t;
             if (nev >= 2 * g->nt) e = record(ev[2 * t], st);
@@ -2493,6 +2665,10 @@ void ozaki_group_destroy(OzGroup *g) {
     if (g->ev_fork) cudaEventDestroy(g->ev_fork);
     if (g->ev_join) cudaEventDestroy(g->ev_join);
     if (g->side) cudaStreamDestroy(g->side);
+    for (auto &ev : g->ev_blk)
+        if (ev) cudaEventDestroy(ev);
+    if (g->ev_blk_join) cudaEventDestroy(g->ev_blk_join);
+    if (g->blk_side) cudaStreamDestroy(g->blk_side);
     delete g;
 }
 

@@ -81,10 +81,19 @@ int ozaki_group_last_combine(const OzGroup *g);
 // structure-factor form; nev events, may be 0).  defer_last_combine: the structure-factor form's
 // last combine batch is left to the caller.  ev_t: event pairs recorded around the T-application
 // launches (one pair, or one per atom panel when each panel applies T itself; nev_t events, may
-// be 0; plain records, so not for a run under graph capture).
+// be 0; plain records, so not for a run under graph capture).  host_out (streamable groups only,
+// see ozaki_group_streamable; not under graph capture): the combine table whose outputs are the
+// caller's page-locked host H and S; the S/H products then run in column blocks and each block is
+// combined into those outputs while the next block's products run (the whole combine is done
+// when the call's work on st completes; defer_last_combine does not apply).
 int ozaki_group_run(OzGroup *g, const DevSystem &sys, const KTable &ktab, cudaStream_t st, const cudaEvent_t *ev,
                     int nev, int *launches, bool defer_last_combine = false, const cudaEvent_t *ev_t = nullptr,
-                    int nev_t = 0);
+                    int nev_t = 0, const SfTab *host_out = nullptr);
+// A structure-factor group whose host outputs can be written in column blocks while its products
+// run (pair tiles, every type in one combine batch, at least two blocks; HSDLA_STREAM_OUTPUT=0
+// turns it off), and its block count.
+bool ozaki_group_streamable(const OzGroup *g);
+int ozaki_group_output_blocks(const OzGroup *g);
 // Event pairs ozaki_group_run records around the group's T application (see ev_t).
 int ozaki_group_tapply_events(const OzGroup *g);
 void ozaki_group_destroy(OzGroup *g);

@@ -107,7 +107,9 @@ __global__ void __launch_bounds__(kSfTile * kSfRows) sf_combine_kernel(const __g
             vh.x = fma(f.x, ph.x, fma(-f.y, ph.y, vh.x));
             vh.y = fma(f.x, ph.y, fma(f.y, ph.x, vh.y));
         }
-        double2 *so = E.S + row + E.ldo * col, *ho = E.H + row + E.ldo * col;
+        const bool x = E.Sx && row < tab.xrow1;
+        double2 *so = x ? E.Sx + row + E.ldx * col : E.S + row + E.ldo * col;
+        double2 *ho = x ? E.Hx + row + E.ldx * col : E.H + row + E.ldo * col;
         if (!first) {
             const double2 s0 = E.Si[row + E.ldi * col], h0 = E.Hi[row + E.ldi * col];
             vs.x += s0.x; vs.y += s0.y;

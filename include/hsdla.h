@@ -35,9 +35,13 @@
  *     the strict upper triangle of the diagonal 512 x 512 blocks to zero and leaves the rest
  *     of it untouched (the reference leaves it unset as well).  Where every H and S given to
  *     hsdla_create_hs is page-locked host memory that the GPU addresses at the same pointer
- *     (cudaHostAlloc, cudaMallocHost) and the plan takes the structure-factor form, the last
+ *     (cudaHostAlloc, cudaMallocHost) and the plan takes the structure-factor form, the
  *     combine writes the lower triangles in place and the whole strict upper triangle stays
- *     untouched (HSDLA_DIRECT_OUTPUT=0 keeps the download).
+ *     untouched (HSDLA_DIRECT_OUTPUT=0 keeps the download).  With Ozaki precision and every
+ *     type in one combine batch this happens in column blocks while the digit products of the
+ *     next block run: each block's diagonal square is written in place, the rows below it are
+ *     combined on the device and copied by the copy engine (HSDLA_STREAM_OUTPUT=0: all after
+ *     the products).
  */
 #ifndef HSDLA_H
 #define HSDLA_H
@@ -131,7 +135,9 @@ typedef struct hsdla_report {
                                  /* two 256 x 128 halves in alternating TMEM buffers (2); 0 otherwise */
     int32_t merged_units;        /* the same launches: 1 = adjacent digit diagonals share exact accumulation units */
     int32_t tile_tuned;          /* 1 = those two were chosen by timing on this plan's data (or a cached result) */
-    int32_t reserved[2];
+    int32_t output_blocks;       /* hsdla_create_hs, outputs written in place: the column blocks they were written
+                                    in while the digit products of the next block ran (0 = after all products) */
+    int32_t reserved[1];
 } hsdla_report;
 
 typedef struct hsdla_context hsdla_context;

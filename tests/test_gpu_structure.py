@@ -96,9 +96,11 @@ def test_structure_factor_variants(ctx, knob, monkeypatch):
 @pytest.mark.parametrize("precision", ["fp64", "ozaki"])
 @pytest.mark.parametrize("batch", ["2", "8"])
 def test_outputs_written_in_place(ctx, precision, batch, monkeypatch):
-    """Page-locked host outputs: the last combine writes H and S itself (after earlier batches on
-    the device with a batch of 2 types) and the lower triangles equal, bit for bit, those of the
-    download into pageable buffers; the strict upper triangle is not touched at all."""
+    """Page-locked host outputs: the combine writes H and S itself and the lower triangles equal,
+    bit for bit, those of the download into pageable buffers; the strict upper triangle is not
+    touched at all.  With a batch of 2 types the last batch's combine does it after the earlier
+    batches on the device; with every type in one batch (Ozaki) the products run in column blocks
+    and each block's combine writes its columns while the next block's products run."""
     torch = pytest.importorskip("torch")
     monkeypatch.setenv("HSDLA_TYPE_BATCH", batch)
     s = synth.make_system("c1")
@@ -115,6 +117,7 @@ def test_outputs_written_in_place(ctx, precision, batch, monkeypatch):
     monkeypatch.setenv("HSDLA_SF", "1")
     res, rep = ctx.create_hs(s, precision=precision, num_slices=11 if precision == "ozaki" else 0, out=outs)
     assert rep["outputs_in_place"] == 1
+    assert (rep["output_blocks"] > 1) == (precision == "ozaki" and batch == "8"), rep["output_blocks"]
     for (H, S), (Hr, Sr), kp in zip(res, res_ref, s.kpoints):
         il = np.tril_indices(kp.n_g)
         iu = np.triu_indices(kp.n_g, 1)
