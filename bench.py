@@ -325,12 +325,18 @@ def run_ours(args):
     e2e_flop = sys_.flop_per_kpoint(G)
     h2d = sum(a.nbytes for a in (kp.g, tmats[0], tmats[1], tmats[2], sys_.u, sys_.u_dr, sys_.dE_u,
                                   sys_.dE_u_dr, sys_.dE_u_norm, sys_.atom_pos, sys_.atom_type, sys_.type_rmt))
-    # the end-to-end outputs against the device path's (lower triangles; the same launches, so the
-    # same bits), outside the timed region
-    il = np.tril_indices(G)
-    e2e_same = bool(np.array_equal(Hh.numpy().T[il], H_oz.cpu().numpy().T[il]) and
-                    np.array_equal(Sh.numpy().T[il], S_oz.cpu().numpy().T[il]))
-    del il
+    # the end-to-end outputs against the device path's, lower triangles, outside the timed region
+    # (its own one-k-point plan: the slice autotuner may choose another digit count, else the same
+    # launches give the same bits)
+    e2e_vs = {"num_slices": rep_e["num_slices"], "device_path_num_slices": rep["num_slices"]}
+    rel, same = 0.0, True
+    for Xh, Xd in ((Hh, H_oz), (Sh, S_oz)):
+        d = torch.tril(Xh.to(Xd.device).T - Xd.T)      # device buffers are column-major: tensor[col, row]
+        rel = max(rel, float(torch.linalg.norm(d) / torch.linalg.norm(torch.tril(Xd.T))))
+        same = same and bool(torch.count_nonzero(d) == 0)
+        del d
+    e2e_vs["rel_fro"] = rel
+    e2e_vs["identical"] = same
     if rep_e["outputs_in_place"]:
         # the combine wrote the lower triangles of H and S into the page-locked buffers
         d2h = 2 * 16 * G * (G + 1) // 2
@@ -449,7 +455,7 @@ def run_ours(args):
                                     "of the next block ran" % rep_e["output_blocks"]) if rep_e["output_blocks"]
                         else "written in place by the last combine" if rep_e["outputs_in_place"]
                         else "downloaded by the copy engine",
-                        "equal_to_device_path": e2e_same,
+                        "vs_device_path": e2e_vs,
                         "note": "hsdla_create_hs on the rank's first k-point, pinned host buffers; "
                                 "value = mean over calls_ms"},
                 "gpu_launches": launches,
