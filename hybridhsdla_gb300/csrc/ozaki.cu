@@ -71,6 +71,8 @@ struct OzJob {
     int32_t lmap, rmap;        // tensor-map index (0..3) of the left / right digit operand
     int32_t lower;             // 1: only tiles and elements with row >= col
     int32_t accum;             // 1: the first unit of a tile adds to the output instead of storing
+    int32_t ksteps_last;       // pair tiles: K steps of 32 bytes the last k-block holds (1-4; 0: 4)
+    int32_t reserved0;
     int64_t lplane, rplane;    // rows per digit plane in each map
     int64_t lrow0, rrow0;      // first operand row (output row / col 0) inside a plane
     int64_t lk0, rk0;          // first contraction byte (multiple of 128)
@@ -822,6 +824,7 @@ __global__ void __launch_bounds__(kPairThreads, 1)
                 // the job's fields in registers: the asm statements below clobber memory, and the
                 // issuer must not reload them between MMAs
                 const int64_t jnkb = j.nkb;
+                const int jksl = j.ksteps_last > 0 ? j.ksteps_last : kKBlock / 32;
                 for (int u = 0; ok && u < units.n; ++u) {
                     const int t = units.t[u], merged = (units.flags[u] & kUnitMerged) ? 1 : 0;
                     const int64_t ck = merged ? jnkb : chunk_kblocks(min(s, t - 1) - max(1, t - s) + 1);
@@ -856,10 +859,19 @@ __global__ void __launch_bounds__(kPairThreads, 1)
                                             mma_f8_pair(d_im, dai + o, dbr + o, id_neg, 1u);
                                             first = false;
                                         };
-                                        // whole blocks as straight-line code: a bound on the steps (to skip
-                                        // the zero padding past 2L) slowed the launches by 2-10%
+                                        // whole blocks as straight-line code (a bound in this loop slowed the
+                                        // launches by 2-10%).  With 256 x 256 accumulators the job's last
+                                        // k-block stops early, where the K steps past the contraction length
+                                        // hold zero digits (lmax 8: 2L = 162 of 256; c1 -10%); the half-width
+                                        // tiles keep whole blocks, as the check alone cost them 3-6% (c2, c3)
+                                        if (kHalves == 2 || kb + 1 < jnkb || jksl == kKBlock / 32) {
 #pragma unroll
-                                        for (int kk = 0; kk < kKBlock / 32; ++kk) step(kk);
+                                            for (int kk = 0; kk < kKBlock / 32; ++kk) step(kk);
+                                        } else {
+                                            step(0);
+                                            if (jksl > 1) step(1);
+                                            if (jksl > 2) step(2);
+                                        }
                                         mma_commit_pair(&bars.empty[stage]);
                                         if (++stage == kStages) { stage = 0; phase ^= 1; }
                                     }
@@ -1980,6 +1992,8 @@ static int group_prepare_sf(OzakiPlan &oz, const OzGroupDesc &d, const std::vect
     g->pair = use_pair();
     g->bpad = round_up(d.twoL, kKBlock);
     const int64_t tkb = g->bpad / kKBlock, KT = g->bpad * d.nt;
+    // K steps of 32 bytes in a type's last k-block (the contraction length is 2L per type)
+    const int ksl = (int)((d.twoL - (tkb - 1) * kKBlock + 31) / 32);
     g->kb = kb;
     g->d_err = oz.d_error;
     g->sf_tab = d.sf_tab;
@@ -2083,6 +2097,7 @@ static int group_prepare_sf(OzakiPlan &oz, const OzGroupDesc &d, const std::vect
             j.lrow0 = t * d.twoL; j.rrow0 = g->row0[k];
             j.rk0 = t * g->bpad;
             j.nkb = tkb;
+            j.ksteps_last = ksl;
             j.m = d.twoL; j.n = kb[k].G;
             j.out = kb[k].Z + d.twoL * t; j.ldo = d.twoL * d.nt;
             j.el = g->dT.expo + t * d.twoL; j.er = g->dM.expo + g->row0[k];
@@ -2113,6 +2128,7 @@ static int group_prepare_sf(OzakiPlan &oz, const OzGroupDesc &d, const std::vect
                 j.lrow0 = g->row0[k]; j.rrow0 = g->row0[k];
                 j.lk0 = t * g->bpad; j.rk0 = t * g->bpad;
                 j.nkb = tkb;
+                j.ksteps_last = ksl;
                 j.m = kb[k].G; j.n = kb[k].G;
                 j.out = (which == 0 ? kb[k].PS : kb[k].PH) + (t % g->tbatch) * kb[k].pstride;
                 j.ldo = kb[k].G;

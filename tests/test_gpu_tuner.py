@@ -54,13 +54,16 @@ def test_first_run_tunes_tiles_and_reports_them(ctx):
     pl2.close()
 
 
+@pytest.mark.parametrize("cfg", ["c0", "t1"])
 @pytest.mark.parametrize("halves,merge", [("1", "1"), ("2", "0"), ("1", "0")])
-def test_every_tile_configuration_matches_oracle(ctx, halves, merge):
+def test_every_tile_configuration_matches_oracle(ctx, cfg, halves, merge):
+    """c0 (2L = 98: whole k-blocks) and t1 (2L = 50: the 256 x 256 accumulators stop the
+    k-block after two K steps)."""
     env = {"HSDLA_PAIR_HALVES": halves, "HSDLA_MERGE": merge}
     old = {k: os.environ.get(k) for k in env}
     os.environ.update(env)
     try:
-        s = synth.make_system("c0")
+        s = synth.make_system(cfg)
         res, rep = ctx.create_hs(s, precision="ozaki", num_slices=11)
     finally:
         for k, v in old.items():
@@ -69,11 +72,11 @@ def test_every_tile_configuration_matches_oracle(ctx, halves, merge):
             else:
                 os.environ[k] = v
     assert rep["tile_halves"] == int(halves) and rep["merged_units"] == int(merge) and rep["tile_tuned"] == 0
-    (H, S), = res
-    Hr, Sr = oracle.reference_hs(s, s.kpoints[0])
-    for X, R in ((H, Hr), (S, Sr)):
-        fro, mx = oracle.lower_errors(X, R)
-        assert fro < TOL and mx < TOL, (halves, merge, fro, mx)
+    for (H, S), kp in zip(res, s.kpoints):
+        Hr, Sr = oracle.reference_hs(s, kp)
+        for X, R in ((H, Hr), (S, Sr)):
+            fro, mx = oracle.lower_errors(X, R)
+            assert fro < TOL and mx < TOL, (cfg, halves, merge, fro, mx)
 
 
 def test_graph_is_recaptured_with_the_tuned_tiles(ctx):
