@@ -124,3 +124,40 @@ def test_outputs_written_in_place(ctx, precision, batch, monkeypatch):
         for X, R in ((H, Hr), (S, Sr)):
             assert np.array_equal(X[il], R[il])
             assert np.all(X[iu] == complex(7.0, -3.0))
+
+
+def test_streamed_outputs_of_a_kpoint_group(ctx, monkeypatch):
+    """Page-locked outputs of a group of three k-points with different basis sizes: the column-block
+    launches run over every k-point's tiles, each block's columns go to the host (diagonal square
+    in place, the rest by the copy engine) per k-point, and the lower triangles equal, bit for bit,
+    the download into pageable buffers; the strict upper triangles stay untouched; the oracle
+    agrees on the k-point with the fewest G-vectors."""
+    torch = pytest.importorskip("torch")
+    cfg = dict(synth.CONFIGS["c1"], kpts=[(0.1, 0.2, 0.3), (0.0, 0.0, 0.0), (0.25, -0.25, 0.5)],
+               n_g=(2600, 3000))
+    s = synth.make_system(cfg)
+    assert len({kp.n_g for kp in s.kpoints}) > 1
+    monkeypatch.setenv("HSDLA_TYPE_BATCH", "8")
+    res_ref, rep_ref = ctx.create_hs(s, precision="ozaki", num_slices=11)
+    assert rep_ref["outputs_in_place"] == 0
+    outs, keep = [], []
+    for kp in s.kpoints:
+        pair = []
+        for _ in range(2):
+            t = torch.full((kp.n_g, kp.n_g), complex(7.0, -3.0), dtype=torch.complex128).pin_memory()
+            keep.append(t)
+            pair.append(t.numpy().T)
+        outs.append(tuple(pair))
+    res, rep = ctx.create_hs(s, precision="ozaki", num_slices=11, out=outs)
+    assert rep["outputs_in_place"] == 1 and rep["output_blocks"] > 1, rep
+    for (H, S), (Hr, Sr), kp in zip(res, res_ref, s.kpoints):
+        il = np.tril_indices(kp.n_g)
+        iu = np.triu_indices(kp.n_g, 1)
+        for X, R in ((H, Hr), (S, Sr)):
+            assert np.array_equal(X[il], R[il])
+            assert np.all(X[iu] == complex(7.0, -3.0))
+    k = int(np.argmin([kp.n_g for kp in s.kpoints]))
+    Ho, So = oracle.reference_hs(s, s.kpoints[k])
+    for X, R in ((res[k][0], Ho), (res[k][1], So)):
+        fro, mx = oracle.lower_errors(X, R)
+        assert fro < TOL and mx < TOL, (fro, mx)
