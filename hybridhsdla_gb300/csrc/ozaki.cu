@@ -1423,21 +1423,24 @@ bool use_pair() {
 
 // Accumulation units of a pair launch (see PairUnits).  Diagonals t and t + 1 share a unit when
 // the left operand carries the 2^-5-scaled planes, each fits one K-chunk, and either the sum
-// stays exact -- every partial sum a multiple of 2^-5 below 2^19, with |sum| <= nkb 128 x 2
-// (re/im) x 256 (|product|) x (n_t + n_{t+1} / 32) -- or t >= kLooseT, where even an FP32
+// stays exact -- every partial sum a multiple of 2^-5 below 2^19, with |sum| <= K x 2 (re/im) x
+// 256 (|product|) x (n_t + n_{t+1} / 32), K the contraction bytes that can hold nonzero digits
+// (kvalid, at most nkb 128: the slicer writes zero digits past 2L in each type's k-blocks, so the
+// per-type products of lmax 8 (2L = 162) count 162, not 256) -- or t >= kLooseT, where even an FP32
 // rounding (2^-24 of the sum) stays far below the result's FP64 precision.  The low-order
 // diagonals are not small everywhere: in a Gram element (S_gg) the products d_p(M_k) d_p(W_k) of
 // rows with w_k = 1 add up with one sign, so diagonal 2p carries ~K 2^8 2^(2-10p) whatever the
 // size of S_gg -- from t = 9 on below 2^-26 of S_gg, and exact here anyway (|sum| ~ 2^14).
 constexpr int kLooseT = 9;
-PairUnits pair_units(int s, int64_t nkb, bool merge) {
+PairUnits pair_units(int s, int64_t nkb, bool merge, int64_t kvalid = 0) {
     PairUnits p;
     memset(&p, 0, sizeof(p));
     auto pairs = [&](int t) { return std::min(s, t - 1) - std::max(1, t - s) + 1; };
+    const int64_t K = kvalid > 0 ? std::min(kvalid, nkb * kKBlock) : nkb * kKBlock;
     for (int t = 2; t <= s + 1;) {
         bool m = false;
         if (merge && t + 1 <= s + 1 && chunk_kblocks(pairs(t)) >= nkb && chunk_kblocks(pairs(t + 1)) >= nkb) {
-            const int64_t bound = nkb * kKBlock * 2 * 256;
+            const int64_t bound = K * 2 * 256;
             m = t >= kLooseT || bound * (32 * pairs(t) + pairs(t + 1)) <= ((int64_t)1 << 24);
         }
         p.t[p.n] = (int8_t)t;
@@ -2106,14 +2109,14 @@ static int group_prepare_sf(OzakiPlan &oz, const OzGroupDesc &d, const std::vect
     g->n_jobs_t = (int)jt.size();
     // on pair tiles (256 x 256: one tile row per type) in merged accumulation units
     rc = upload_schedule(jt, g->d_jobs_t, g->d_list_t, g->tiles_t, g->pair ? kPairTile : kTileN);
-    g->units_t = g->pair ? pair_units(s, tkb, env_int("HSDLA_MERGE", 1) != 0) : pair_units_plain(s);
+    g->units_t = g->pair ? pair_units(s, tkb, env_int("HSDLA_MERGE", 1) != 0, d.twoL) : pair_units_plain(s);
     if (rc) return fail(rc);
     g->maps_t[0] = g->halves_t == 2 ? g->dM.map64 : g->dM.map;  // right operand
     g->maps_t[1] = g->dM.map; g->maps_t[2] = g->dM.map; g->maps_t[3] = g->dT.map;
     // per type: S_t = M_t^H diag(w_t) M_t and H_t = M_t^H Z_t into the products; on pair tiles
     // with merged accumulation units (HSDLA_MERGE=0: one per diagonal)
     g->merged = env_int("HSDLA_MERGE", 1) != 0;
-    g->units = g->pair ? pair_units(s, tkb, g->merged) : pair_units_plain(s);
+    g->units = g->pair ? pair_units(s, tkb, g->merged, d.twoL) : pair_units_plain(s);
     const int64_t tile = g->pair ? kPairTile : kTileN;
     g->n_jobs_sh = 2 * g->nk;
     std::vector<OzJob> all;
@@ -2609,7 +2612,7 @@ int ozaki_group_run(OzGroup *g, const DevSystem &sys, const KTable &ktab, cudaSt
 static void set_sh_tiles(OzGroup *g, int halves, bool merged) {
     g->halves = halves;
     g->merged = merged;
-    g->units = pair_units(g->s, g->bpad / kKBlock, merged);
+    g->units = pair_units(g->s, g->bpad / kKBlock, merged, g->twoL);
     g->maps_sh[1] = halves == 2 ? g->dW.map64 : g->dW.map;
     g->maps_sh[2] = halves == 2 ? g->dX.map64 : g->dX.map;
 }
