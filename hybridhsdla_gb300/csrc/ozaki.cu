@@ -1664,36 +1664,8 @@ int64_t schedule_capacity_lower(int64_t n) {
 
 int64_t ozaki_herkx_workspace(int s, int64_t K, int64_t n) {
     const int64_t Kpad = round_up(std::max<int64_t>(K, 1), kKBlock);
-    return 2 * operand_bytes(s, n, Kpad) + 4096 + 4096 + round_up(sizeof(int4) * schedule_capacity_lower(n), 1024);
-}
-
-int ozaki_herkx(OzakiPlan &oz, const double2 *P, int64_t ldp, const double2 *Q, int64_t ldq, const double *w,
-                int64_t K, int64_t n, double2 *out, int64_t ldo, void *ws, cudaStream_t st, int *launches) {
-    const int s = oz.num_slices;
-    const int64_t Kpad = round_up(std::max<int64_t>(K, 1), kKBlock);
-    Arena ar{reinterpret_cast<char *>(ws)};
-    DigitOperand dp, dq;
-    carve_operand(ar, dp, s, n, Kpad);
-    carve_operand(ar, dq, s, n, Kpad);
-    OzJob *d_jobs = ar.take<OzJob>(4);
-    int4 *d_list = ar.take<int4>(schedule_capacity_lower(n));
-    cudaError_t e = slice(P, ldp, nullptr, K, n, Kpad, Kpad, s, dp, st);
-    if (e == cudaSuccess) e = slice(Q, ldq, w, K, n, Kpad, Kpad, s, dq, st);
-    if (e != cudaSuccess) { g_oz_err = cudaGetErrorString(e); return HSDLA_ERR_CUDA; }
-    int rc = make_map(dp, s);
-    if (!rc) rc = make_map(dq, s);
-    if (rc) return rc;
-    CUtensorMap maps[4] = {dp.map, dq.map, dp.map, dp.map};
-    std::vector<OzJob> jobs(1);
-    OzJob &j = jobs[0];
-    memset(&j, 0, sizeof(j));
-    j.lmap = 0; j.rmap = 1; j.lower = 1;
-    j.lplane = dp.plane_rows; j.rplane = dq.plane_rows;
-    j.nkb = Kpad / kKBlock; j.m = n; j.n = n;
-    j.out = out; j.ldo = ldo; j.el = dp.expo; j.er = dq.expo;
-    rc = launch_gemm(jobs, maps, s, oz.d_error, d_jobs, st, nullptr, nullptr, d_list);
-    if (launches) *launches = 3;
-    return rc;
+    return 2 * operand_bytes(s, n, Kpad) + 4096 + 4096 + round_up(sizeof(int4) * schedule_capacity_lower(n), 1024) +
+           round_up(sizeof(int) * kProgressCap, 1024);
 }
 
 // ---------------------------------------------------------------- k-point groups
@@ -1880,6 +1852,49 @@ cudaError_t launch_prepared(const CUtensorMap *maps, int s, int *d_err, const Oz
 }
 
 }  // namespace
+
+// P^H diag(w) Q (lower triangle) for one pair of K x n operands: the contraction behind
+// hsdla_zherkx_lower and the BLAS-shaped plugin.
+int ozaki_herkx(OzakiPlan &oz, const double2 *P, int64_t ldp, const double2 *Q, int64_t ldq, const double *w,
+                int64_t K, int64_t n, double2 *out, int64_t ldo, void *ws, cudaStream_t st, int *launches) {
+    const int s = oz.num_slices;
+    const int64_t Kpad = round_up(std::max<int64_t>(K, 1), kKBlock);
+    Arena ar{reinterpret_cast<char *>(ws)};
+    DigitOperand dp, dq;
+    carve_operand(ar, dp, s, n, Kpad);
+    carve_operand(ar, dq, s, n, Kpad);
+    OzJob *d_jobs = ar.take<OzJob>(4);
+    int4 *d_list = ar.take<int4>(schedule_capacity_lower(n));
+    cudaError_t e = slice(P, ldp, nullptr, K, n, Kpad, Kpad, s, dp, st);
+    if (e == cudaSuccess) e = slice(Q, ldq, w, K, n, Kpad, Kpad, s, dq, st);
+    if (e != cudaSuccess) { g_oz_err = cudaGetErrorString(e); return HSDLA_ERR_CUDA; }
+    int rc = make_map(dp, s);
+    if (!rc) rc = make_map(dq, s);
+    if (rc) return rc;
+    CUtensorMap maps[4] = {dp.map, dq.map, dp.map, dp.map};
+    std::vector<OzJob> jobs(1);
+    OzJob &j = jobs[0];
+    memset(&j, 0, sizeof(j));
+    j.lmap = 0; j.rmap = 1; j.lower = 1;
+    j.lplane = dp.plane_rows; j.rplane = dq.plane_rows;
+    j.nkb = Kpad / kKBlock; j.m = n; j.n = n;
+    j.out = out; j.ldo = ldo; j.el = dp.expo; j.er = dq.expo;
+    if (use_pair()) {
+        // CTA-pair 256 x 256 tiles with 256 x 256 accumulators, one exact unit per diagonal and
+        // K chunk (no merged units: the left operand has no scaled planes), pairs in lockstep
+        int *d_progress = ar.take<int>(kProgressCap);
+        int64_t tiles = 0;
+        rc = upload_schedule(jobs, d_jobs, d_list, tiles, kPairTile);
+        if (rc) return rc;
+        const cudaError_t el = launch_pair(maps, s, oz.d_error, d_jobs, 1, tiles, d_list, d_progress, st,
+                                           pair_units(s, j.nkb, false), 1);
+        if (el != cudaSuccess) { g_oz_err = cudaGetErrorString(el); return HSDLA_ERR_CUDA; }
+    } else {
+        rc = launch_gemm(jobs, maps, s, oz.d_error, d_jobs, st, nullptr, nullptr, d_list);
+    }
+    if (launches) *launches = 3;
+    return rc;
+}
 
 // Run-time scratch of a group (digit planes and exponents, rewritten by every run; groups of a
 // plan share it) and its persistent part (T digits, job tables, tile schedules, lockstep slots).
