@@ -38,8 +38,10 @@ def _exact_limit(s):
     return 2 ** (5 * ((s + 1) // 2) - 2)
 
 
-@pytest.mark.parametrize("n,K,s", [(128, 128, 3), (200, 300, 5), (300, 1000, 7)])
+@pytest.mark.parametrize("n,K,s", [(128, 128, 3), (200, 300, 5), (300, 1000, 7), (3000, 2000, 5)])
 def test_ozaki_exact_on_integer_operands(ctx, n, K, s):
+    """Integer operands that the kept digits represent exactly give the exact product, bit for
+    bit; n = 3000 spans 78 CTA-pair tiles (more than one wave, a ragged last tile row)."""
     import torch
     rng = np.random.default_rng(n + K)
     lim = _exact_limit(s)
