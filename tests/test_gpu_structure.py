@@ -161,3 +161,21 @@ def test_streamed_outputs_of_a_kpoint_group(ctx, monkeypatch):
     for X, R in ((res[k][0], Ho), (res[k][1], So)):
         fro, mx = oracle.lower_errors(X, R)
         assert fro < TOL and mx < TOL, (fro, mx)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "ozaki"])
+@pytest.mark.parametrize("sf", [True, False])
+@pytest.mark.parametrize("cfg,lmaxs", [("t1", (4, 2, 3)), ("c0", (6, 4))])
+def test_types_with_different_lmax_match_oracle(ctx, cfg, lmaxs, precision, sf):
+    """Types of one system with different lmax (the reference's per-atom lmaxs,
+    h_and_s_stripped_v2.cpp:64-86: the rows l > lmax of an atom are zero), in both forms."""
+    s = synth.make_system(cfg)
+    s.type_lmax = np.asarray(lmaxs, np.int32)
+    s.type_lmax_nonsph = np.asarray(lmaxs, np.int32)
+    res, rep = _run(ctx, s, precision, sf)
+    assert (rep["num_row_sets"] > 0) == sf
+    for (H, S), kp in zip(res, s.kpoints):
+        Hr, Sr = oracle.reference_hs(s, kp)
+        for X, R in ((H, Hr), (S, Sr)):
+            fro, mx = oracle.lower_errors(X, R)
+            assert fro < TOL and mx < TOL, (cfg, precision, sf, fro, mx)
