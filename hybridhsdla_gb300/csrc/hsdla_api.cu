@@ -949,7 +949,14 @@ int64_t group_persist_bytes(const hsdla_plan *pl, const std::vector<int> &kidx) 
     if (pl->opts.precision == HSDLA_PREC_OZAKI_FP8)
         return ozaki_group_persist_bytes(pl->oz.num_slices, 2 * (int64_t)pl->L, pl->na, pl->nt, G,
                                          pl->sf ? std::max(pl->panels, pl->nt) : pl->panels);
-    return 4096 + (int64_t)sizeof(Fp64Job) * (int64_t)kidx.size() * (std::max(pl->na, pl->nt) + 4);
+    // the FP64 group keeps two job tables, each rounded up to 1 KiB: the T applications (one per
+    // type when hoisted, else one per atom, per k-point) and the S/H products (two per type in
+    // the structure-factor form, else two, per k-point)
+    const int64_t nk = (int64_t)kidx.size();
+    const int64_t n_t = nk * (pl->hoist ? pl->nt : pl->na);
+    const int64_t n_sh = nk * 2 * (pl->sf ? pl->nt : 1);
+    auto up = [](int64_t b) { return (b + 1023) / 1024 * 1024; };
+    return up((int64_t)sizeof(Fp64Job) * n_t) + up((int64_t)sizeof(Fp64Job) * n_sh);
 }
 
 // Device-memory budget for one group's workspace: HSDLA_WORKSPACE_BUDGET (bytes), else 85% of
@@ -1187,6 +1194,9 @@ int prepare_groups(hsdla_plan *pl, void *ws, cudaStream_t st) {
             g.n_jobs_t = (int)jt.size();
             g.d_jobs_t = reinterpret_cast<Fp64Job *>(keep(sizeof(Fp64Job) * jt.size()));
             g.d_jobs_sh = reinterpret_cast<Fp64Job *>(keep(sizeof(Fp64Job) * jsh.size()));
+            if (pp - reinterpret_cast<char *>(g.persist) > g.persist_bytes)
+                return set_err(ctx, HSDLA_ERR_NOMEM, "job tables (%lld bytes) exceed the group's %lld persistent bytes",
+                               (long long)(pp - reinterpret_cast<char *>(g.persist)), (long long)g.persist_bytes);
             if (cudaHostAlloc((void **)&g.h_jobs_sh, sizeof(Fp64Job) * jsh.size(), cudaHostAllocDefault) != cudaSuccess) {
                 g.h_jobs_sh = nullptr;
                 return set_err(ctx, HSDLA_ERR_NOMEM, "pinned job table allocation failed");

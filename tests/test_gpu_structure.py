@@ -179,3 +179,29 @@ def test_types_with_different_lmax_match_oracle(ctx, cfg, lmaxs, precision, sf):
         for X, R in ((H, Hr), (S, Sr)):
             fro, mx = oracle.lower_errors(X, R)
             assert fro < TOL and mx < TOL, (cfg, precision, sf, fro, mx)
+
+
+EDGE_CONFIGS = {
+    # lmax 12 and 14 (2L = 338 and 450 per type: 3 and 4 contraction blocks, other unit plans)
+    "lmax12": dict(cell=(10.0, 10.0, 12.0), atoms=4, types=2, rmt=2.0, min_sep=4.2, lmax=12,
+                   kpts=[(0.1, 0.2, 0.3)], n_g=300, seed=21),
+    "lmax14": dict(cell=(10.0, 10.0, 12.0), atoms=3, types=2, rmt=2.0, min_sep=4.2, lmax=14,
+                   kpts=[(0.05, 0.15, 0.25)], n_g=260, seed=22),
+    # twelve types of one atom each: every structure factor a single phase
+    "types12": dict(cell=(14.0, 14.0, 14.0), atoms=12, types=12, rmt=1.8, min_sep=3.8, lmax=4,
+                    kpts=[(0.1, 0.2, 0.3), (0.0, 0.0, 0.0)], n_g=(400, 520), seed=23),
+}
+
+
+@pytest.mark.parametrize("precision", ["fp64", "ozaki"])
+@pytest.mark.parametrize("sf", [True, False])
+@pytest.mark.parametrize("name", sorted(EDGE_CONFIGS))
+def test_edge_shapes_match_oracle(ctx, name, precision, sf):
+    s = synth.make_system(EDGE_CONFIGS[name])
+    res, rep = _run(ctx, s, precision, sf)
+    assert (rep["num_row_sets"] > 0) == sf
+    for (H, S), kp in zip(res, s.kpoints):
+        Hr, Sr = oracle.reference_hs(s, kp)
+        for X, R in ((H, Hr), (S, Sr)):
+            fro, mx = oracle.lower_errors(X, R)
+            assert fro < TOL and mx < TOL, (name, precision, sf, kp.n_g, fro, mx)
