@@ -637,6 +637,27 @@ __device__ __forceinline__ void mma_f8_pair(uint32_t d_tmem, uint64_t adesc, uin
         "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
         : "memory");
 }
+// The same MMA with the left operand's collector buffer: kFill reads A from shared memory and
+// keeps it for the next MMA, which (kFill = false: lastuse) takes A from the buffer and frees it.
+template <bool kFill>
+__device__ __forceinline__ void mma_f8_pair_ca(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                               uint32_t accumulate) {
+    if constexpr (kFill)
+        asm volatile(
+            "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+            " tcgen05.mma.cta_group::2.kind::f8f6f4.collector::a::fill [%0], %1, %2, %3, p;\n}\n" ::"r"(d_tmem),
+            "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+            : "memory");
+    else
+        asm volatile(
+            "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+            " tcgen05.mma.cta_group::2.kind::f8f6f4.collector::a::lastuse [%0], %1, %2, %3, p;\n}\n" ::"r"(d_tmem),
+            "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+            : "memory");
+}
+#ifndef HSDLA_COLLECTOR_A
+#define HSDLA_COLLECTOR_A 1
+#endif
 __device__ __forceinline__ void mma_commit_pair(uint64_t *bar) {
     const uint16_t both = 3;
     asm volatile(
@@ -853,10 +874,22 @@ __global__ void __launch_bounds__(kPairThreads, 1)
                                         auto step = [&](uint32_t kk) {
                                             const uint64_t o = 2u * kk;
                                             const uint32_t acc = first ? 0u : 1u;
+#if HSDLA_COLLECTOR_A
+                                            // the two MMAs of the real left plane back to back, the
+                                            // second taking A from the collector buffer.  (Not for
+                                            // the imaginary plane: an MMA that reads A from the
+                                            // collector does not apply the negate-A bit, measured:
+                                            // the -A_im B_re term came out as +A_im B_re.)
+                                            mma_f8_pair_ca<true>(d_re, dar + o, dbr + o, id_pos, acc);
+                                            mma_f8_pair_ca<false>(d_im, dar + o, dbi + o, id_pos, acc);
+                                            mma_f8_pair(d_re, dai + o, dbi + o, id_pos, 1u);
+                                            mma_f8_pair(d_im, dai + o, dbr + o, id_neg, 1u);
+#else
                                             mma_f8_pair(d_re, dar + o, dbr + o, id_pos, acc);
                                             mma_f8_pair(d_re, dai + o, dbi + o, id_pos, 1u);
                                             mma_f8_pair(d_im, dar + o, dbi + o, id_pos, acc);
                                             mma_f8_pair(d_im, dai + o, dbr + o, id_neg, 1u);
+#endif
                                             first = false;
                                         };
                                         // whole blocks as straight-line code (a bound in this loop slowed the
