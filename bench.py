@@ -312,7 +312,7 @@ def run_ours(args):
     ctx.create_hs(sys_, kpoints=[kp], precision="ozaki", num_slices=args.slices, tmats=tmats, out=outs_h)  # warm
     torch.cuda.synchronize()
     e2e_steps = max(1, min(args.steps, args.e2e_calls))
-    e2e_calls, e2e_dev, e2e_dom = [], [], []
+    e2e_calls, e2e_dev, e2e_dom, e2e_host = [], [], [], []
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
         tc = time.perf_counter()
@@ -321,6 +321,7 @@ def run_ours(args):
         e2e_calls.append((time.perf_counter() - tc) * 1e3)
         e2e_dev.append(rep_e["ms_total"])
         e2e_dom.append(rep_e["ms_dominant"])
+        e2e_host.append(rep_e["ms_host_setup"])
     e2e_s = (time.perf_counter() - t0) / e2e_steps
     e2e_s = _max_over_ranks(ws, e2e_s)
     e2e_flop = sys_.flop_per_kpoint(G)
@@ -455,6 +456,8 @@ def run_ours(args):
                         # traffic): a slow call whose products kept their time was slowed on the
                         # host side or its link
                         "calls_dominant_ms": [round(x, 2) for x in e2e_dom],
+                        # per call, the host's plan creation and set-up before the first launch
+                        "calls_host_setup_ms": [round(x, 2) for x in e2e_host],
                         "median_ms": float(np.median(e2e_calls)),
                         "outputs": ("written in place by the combine in %d column blocks while the products "
                                     "of the next block ran" % rep_e["output_blocks"]) if rep_e["output_blocks"]

@@ -74,7 +74,7 @@ class ReportStruct(ctypes.Structure):
                 ("outputs_in_place", ctypes.c_int32), ("num_row_sets", ctypes.c_int32),
                 ("rotation_classes", ctypes.c_int32), ("tile_halves", ctypes.c_int32),
                 ("merged_units", ctypes.c_int32), ("tile_tuned", ctypes.c_int32), ("output_blocks", ctypes.c_int32),
-                ("reserved", ctypes.c_int32 * 1)]
+                ("reserved", ctypes.c_int32 * 1), ("ms_host_setup", ctypes.c_double)]
 
     def as_dict(self) -> dict:
         return {f: getattr(self, f) for f, _ in self._fields_ if f != "reserved"}

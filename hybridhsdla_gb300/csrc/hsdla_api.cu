@@ -1127,6 +1127,13 @@ int prepare_groups(hsdla_plan *pl, void *ws, cudaStream_t st) {
             char *oz_ws = reinterpret_cast<char *>((reinterpret_cast<uintptr_t>(p) + 1023) & ~uintptr_t(1023));
             int rc = ozaki_group_prepare(pl->oz, d, kb, oz_ws, g.persist, st, &g.oz);
             if (rc) return set_err(ctx, rc, "group set-up failed: %s", ozaki_last_error());
+            // streamed host output runs the S/H products as one launch per column block: an event
+            // pair for each, where there are more blocks than types
+            const size_t nev = 2 * (size_t)ozaki_group_output_blocks(g.oz);
+            while (pl->sf && g.ev_dom.size() < nev) {
+                g.ev_dom.push_back(nullptr);
+                CUDA_TRY(ctx, cudaEventCreate(&g.ev_dom.back()));
+            }
             g.ev_t.assign(2 * ozaki_group_tapply_events(g.oz), nullptr);
             for (auto &e : g.ev_t) CUDA_TRY(ctx, cudaEventCreate(&e));
         } else {
@@ -1910,6 +1917,7 @@ int hsdla_create_hs(hsdla_context *ctx, const hsdla_system *s, const hsdla_kpoin
         rep->eff_tflops = ms_dev > 0 ? pl->flop / (ms_dev * 1e-3) / 1e12 : 0.0;
         rep->outputs_in_place = dl.in_place ? 1 : 0;
         rep->output_blocks = dl.blocks;
+        rep->ms_host_setup = t_plan + t_setup;
     }
     const clk::time_point t_destroy = clk::now();
     hsdla_plan_destroy(pl);

@@ -2602,6 +2602,12 @@ int ozaki_group_run(OzGroup *g, const DevSystem &sys, const KTable &ktab, cudaSt
                 nl += 1;
             }
         }
+        // event pairs past the types (kept for the streamed form's column blocks) span nothing,
+        // after the S/H launches (the last event closes the group's products)
+        for (int p = g->nt; nev >= 2 * g->nt && p < nev / 2 && e == cudaSuccess; ++p) {
+            e = record(ev[2 * p], st);
+            if (e == cudaSuccess) e = record(ev[2 * p + 1], st);
+        }
         if (launches) *launches = nl;
         if (e != cudaSuccess) { g_oz_err = cudaGetErrorString(e); return HSDLA_ERR_CUDA; }
         return HSDLA_OK;

@@ -138,6 +138,8 @@ typedef struct hsdla_report {
     int32_t output_blocks;       /* hsdla_create_hs, outputs written in place: the column blocks they were written
                                     in while the digit products of the next block ran (0 = after all products) */
     int32_t reserved[1];
+    double ms_host_setup;        /* hsdla_create_hs: host time from the call's start to its first launch (plan
+                                    creation and set-up; the device is idle meanwhile, and ms_total counts it) */
 } hsdla_report;
 
 typedef struct hsdla_context hsdla_context;

@@ -37,7 +37,7 @@ def test_struct_layouts_match_header():
     assert ctypes.sizeof(api.SystemStruct) == 4 * 4 + 8 + 9 * 8 + 13 * 8
     assert ctypes.sizeof(api.KpointStruct) == 3 * 8 + 8 + 8
     assert ctypes.sizeof(api.OptsStruct) == 48
-    assert ctypes.sizeof(api.ReportStruct) == 10 * 8 + 12 * 4
+    assert ctypes.sizeof(api.ReportStruct) == 11 * 8 + 12 * 4
 
 
 def _header_fields(struct_name):
