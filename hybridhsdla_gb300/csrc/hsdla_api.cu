@@ -23,6 +23,7 @@
 #include <mutex>
 #include <set>
 #include <string>
+#include <thread>
 #include <tuple>
 #include <vector>
 
@@ -712,8 +713,14 @@ int hsdla_plan_create(hsdla_context *ctx, const hsdla_system *s, const hsdla_kpo
     if (!ctx || !out) return HSDLA_ERR_ARG;
     *out = nullptr;
     CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+    // HSDLA_TRACE=1: host time of the creation's phases on stderr
+    using pclk = std::chrono::steady_clock;
+    const bool ptrace = env_flag("HSDLA_TRACE", false);
+    const pclk::time_point p0 = pclk::now();
+    const auto pms = [&]() { return std::chrono::duration<double, std::milli>(pclk::now() - p0).count(); };
     int rc = validate(ctx, s, kpts, nk);
     if (rc) return rc;
+    const double p_valid = pms();
     // atoms with rotations: (type, rotation) classes keep the structure-factor form where they
     // shrink the work (HSDLA_SF=0 or HSDLA_CLASSES=0 keeps the per-atom form)
     const char *sf_env0 = getenv("HSDLA_SF");
@@ -791,6 +798,7 @@ int hsdla_plan_create(hsdla_context *ctx, const hsdla_system *s, const hsdla_kpo
         add(sizeof(double2) * (int64_t)na * (ext[0] + ext[1] + ext[2]));
         add(sizeof(double2) * (int64_t)nt * ext[0] * ext[1] * ext[2]);
     }
+    const double p_tables = pms();
     rc = ctx_malloc(ctx, &pl->tables, bytes);
     if (rc) { delete pl; return rc; }
     pl->tables_bytes = bytes;
@@ -809,9 +817,13 @@ int hsdla_plan_create(hsdla_context *ctx, const hsdla_system *s, const hsdla_kpo
     if (!stage) { pageable.reset(new char[std::max<int64_t>(upload_bytes, 1)]); stage = pageable.get(); }
     char *hp = stage;
     char *dp = reinterpret_cast<char *>(pl->tables);
+    // copies of 256 KB and more (the T blocks) are made together below, on several threads
+    struct Pending { char *dst; const char *src; int64_t n; };
+    std::vector<Pending> pend;
     auto put = [&](const void *src, int64_t b) -> void * {
         void *d = dp;
-        if (b > 0 && src) memcpy(hp, src, b);
+        if (b >= (int64_t)1 << 18 && src) pend.push_back({hp, reinterpret_cast<const char *>(src), b});
+        else if (b > 0 && src) memcpy(hp, src, b);
         const int64_t adv = (b + 255) & ~int64_t(255);
         hp += adv; dp += adv;
         return d;
@@ -890,6 +902,35 @@ int hsdla_plan_create(hsdla_context *ctx, const hsdla_system *s, const hsdla_kpo
         pl->sf_tab = (double2 *)dev_only(sizeof(double2) * (int64_t)nt * ext[0] * ext[1] * ext[2]);
     }
     std::vector<unsigned long long> tstats((size_t)5 * nt, 0);
+    {
+        // the pending copies as one byte range split evenly over up to four threads (one copying
+        // thread moves ~25 GB/s on the GB300 machine's host, 0.25 ms for c2's 6 MB of T blocks)
+        int64_t tot = 0;
+        for (const auto &q : pend) tot += q.n;
+        auto copy_range = [&](int64_t lo, int64_t hi) {
+            int64_t off = 0;
+            for (const auto &q : pend) {
+                const int64_t a = std::max(lo, off), b = std::min(hi, off + q.n);
+                if (a < b) memcpy(q.dst + (a - off), q.src + (a - off), (size_t)(b - a));
+                off += q.n;
+            }
+        };
+        const int nth = tot >= ((int64_t)4 << 20) ? 4 : 1;
+        const int64_t per = (tot + nth - 1) / nth;
+        std::vector<std::thread> th;
+        int started = 0;              // threads 1..started copy ranges 1..started
+        try {
+            for (int t = 1; t < nth; ++t) {
+                th.emplace_back(copy_range, std::min(tot, t * per), std::min(tot, (t + 1) * per));
+                ++started;
+            }
+        } catch (...) {               // a thread that cannot start leaves its ranges to this one
+        }
+        copy_range(0, std::min(tot, per));
+        if (started + 1 < nth) copy_range(std::min(tot, (started + 1) * per), tot);
+        for (auto &x : th) x.join();
+    }
+    const double p_staged = pms();
     cudaError_t e = cudaMemcpyAsync(pl->tables, stage, upload_bytes, cudaMemcpyHostToDevice, ctx->stream);
     if (e == cudaSuccess) e = cudaMemsetAsync(d_stats, 0, sizeof(unsigned long long) * 5 * nt, ctx->stream);
     if (e == cudaSuccess) e = launch_tfull(d_taa, d_tab, d_tbb, nt, L, pl->Tfull, d_stats, ctx->stream);
@@ -900,11 +941,18 @@ int hsdla_plan_create(hsdla_context *ctx, const hsdla_system *s, const hsdla_kpo
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(tstats.data(), d_stats, sizeof(unsigned long long) * 5 * nt, cudaMemcpyDeviceToHost,
                             ctx->stream);
+    const double p_enq = pms();
     if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
     if (e != cudaSuccess) {
         hsdla_plan_destroy(pl);
         return set_err(ctx, HSDLA_ERR_CUDA, "table upload failed: %s", cudaGetErrorString(e));
     }
+    if (ptrace)
+        fprintf(stderr,
+                "hsdla_plan_create: validate %.3f, host tables %.3f, staging %.3f, enqueue %.3f, device wait %.3f ms "
+                "(%lld bytes uploaded)\n",
+                p_valid, p_tables - p_valid, p_staged - p_tables, p_enq - p_staged, pms() - p_enq,
+                (long long)upload_bytes);
     rc = check_tmats(ctx, tstats, nt, use_classes ? &cls.class_type : nullptr);
     if (rc) { hsdla_plan_destroy(pl); return rc; }
     if (pl->opts.precision == HSDLA_PREC_OZAKI_FP8) {
@@ -1565,10 +1613,14 @@ int hsdla_plan_execute(hsdla_plan *pl, hsdla_cx *const *dH, hsdla_cx *const *dS,
     rc = ctx_workspace(ctx, hsdla_plan_workspace_bytes(pl), &ws);
     if (rc) return rc;
     if (pl->prepared_ws != ws) {
+        const auto q0 = std::chrono::steady_clock::now();
         CUDA_TRY(ctx, cudaStreamSynchronize(st));
         release_groups(pl);
         rc = prepare_groups(pl, ws, st);
         if (rc) { release_groups(pl); return rc; }
+        if (env_flag("HSDLA_TRACE", false))
+            fprintf(stderr, "hsdla_plan_execute: group set-up %.3f ms (host, before the first launch)\n",
+                    std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - q0).count());
         if (pl->tiles_tuned)
             for (auto &g : pl->groups) ozaki_group_set_tiles(g.oz, pl->tile_h, pl->tile_m);
     }

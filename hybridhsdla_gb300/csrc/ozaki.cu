@@ -2122,8 +2122,7 @@ static int group_prepare_sf(OzakiPlan &oz, const OzGroupDesc &d, const std::vect
     g->panels = 1;
     SliceTab tT = slice_table(d.Tfull, d.twoL, nullptr, d.twoL, d.nt * d.twoL, d.twoL, g->bpad, s, g->dT);
     tT.scaled = g->pair ? 1 : 0;
-    cudaError_t e = slice_launch(tT, st);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    cudaError_t e = slice_launch(tT, st);    // stream-ordered before every use of the T digits
     if (e != cudaSuccess) { g_oz_err = cudaGetErrorString(e); return fail(HSDLA_ERR_CUDA); }
     int rc = make_map(g->dM, g->pair ? 2 * s : s);
     if (!rc) rc = make_map(g->dW, s);
