@@ -461,10 +461,13 @@ __global__ void __launch_bounds__(kTfThreads) tfull_kernel(const double2 *__rest
         if (!isfinite(x.x) || !isfinite(x.y)) flags |= 2u;
         if (!isfinite(b.x) || !isfinite(b.y)) flags |= 4u;
         const bool low = r >= c;
-        out[r + n * c] = low ? a : make_double2(aT.x, -aT.y);
-        out[(L + r) + n * (L + c)] = low ? b : make_double2(bT.x, -bT.y);
-        out[r + n * (L + c)] = x;
-        out[(L + r) + n * c] = make_double2(xT.x, -xT.y);
+        // a non-finite entry is flagged above and assembled as zero, so that nothing downstream
+        // (the digit slicing above all) meets it before the flag is read
+        auto fin = [](double2 v) { return (isfinite(v.x) && isfinite(v.y)) ? v : make_double2(0.0, 0.0); };
+        out[r + n * c] = fin(low ? a : make_double2(aT.x, -aT.y));
+        out[(L + r) + n * (L + c)] = fin(low ? b : make_double2(bT.x, -bT.y));
+        out[r + n * (L + c)] = fin(x);
+        out[(L + r) + n * c] = fin(make_double2(xT.x, -xT.y));
         if (low) {
             // |T|^2 of the pair and |T - T^H|^2 (the mirror element is the pair's other half)
             st[0] = max(st[0], bits(fmax(a.x * a.x + a.y * a.y, aT.x * aT.x + aT.y * aT.y)));

@@ -128,6 +128,11 @@ struct hsdla_plan {
     // the structure factors SF_t over the box of G-vector differences
     bool sf = false;
     int classes = 0;                 // (type, rotation) classes the structure-factor form runs over (0: types)
+    // T-block check read after the call's own synchronisation (hsdla_create_hs): the device's
+    // statistics land in the context's page-locked staging, checked once the stream is idle
+    bool tcheck_pending = false;
+    const unsigned long long *tcheck_host = nullptr;
+    std::vector<int32_t> tcheck_class_type;
     double *wt = nullptr;
     double2 *sf_tab = nullptr;
     SfTab sf_dims{};                 // box extents and offsets (entries filled per group)
@@ -708,8 +713,27 @@ int hsdla_prepare_tmat(int32_t lmax, int32_t lmax_nonsph, const hsdla_cx *taa, c
     return HSDLA_OK;
 }
 
+}  // extern "C"
+
+namespace {
+int plan_create_impl(hsdla_context *ctx, const hsdla_system *s, const hsdla_kpoint *kpts, int32_t nk,
+                     const hsdla_opts *opts, hsdla_plan **out, bool defer_tcheck);
+}
+
+extern "C" {
+
 int hsdla_plan_create(hsdla_context *ctx, const hsdla_system *s, const hsdla_kpoint *kpts, int32_t nk,
                       const hsdla_opts *opts, hsdla_plan **out) {
+    return plan_create_impl(ctx, s, kpts, nk, opts, out, false);
+}
+
+}  // extern "C"
+
+namespace {
+// defer_tcheck: leave the T-block check to the caller (after its own synchronisation), so that the
+// device runs on while the host sets up the execution
+int plan_create_impl(hsdla_context *ctx, const hsdla_system *s, const hsdla_kpoint *kpts, int32_t nk,
+                     const hsdla_opts *opts, hsdla_plan **out, bool defer_tcheck) {
     if (!ctx || !out) return HSDLA_ERR_ARG;
     *out = nullptr;
     CUDA_TRY(ctx, cudaSetDevice(ctx->device));
@@ -804,11 +828,14 @@ int hsdla_plan_create(hsdla_context *ctx, const hsdla_system *s, const hsdla_kpo
     pl->tables_bytes = bytes;
     // staging of the uploaded part, page-locked and kept by the context (pageable if pinning
     // fails); left uninitialised: every byte that matters is written
-    if (ctx->staging_bytes < upload_bytes) {
+    // (the T-block statistics come back behind the uploaded part)
+    const int64_t stats_off = (upload_bytes + 255) & ~int64_t(255);
+    const int64_t stage_need = stats_off + (int64_t)sizeof(unsigned long long) * 5 * nt;
+    if (ctx->staging_bytes < stage_need) {
         if (ctx->staging) cudaFreeHost(ctx->staging);
         ctx->staging = nullptr;
         ctx->staging_bytes = 0;
-        const int64_t want = std::max<int64_t>(upload_bytes, (int64_t)1 << 20);
+        const int64_t want = std::max<int64_t>(stage_need, (int64_t)1 << 20);
         if (cudaHostAlloc(&ctx->staging, (size_t)want, cudaHostAllocDefault) == cudaSuccess) ctx->staging_bytes = want;
         else { cudaGetLastError(); ctx->staging = nullptr; }
     }
@@ -938,11 +965,14 @@ int hsdla_plan_create(hsdla_context *ctx, const hsdla_system *s, const hsdla_kpo
     if (e == cudaSuccess && pl->sf)
         e = launch_sf_table(d_ex, d_ex + (size_t)na * ext[0], d_ex + (size_t)na * (ext[0] + ext[1]), d_order,
                             d_order + na, nt, ext[0], ext[1], ext[2], pl->sf_tab, ctx->stream);
+    const bool defer = defer_tcheck && ctx->staging != nullptr;
+    unsigned long long *stats_host =
+        defer ? reinterpret_cast<unsigned long long *>(reinterpret_cast<char *>(ctx->staging) + stats_off) : tstats.data();
     if (e == cudaSuccess)
-        e = cudaMemcpyAsync(tstats.data(), d_stats, sizeof(unsigned long long) * 5 * nt, cudaMemcpyDeviceToHost,
+        e = cudaMemcpyAsync(stats_host, d_stats, sizeof(unsigned long long) * 5 * nt, cudaMemcpyDeviceToHost,
                             ctx->stream);
     const double p_enq = pms();
-    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (e == cudaSuccess && !defer) e = cudaStreamSynchronize(ctx->stream);
     if (e != cudaSuccess) {
         hsdla_plan_destroy(pl);
         return set_err(ctx, HSDLA_ERR_CUDA, "table upload failed: %s", cudaGetErrorString(e));
@@ -953,8 +983,14 @@ int hsdla_plan_create(hsdla_context *ctx, const hsdla_system *s, const hsdla_kpo
                 "(%lld bytes uploaded)\n",
                 p_valid, p_tables - p_valid, p_staged - p_tables, p_enq - p_staged, pms() - p_enq,
                 (long long)upload_bytes);
-    rc = check_tmats(ctx, tstats, nt, use_classes ? &cls.class_type : nullptr);
-    if (rc) { hsdla_plan_destroy(pl); return rc; }
+    if (defer) {
+        pl->tcheck_pending = true;
+        pl->tcheck_host = stats_host;
+        if (use_classes) pl->tcheck_class_type = cls.class_type;
+    } else {
+        rc = check_tmats(ctx, tstats, nt, use_classes ? &cls.class_type : nullptr);
+        if (rc) { hsdla_plan_destroy(pl); return rc; }
+    }
     if (pl->opts.precision == HSDLA_PREC_OZAKI_FP8) {
         pl->autotune = pl->opts.num_slices == 0;
         rc = ozaki_plan_init(pl->oz, pl->opts.num_slices, pl->opts.target_rel_err);
@@ -965,7 +1001,7 @@ int hsdla_plan_create(hsdla_context *ctx, const hsdla_system *s, const hsdla_kpo
     return HSDLA_OK;
 }
 
-}  // extern "C"
+}  // namespace
 
 namespace {
 
@@ -1614,7 +1650,8 @@ int hsdla_plan_execute(hsdla_plan *pl, hsdla_cx *const *dH, hsdla_cx *const *dS,
     if (rc) return rc;
     if (pl->prepared_ws != ws) {
         const auto q0 = std::chrono::steady_clock::now();
-        CUDA_TRY(ctx, cudaStreamSynchronize(st));
+        // groups prepared before may still be in use by queued work (a fresh plan has none)
+        if (pl->prepared_ws) CUDA_TRY(ctx, cudaStreamSynchronize(st));
         release_groups(pl);
         rc = prepare_groups(pl, ws, st);
         if (rc) { release_groups(pl); return rc; }
@@ -1889,7 +1926,8 @@ int hsdla_create_hs(hsdla_context *ctx, const hsdla_system *s, const hsdla_kpoin
     CUDA_TRY(ctx, cudaEventCreate(&e1));
     cudaEventRecord(e0, ctx->stream);
     hsdla_plan *pl = nullptr;
-    int rc = hsdla_plan_create(ctx, s, kpts, nk, opts, &pl);
+    // the T blocks' check read after the launches (HSDLA_DEFER_TCHECK=0: before them)
+    int rc = plan_create_impl(ctx, s, kpts, nk, opts, &pl, env_flag("HSDLA_DEFER_TCHECK", true));
     t_plan = ms_since(t_start);
     if (rc) { cudaEventDestroy(e0); cudaEventDestroy(e1); return rc; }
     // device outputs: one buffer of the largest size, reused per k-point group
@@ -1963,6 +2001,13 @@ int hsdla_create_hs(hsdla_context *ctx, const hsdla_system *s, const hsdla_kpoin
     float ms_dev = 0.f;
     if (es == cudaSuccess) cudaEventElapsedTime(&ms_dev, e0, e1);
     if (rc == HSDLA_OK && es != cudaSuccess) rc = set_err(ctx, HSDLA_ERR_CUDA, "sync failed: %s", cudaGetErrorString(es));
+    if (pl->tcheck_pending && (rc == HSDLA_OK || es == cudaSuccess)) {
+        // the T blocks' check, deferred past the launches (their statistics are on the host now)
+        const int nt = pl->nt;
+        const std::vector<unsigned long long> st(pl->tcheck_host, pl->tcheck_host + 5 * (size_t)nt);
+        const int rct = check_tmats(ctx, st, nt, pl->tcheck_class_type.empty() ? nullptr : &pl->tcheck_class_type);
+        if (rct) rc = rct;
+    }
     if (rc == HSDLA_OK && rep) {
         rep->ms_total = ms_dev;   // end-to-end: upload, compute, download
         rep->ms_per_kpoint = nk ? ms_dev / nk : 0.0;

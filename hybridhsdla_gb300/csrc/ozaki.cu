@@ -1138,7 +1138,9 @@ __device__ __forceinline__ void write_part(const long long (&x)[kVec], int part,
         uint32_t w0 = 0, w1 = 0;
 #pragma unroll
         for (int v = 0; v < kVec; ++v) {
-            const int idx = i == 0 ? (int)u[v] + 16 : (int)(u[v] & 31);
+            // (the top digit of a finite row is in [-16, 16]; the clamp keeps the table read in
+            // bounds for any row)
+            const int idx = i == 0 ? min(max((int)u[v] + 16, 0), 32) : (int)(u[v] & 31);
             const uint32_t b = (uint32_t)g_e4m3_lut[idx] << (8 * (v & 3));
             if (v < 4) w0 |= b; else w1 |= b;
             u[v] >>= 5;

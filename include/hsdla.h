@@ -166,7 +166,9 @@ int hsdla_prepare_tmat(int32_t lmax, int32_t lmax_nonsph, const hsdla_cx *taa, c
 
 /* H and S for nk k-points, HOST buffers in and out (the create_HS2 drop-in; nk = 1 is
  * exactly create_HS2's contract, h_and_s.cpp:591-893).  H[i], S[i]: n_g(i) x n_g(i)
- * column-major host arrays with leading dimension ld[i] >= n_g(i). */
+ * column-major host arrays with leading dimension ld[i] >= n_g(i).  The T blocks' check
+ * (finite, Hermitian) is read after the launches: a call that returns HSDLA_ERR_INPUT for
+ * it may have written H and S. */
 int hsdla_create_hs(hsdla_context *ctx, const hsdla_system *sys, const hsdla_kpoint *kpts, int32_t nk,
                     hsdla_cx *const *H, hsdla_cx *const *S, const int64_t *ld,
                     const hsdla_opts *opts, hsdla_report *report);
