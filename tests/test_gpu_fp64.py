@@ -142,22 +142,25 @@ def test_rejects_non_hermitian_taa(ctx):
     assert e.value.code == -4
 
 
-def test_rejects_non_hermitian_tbb_and_nonfinite_tab(ctx):
+@pytest.mark.parametrize("precision", ["fp64", "ozaki"])
+def test_rejects_non_hermitian_tbb_and_nonfinite_tab(ctx, precision):
     """The T blocks are checked on the device as they are assembled: T_BB not Hermitian, or a
-    non-finite value in T_AB, is an input error naming the block, and the context stays usable."""
+    non-finite value in T_AB, is an input error naming the block, and the context stays usable.
+    hsdla_create_hs reads the check after its launches; the non-finite entry is assembled as
+    zero, so the Ozaki digit slicing of T and of T M meets finite values only."""
     s = synth.make_system("t0")
     base = oracle.prepare_tmats(s)
     tm = [x.copy() for x in base]
     tm[2][1, 3, 1] += 0.25j
     with pytest.raises(api.HsdlaError) as e:
-        ctx.create_hs(s, tmats=tuple(tm))
+        ctx.create_hs(s, tmats=tuple(tm), precision=precision)
     assert e.value.code == -4 and "T_BB of type 1 is not Hermitian" in str(e.value)
     tm = [x.copy() for x in base]
     tm[1][0, 2, 3] = np.nan
     with pytest.raises(api.HsdlaError) as e:
-        ctx.create_hs(s, tmats=tuple(tm))
+        ctx.create_hs(s, tmats=tuple(tm), precision=precision)
     assert e.value.code == -4 and "T block 1 of type 0 not finite" in str(e.value)
-    res, _ = ctx.create_hs(s, tmats=base)
+    res, _ = ctx.create_hs(s, tmats=base, precision=precision)
     assert np.isfinite(res[0][0]).all()
 
 
