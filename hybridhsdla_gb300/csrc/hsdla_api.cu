@@ -2016,6 +2016,23 @@ int hsdla_create_hs(hsdla_context *ctx, const hsdla_system *s, const hsdla_kpoin
         rep->output_blocks = dl.blocks;
         rep->ms_host_setup = t_plan + t_setup;
     }
+    if (trace && es == cudaSuccess) {
+        // the S/H launches on the call's device timeline (ms from its start): the gaps between
+        // them are the combines (and, streamed, the host writes of each block's diagonal square)
+        std::string tl;
+        for (const auto &g : pl->groups)
+            for (size_t i = 0; i + 1 < g.ev_dom.size(); i += 2) {
+                float a = 0.f, b = 0.f;
+                if (cudaEventElapsedTime(&a, e0, g.ev_dom[i]) == cudaSuccess &&
+                    cudaEventElapsedTime(&b, e0, g.ev_dom[i + 1]) == cudaSuccess && b > a) {
+                    char buf[48];
+                    snprintf(buf, sizeof(buf), " %.2f-%.2f", a, b);
+                    tl += buf;
+                }
+            }
+        cudaGetLastError();
+        fprintf(stderr, "hsdla_create_hs: S/H launches at%s of %.2f ms\n", tl.c_str(), ms_dev);
+    }
     const clk::time_point t_destroy = clk::now();
     hsdla_plan_destroy(pl);
     cudaEventDestroy(e0);
