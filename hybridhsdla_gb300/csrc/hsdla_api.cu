@@ -931,7 +931,8 @@ int plan_create_impl(hsdla_context *ctx, const hsdla_system *s, const hsdla_kpoi
     std::vector<unsigned long long> tstats((size_t)5 * nt, 0);
     {
         // the pending copies as one byte range split evenly over up to four threads (one copying
-        // thread moves ~25 GB/s on the GB300 machine's host, 0.25 ms for c2's 6 MB of T blocks)
+        // thread on a GB300's Grace host moves ~25 GB/s: 0.25 ms for the 6 MB of T blocks of 8
+        // types at lmax 10)
         int64_t tot = 0;
         for (const auto &q : pend) tot += q.n;
         auto copy_range = [&](int64_t lo, int64_t hi) {
