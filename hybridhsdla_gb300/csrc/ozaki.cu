@@ -554,8 +554,11 @@ constexpr int kLdCols = kLdColsPair();
 #ifndef HSDLA_PAIR_STAGING_KB
 #define HSDLA_PAIR_STAGING_KB 32
 #endif
+// Drain staging buffers per epilogue warp: one buffer of 4 columns (2 KB) per warp drains with
+// half the proxy fences and read-waits of two 2-column buffers; c2's per-type S/H launches took
+// 23.35-23.41 ms against 24.37-24.43 (two buffers) and 27.8 ms (four), same box, alternating builds.
 #ifndef HSDLA_DRAIN_BUFS
-#define HSDLA_DRAIN_BUFS 2
+#define HSDLA_DRAIN_BUFS 1
 #endif
 constexpr int kPairStages = HSDLA_PAIR_STAGES;
 constexpr int kPairStagesHalf = 4;          // 48 KB stages of the half-width tiles
