@@ -556,7 +556,7 @@ constexpr int kLdCols = kLdColsPair();
 #endif
 // Drain staging buffers per epilogue warp: one buffer of 4 columns (2 KB) per warp drains with
 // half the proxy fences and read-waits of two 2-column buffers; c2's per-type S/H launches took
-// 23.35-23.41 ms against 24.37-24.43 (two buffers) and 27.8 ms (four), same box, alternating builds.
+// 23.35-23.41 ms against 24.37-24.43 (two buffers) and 27.8 ms (four) on one GB300, builds alternating.
 #ifndef HSDLA_DRAIN_BUFS
 #define HSDLA_DRAIN_BUFS 1
 #endif
